@@ -1,0 +1,583 @@
+// C ABI of gbchol (include/gbchol.h): solver handle, factor upload, level
+// analysis, solves and refinement.
+//
+// Host-side counterpart of the reference's CholeskySolver<Float>
+// (src/cholesky_solver.h:22-99, src/cholesky_solver.cpp:152-486) and of the
+// CUDA driver shim (src/cuda_driver.cpp): this library links the CUDA
+// runtime directly and shares the primary context with PyTorch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "gbchol.h"
+#include "host/host.h"
+#include "kernels.h"
+#include "refine.h"
+
+using namespace gbchol;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) {
+            changed = cudaSetDevice(dev) == cudaSuccess;
+        }
+    }
+    ~DeviceGuard() {
+        if (changed) cudaSetDevice(prev);
+    }
+};
+
+#define CUDA_TRY(expr)                                                                     \
+    do {                                                                                   \
+        cudaError_t _e = (expr);                                                           \
+        if (_e != cudaSuccess)                                                             \
+            return fail(_e == cudaErrorMemoryAllocation ? GBCHOL_ENOMEM : GBCHOL_ECUDA,    \
+                        std::string("CUDA error: ") + cudaGetErrorString(_e) + " (" #expr   \
+                                                                               ")");        \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t count = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        count = 0;
+    }
+    cudaError_t alloc(size_t n) {
+        release();
+        if (n == 0) n = 1;
+        cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+        if (e == cudaSuccess) count = n;
+        else p = nullptr;
+        return e;
+    }
+    cudaError_t upload(const T* h, size_t n) {
+        cudaError_t e = alloc(n);
+        if (e != cudaSuccess || n == 0) return e;
+        return cudaMemcpy(p, h, n * sizeof(T), cudaMemcpyHostToDevice);
+    }
+};
+
+// One triangle (L or L^T) in CSR form with its level analysis.
+struct Triangle {
+    DevBuf<int32_t> rowptr, cols, order;
+    DevBuf<float> v32;
+    DevBuf<double> v64;
+    std::vector<int32_t> row_levels, order_h;
+    int32_t max_lvl = 0;
+};
+
+}  // namespace
+
+struct gbchol_host_factor {
+    Factor F;
+};
+
+struct gbchol_solver {
+    int device = 0;
+    int32_t n = 0;
+    int32_t store = 0;
+    Factor F;                 // host copy of the factor
+    int64_t nnz_a = 0;
+    double t_factor = 0.0, t_analysis = 0.0;
+    DevBuf<int32_t> perm;
+    Triangle lower, upper;    // CSR of L (diagonal last), CSR of L^T (diagonal first)
+    DevBuf<int32_t> a_rowptr, a_cols;
+    DevBuf<double> a_vals;    // symmetric A, original ordering
+    DevBuf<int32_t> flags, status;
+    DevBuf<int32_t> max_lvl;
+    int epoch = 0;
+    DevBuf<unsigned char> tmp;      // permuted-space work array
+    DevBuf<double> r64;             // refinement residual
+    DevBuf<double> partials;        // refinement block partial sums
+    DevBuf<RefineState> rstate;
+    cudaStream_t last_stream = nullptr;
+
+    int next_epoch(cudaStream_t s) {
+        if (epoch >= INT_MAX - 8) {
+            cudaMemsetAsync(flags.p, 0, sizeof(int32_t) * (size_t)std::max(n, 1), s);
+            epoch = 0;
+        }
+        return ++epoch;
+    }
+};
+
+namespace {
+
+// Validates a CSC factor: diagonal first and positive-free of structure
+// errors (sorted strictly increasing rows, all rows in [col, n)).
+int validate_factor(int32_t n, const int32_t* perm, const int32_t* colptr, const int32_t* rowidx) {
+    if (n < 0) return fail(GBCHOL_EINVAL, "Invalid factor: negative size.");
+    std::vector<char> seen((size_t)n, 0);
+    for (int32_t k = 0; k < n; ++k) {
+        if (perm[k] < 0 || perm[k] >= n || seen[perm[k]])
+            return fail(GBCHOL_EINVAL, "Invalid factor: perm is not a permutation.");
+        seen[perm[k]] = 1;
+    }
+    if (colptr[0] != 0) return fail(GBCHOL_EINVAL, "Invalid factor: colptr[0] != 0.");
+    for (int32_t j = 0; j < n; ++j) {
+        int32_t s = colptr[j], e = colptr[j + 1];
+        if (e <= s) return fail(GBCHOL_EINVAL, "Invalid factor: empty column (missing diagonal).");
+        if (rowidx[s] != j) return fail(GBCHOL_EINVAL, "Invalid factor: diagonal must come first.");
+        for (int32_t k = s + 1; k < e; ++k)
+            if (rowidx[k] <= rowidx[k - 1] || rowidx[k] >= n)
+                return fail(GBCHOL_EINVAL, "Invalid factor: row indices must be sorted and < n.");
+    }
+    return GBCHOL_OK;
+}
+
+// Fundamental supernodes of a factor pattern (for statistics and the
+// supernodal kernels): column j+1 continues j's supernode when it is j's
+// only child and has j's structure minus j.
+void detect_supernodes(Factor& F) {
+    const int32_t n = F.n;
+    F.parent.assign((size_t)n, -1);
+    std::vector<int32_t> nchild((size_t)n, 0);
+    for (int32_t j = 0; j < n; ++j) {
+        if (F.colptr[j + 1] - F.colptr[j] > 1) {
+            F.parent[j] = F.rowidx[F.colptr[j] + 1];
+            nchild[F.parent[j]]++;
+        }
+    }
+    F.sn_start.assign(1, 0);
+    for (int32_t j = 1; j < n; ++j) {
+        int32_t cp = F.colptr[j] - F.colptr[j - 1], cc = F.colptr[j + 1] - F.colptr[j];
+        bool merge = F.parent[j - 1] == j && cp == cc + 1 && nchild[j] == 1;
+        if (!merge) F.sn_start.push_back(j);
+    }
+    F.sn_start.push_back(n);
+}
+
+// Host counting sort of rows by level, stable in row id: the `levels` array
+// of the reference (src/cholesky_solver.cpp:349-367).
+void sort_by_level(const std::vector<int32_t>& lev, int32_t max_lvl, std::vector<int32_t>& order) {
+    const int32_t n = (int32_t)lev.size();
+    std::vector<int32_t> ptr((size_t)max_lvl + 2, 0);
+    for (int32_t i = 0; i < n; ++i) ptr[(size_t)lev[i] + 1]++;
+    for (int32_t l = 0; l <= max_lvl; ++l) ptr[(size_t)l + 1] += ptr[l];
+    order.resize((size_t)n);
+    for (int32_t i = 0; i < n; ++i) order[ptr[lev[i]]++] = i;
+}
+
+int analyze_triangle(gbchol_solver* h, Triangle& t, bool lower) {
+    const int32_t n = h->n;
+    DevBuf<int32_t> lev;
+    CUDA_TRY(lev.alloc((size_t)n));
+    CUDA_TRY(cudaMemset(h->max_lvl.p, 0, sizeof(int32_t)));
+    int ep = h->next_epoch(nullptr);
+    CUDA_TRY(launch_level_analysis(lower, n, t.rowptr.p, t.cols.p, lev.p, h->flags.p, ep,
+                                   h->max_lvl.p, h->status.p, nullptr));
+    CUDA_TRY(cudaDeviceSynchronize());
+    int32_t st = 0;
+    CUDA_TRY(cudaMemcpy(&st, h->status.p, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (st != 0) {
+        cudaMemset(h->status.p, 0, sizeof(int32_t));
+        return fail(GBCHOL_ETIMEOUT, "Level analysis: a device-side wait expired (malformed factor?).");
+    }
+    t.row_levels.resize((size_t)n);
+    CUDA_TRY(cudaMemcpy(t.row_levels.data(), lev.p, sizeof(int32_t) * (size_t)n,
+                        cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(&t.max_lvl, h->max_lvl.p, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    sort_by_level(t.row_levels, t.max_lvl, t.order_h);
+    CUDA_TRY(t.order.upload(t.order_h.data(), (size_t)n));
+    return GBCHOL_OK;
+}
+
+// Uploads the factor (both triangles) and runs the analysis.
+int setup_device(gbchol_solver* h) {
+    auto t0 = std::chrono::steady_clock::now();
+    const Factor& F = h->F;
+    const int32_t n = F.n;
+    CUDA_TRY(cudaGetDevice(&h->device));
+    CUDA_TRY(h->perm.upload(F.perm.data(), (size_t)n));
+    CUDA_TRY(h->flags.alloc((size_t)std::max(n, 1)));
+    CUDA_TRY(cudaMemset(h->flags.p, 0, sizeof(int32_t) * (size_t)std::max(n, 1)));
+    CUDA_TRY(h->status.alloc(1));
+    CUDA_TRY(cudaMemset(h->status.p, 0, sizeof(int32_t)));
+    CUDA_TRY(h->max_lvl.alloc(1));
+    // L^T in CSR is L in CSC (the reference's "upper" triangle, :280)
+    CUDA_TRY(h->upper.rowptr.upload(F.colptr.data(), (size_t)n + 1));
+    CUDA_TRY(h->upper.cols.upload(F.rowidx.data(), F.rowidx.size()));
+    // L in CSR (cholmod_transpose, :252): columns ascending, diagonal last
+    std::vector<int32_t> rp, ci;
+    std::vector<double> rv;
+    transpose(n, F.colptr, F.rowidx, F.vals, rp, ci, rv);
+    CUDA_TRY(h->lower.rowptr.upload(rp.data(), rp.size()));
+    CUDA_TRY(h->lower.cols.upload(ci.data(), ci.size()));
+    if (h->store & GBCHOL_STORE_F64) {
+        CUDA_TRY(h->lower.v64.upload(rv.data(), rv.size()));
+        CUDA_TRY(h->upper.v64.upload(F.vals.data(), F.vals.size()));
+    }
+    if (h->store & GBCHOL_STORE_F32) {
+        // FP64 -> FP32 cast on the host (src/cholesky_solver.cpp:257-271)
+        std::vector<float> f(rv.size());
+        for (size_t k = 0; k < rv.size(); ++k) f[k] = (float)rv[k];
+        CUDA_TRY(h->lower.v32.upload(f.data(), f.size()));
+        for (size_t k = 0; k < F.vals.size(); ++k) f[k] = (float)F.vals[k];
+        CUDA_TRY(h->upper.v32.upload(f.data(), f.size()));
+    }
+    if (n > 0) {
+        int rc = analyze_triangle(h, h->lower, true);
+        if (rc) return rc;
+        rc = analyze_triangle(h, h->upper, false);
+        if (rc) return rc;
+    }
+    CUDA_TRY(cudaDeviceSynchronize());
+    h->t_analysis = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return GBCHOL_OK;
+}
+
+int check_store(int32_t store) {
+    if ((store & ~(GBCHOL_STORE_F32 | GBCHOL_STORE_F64 | GBCHOL_STORE_A64)) != 0 ||
+        (store & (GBCHOL_STORE_F32 | GBCHOL_STORE_F64)) == 0)
+        return fail(GBCHOL_EINVAL, "Invalid storage flags.");
+    return GBCHOL_OK;
+}
+
+int ensure_tmp(gbchol_solver* h, size_t bytes) {
+    if (h->tmp.count >= bytes) return GBCHOL_OK;
+    CUDA_TRY(h->tmp.alloc(bytes));
+    return GBCHOL_OK;
+}
+
+int check_rhs(int32_t nrhs) {
+    if (nrhs > GBCHOL_MAX_RHS) return fail(GBCHOL_EINVAL, "The number of RHS should be less than 128.");
+    if (nrhs < 1) return fail(GBCHOL_EINVAL, "The number of RHS must be at least 1.");
+    return GBCHOL_OK;
+}
+
+RowSweepArgs sweep_args(gbchol_solver* h, const Triangle& t, bool f32, int nrhs) {
+    RowSweepArgs a;
+    a.n = h->n;
+    a.nrhs = nrhs;
+    a.rowptr = t.rowptr.p;
+    a.cols = t.cols.p;
+    a.vals = f32 ? (const void*)t.v32.p : (const void*)t.v64.p;
+    a.order = t.order.p;
+    a.perm = h->perm.p;
+    a.tmp = h->tmp.p;
+    a.flags = h->flags.p;
+    a.status = h->status.p;
+    return a;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbchol_last_error(void) { return g_last_error.c_str(); }
+
+const char* gbchol_version(void) { return "gbchol 0.1.0 (sm_103a)"; }
+
+int gbchol_create(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t* jj,
+                  const double* x, int32_t matrix_type, int32_t store, gbchol_handle* out) {
+    if (!out) return fail(GBCHOL_EINVAL, "out must not be NULL.");
+    *out = nullptr;
+    if (int rc = check_store(store)) return rc;
+    if (n_rows < 0) return fail(GBCHOL_EINVAL, "The number of rows must be non-negative.");
+    if (nnz > 0 && (!ii || !jj || !x)) return fail(GBCHOL_EINVAL, "Null input array.");
+    if (matrix_type != GBCHOL_COO && !ii) return fail(GBCHOL_EINVAL, "Null pointer array.");
+    std::unique_ptr<gbchol_solver> h(new (std::nothrow) gbchol_solver());
+    if (!h) return fail(GBCHOL_ENOMEM, "Out of host memory.");
+    h->n = n_rows;
+    h->store = store;
+    std::string err;
+    Csc A;
+    Status st = build_csc(n_rows, nnz, ii, jj, x, matrix_type, A, err);
+    if (st != ST_OK) return fail(GBCHOL_EINVAL, err);
+    auto t0 = std::chrono::steady_clock::now();
+    FactorOptions opt;
+    st = factorize(A, opt, h->F, err);
+    h->t_factor = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (st == ST_NOT_POSDEF) return fail(GBCHOL_ENOTPOSDEF, "Matrix is not positive definite!");
+    if (st != ST_OK) return fail(st == ST_NOMEM ? GBCHOL_ENOMEM : GBCHOL_EINVAL, err);
+    if (store & GBCHOL_STORE_A64) {
+        Csc S;
+        symmetric_from_lower(A, S);
+        h->nnz_a = S.nnz();
+        CUDA_TRY(h->a_rowptr.upload(S.colptr.data(), S.colptr.size()));
+        CUDA_TRY(h->a_cols.upload(S.rowidx.data(), S.rowidx.size()));
+        CUDA_TRY(h->a_vals.upload(S.vals.data(), S.vals.size()));
+    }
+    if (int rc = setup_device(h.get())) return rc;
+    *out = h.release();
+    return GBCHOL_OK;
+}
+
+int gbchol_create_from_factor(int32_t n, const int32_t* perm, const int32_t* colptr,
+                              const int32_t* rowidx, const double* vals, int32_t store,
+                              gbchol_handle* out) {
+    if (!out) return fail(GBCHOL_EINVAL, "out must not be NULL.");
+    *out = nullptr;
+    if (int rc = check_store(store & ~GBCHOL_STORE_A64)) return rc;
+    if (n < 0 || !perm || !colptr || (n > 0 && (!rowidx || !vals)))
+        return fail(GBCHOL_EINVAL, "Invalid factor arrays.");
+    if (int rc = validate_factor(n, perm, colptr, rowidx)) return rc;
+    std::unique_ptr<gbchol_solver> h(new (std::nothrow) gbchol_solver());
+    if (!h) return fail(GBCHOL_ENOMEM, "Out of host memory.");
+    h->n = n;
+    h->store = store & ~GBCHOL_STORE_A64;
+    Factor& F = h->F;
+    F.n = n;
+    F.perm.assign(perm, perm + n);
+    F.colptr.assign(colptr, colptr + n + 1);
+    F.rowidx.assign(rowidx, rowidx + colptr[n]);
+    F.vals.assign(vals, vals + colptr[n]);
+    detect_supernodes(F);
+    if (int rc = setup_device(h.get())) return rc;
+    *out = h.release();
+    return GBCHOL_OK;
+}
+
+int gbchol_factorize(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t* jj,
+                     const double* x, int32_t matrix_type, int32_t threads,
+                     gbchol_factor_handle* out) {
+    if (!out) return fail(GBCHOL_EINVAL, "out must not be NULL.");
+    *out = nullptr;
+    if (n_rows < 0) return fail(GBCHOL_EINVAL, "The number of rows must be non-negative.");
+    if (nnz > 0 && (!ii || !jj || !x)) return fail(GBCHOL_EINVAL, "Null input array.");
+    if (matrix_type != GBCHOL_COO && !ii) return fail(GBCHOL_EINVAL, "Null pointer array.");
+    std::unique_ptr<gbchol_host_factor> f(new (std::nothrow) gbchol_host_factor());
+    if (!f) return fail(GBCHOL_ENOMEM, "Out of host memory.");
+    std::string err;
+    Csc A;
+    Status st = build_csc(n_rows, nnz, ii, jj, x, matrix_type, A, err);
+    if (st != ST_OK) return fail(GBCHOL_EINVAL, err);
+    FactorOptions opt;
+    opt.threads = threads;
+    st = factorize(A, opt, f->F, err);
+    if (st == ST_NOT_POSDEF) return fail(GBCHOL_ENOTPOSDEF, "Matrix is not positive definite!");
+    if (st != ST_OK) return fail(st == ST_NOMEM ? GBCHOL_ENOMEM : GBCHOL_EINVAL, err);
+    *out = f.release();
+    return GBCHOL_OK;
+}
+
+int gbchol_factor_info(gbchol_factor_handle f, int32_t* n, int64_t* nnz_l, int32_t* n_supernodes,
+                       double* flops) {
+    if (!f) return fail(GBCHOL_EINVAL, "Null factor.");
+    if (n) *n = f->F.n;
+    if (nnz_l) *nnz_l = f->F.nnz();
+    if (n_supernodes) *n_supernodes = f->F.sn_start.empty() ? 0 : (int32_t)f->F.sn_start.size() - 1;
+    if (flops) *flops = f->F.flops;
+    return GBCHOL_OK;
+}
+
+int gbchol_factor_export(gbchol_factor_handle f, int32_t* perm, int32_t* colptr, int32_t* rowidx,
+                         double* vals) {
+    if (!f) return fail(GBCHOL_EINVAL, "Null factor.");
+    const Factor& F = f->F;
+    if (perm) std::copy(F.perm.begin(), F.perm.end(), perm);
+    if (colptr) std::copy(F.colptr.begin(), F.colptr.end(), colptr);
+    if (rowidx) std::copy(F.rowidx.begin(), F.rowidx.end(), rowidx);
+    if (vals) std::copy(F.vals.begin(), F.vals.end(), vals);
+    return GBCHOL_OK;
+}
+
+int gbchol_factor_free(gbchol_factor_handle f) {
+    delete f;
+    return GBCHOL_OK;
+}
+
+int gbchol_destroy(gbchol_handle h) {
+    if (!h) return GBCHOL_OK;
+    {
+        DeviceGuard g(h->device);
+        if (h->last_stream) cudaStreamSynchronize(h->last_stream);
+        delete h;
+    }
+    return GBCHOL_OK;
+}
+
+int gbchol_reserve(gbchol_handle h, int32_t nrhs) {
+    if (!h) return fail(GBCHOL_EINVAL, "Null handle.");
+    if (int rc = check_rhs(nrhs)) return rc;
+    DeviceGuard g(h->device);
+    size_t es = (h->store & GBCHOL_STORE_F64) ? sizeof(double) : sizeof(float);
+    return ensure_tmp(h, (size_t)std::max(h->n, 1) * nrhs * es);
+}
+
+int gbchol_solve(gbchol_handle h, int32_t precision, int32_t nrhs, const void* b, void* x,
+                 void* stream) {
+    if (!h) return fail(GBCHOL_EINVAL, "Null handle.");
+    if (int rc = check_rhs(nrhs)) return rc;
+    const bool f32 = precision == 0;
+    if (precision != 0 && precision != 1) return fail(GBCHOL_EINVAL, "precision must be 0 or 1.");
+    if (f32 && !(h->store & GBCHOL_STORE_F32))
+        return fail(GBCHOL_ESTATE, "This solver keeps no FP32 factor.");
+    if (!f32 && !(h->store & GBCHOL_STORE_F64))
+        return fail(GBCHOL_ESTATE, "This solver keeps no FP64 factor.");
+    if (h->n == 0) return GBCHOL_OK;
+    if (!b || !x) return fail(GBCHOL_EINVAL, "Null b or x.");
+    DeviceGuard g(h->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (int rc = ensure_tmp(h, (size_t)h->n * nrhs * (f32 ? sizeof(float) : sizeof(double)))) return rc;
+    const SweepIO io = f32 ? SweepIO::F32 : SweepIO::F64;
+    RowSweepArgs lo = sweep_args(h, h->lower, f32, nrhs);
+    lo.in = b;
+    lo.epoch = h->next_epoch(s);
+    CUDA_TRY(launch_row_sweep(lo, true, io, s));
+    RowSweepArgs up = sweep_args(h, h->upper, f32, nrhs);
+    up.out = x;
+    up.epoch = h->next_epoch(s);
+    CUDA_TRY(launch_row_sweep(up, false, io, s));
+    h->last_stream = s;
+    return GBCHOL_OK;
+}
+
+int gbchol_solve_refined(gbchol_handle h, int32_t nrhs, const double* b, double* x, double tol,
+                         int32_t max_iter, void* stream, gbchol_refine_stats* stats) {
+    if (!h) return fail(GBCHOL_EINVAL, "Null handle.");
+    if (int rc = check_rhs(nrhs)) return rc;
+    if ((h->store & (GBCHOL_STORE_F32 | GBCHOL_STORE_A64)) != (GBCHOL_STORE_F32 | GBCHOL_STORE_A64))
+        return fail(GBCHOL_ESTATE, "Refinement needs the FP32 factor and the FP64 matrix.");
+    if (max_iter < 0 || max_iter > 100) return fail(GBCHOL_EINVAL, "max_iter must be in [0, 100].");
+    if (!(tol >= 0.0)) return fail(GBCHOL_EINVAL, "tol must be non-negative.");
+    if (h->n == 0) {
+        if (stats) *stats = gbchol_refine_stats{0, 1, 0.0};
+        return GBCHOL_OK;
+    }
+    if (!b || !x) return fail(GBCHOL_EINVAL, "Null b or x.");
+    if ((const void*)b == (const void*)x) return fail(GBCHOL_EINVAL, "b and x must not alias for refinement.");
+    DeviceGuard g(h->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int n = h->n;
+    if (int rc = ensure_tmp(h, (size_t)n * nrhs * sizeof(float))) return rc;
+    if (h->r64.count < (size_t)n * nrhs) CUDA_TRY(h->r64.alloc((size_t)n * nrhs));
+    const int grid = residual_grid(n);
+    if (h->partials.count < (size_t)grid * 2 * nrhs) CUDA_TRY(h->partials.alloc((size_t)grid * 2 * GBCHOL_MAX_RHS));
+    if (!h->rstate.p) CUDA_TRY(h->rstate.alloc(1));
+    CUDA_TRY(cudaMemsetAsync(h->rstate.p, 0, sizeof(RefineState), s));
+    // x0 = A32^{-1} b
+    RowSweepArgs lo = sweep_args(h, h->lower, true, nrhs);
+    lo.in = b;
+    lo.epoch = h->next_epoch(s);
+    CUDA_TRY(launch_row_sweep(lo, true, SweepIO::F32_MIXED, s));
+    RowSweepArgs up = sweep_args(h, h->upper, true, nrhs);
+    up.out = x;
+    up.epoch = h->next_epoch(s);
+    CUDA_TRY(launch_row_sweep(up, false, SweepIO::F32_MIXED, s));
+    ResidualArgs ra;
+    ra.n = n;
+    ra.nrhs = nrhs;
+    ra.rowptr = h->a_rowptr.p;
+    ra.cols = h->a_cols.p;
+    ra.vals = h->a_vals.p;
+    ra.b = b;
+    ra.x = x;
+    ra.r = h->r64.p;
+    ra.partials = h->partials.p;
+    ra.state = h->rstate.p;
+    ra.tol = tol;
+    const int* conv = &h->rstate.p->converged;
+    // Each step: r = b - A x (and the stop decision), d = A32^{-1} r, x += d.
+    // Once converged, every later kernel returns at once.
+    for (int it = 0; it <= max_iter; ++it) {
+        ra.iter = it;
+        ra.first = it == 0;
+        CUDA_TRY(launch_residual(ra, grid, s));
+        if (it == max_iter) break;
+        RowSweepArgs l2 = sweep_args(h, h->lower, true, nrhs);
+        l2.in = h->r64.p;
+        l2.skip = conv;
+        l2.epoch = h->next_epoch(s);
+        CUDA_TRY(launch_row_sweep(l2, true, SweepIO::F32_REFINE, s));
+        RowSweepArgs u2 = sweep_args(h, h->upper, true, nrhs);
+        u2.out = x;
+        u2.skip = conv;
+        u2.epoch = h->next_epoch(s);
+        CUDA_TRY(launch_row_sweep(u2, false, SweepIO::F32_REFINE, s));
+    }
+    h->last_stream = s;
+    if (stats) {
+        RefineState hs;
+        CUDA_TRY(cudaMemcpyAsync(&hs, h->rstate.p, sizeof(RefineState), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        stats->iterations = hs.converged ? hs.iterations : max_iter;
+        stats->converged = hs.converged;
+        stats->max_rel_residual = hs.max_rel;
+    }
+    return GBCHOL_OK;
+}
+
+int gbchol_get_info(gbchol_handle h, gbchol_info* out) {
+    if (!h || !out) return fail(GBCHOL_EINVAL, "Null argument.");
+    gbchol_info i{};
+    i.n = h->n;
+    i.device = h->device;
+    i.nnz_a = h->nnz_a;
+    i.nnz_l = h->F.nnz();
+    i.levels_lower = h->n ? h->lower.max_lvl + 1 : 0;
+    i.levels_upper = h->n ? h->upper.max_lvl + 1 : 0;
+    i.n_supernodes = h->F.sn_start.empty() ? 0 : (int32_t)h->F.sn_start.size() - 1;
+    int32_t mx = 0;
+    for (size_t s = 0; s + 1 < h->F.sn_start.size(); ++s)
+        mx = std::max(mx, h->F.sn_start[s + 1] - h->F.sn_start[s]);
+    i.max_supernode = mx;
+    i.factor_flops = h->F.flops;
+    i.factor_seconds = h->t_factor;
+    i.analysis_seconds = h->t_analysis;
+    i.store = h->store;
+    *out = i;
+    return GBCHOL_OK;
+}
+
+int gbchol_get_levels(gbchol_handle h, int32_t lower, int32_t* row_levels, int32_t* order,
+                      int32_t* max_lvl) {
+    if (!h) return fail(GBCHOL_EINVAL, "Null handle.");
+    const Triangle& t = lower ? h->lower : h->upper;
+    if (row_levels) std::copy(t.row_levels.begin(), t.row_levels.end(), row_levels);
+    if (order) std::copy(t.order_h.begin(), t.order_h.end(), order);
+    if (max_lvl) *max_lvl = t.max_lvl;
+    return GBCHOL_OK;
+}
+
+int gbchol_get_factor(gbchol_handle h, int32_t* perm, int32_t* colptr, int32_t* rowidx,
+                      double* vals) {
+    if (!h) return fail(GBCHOL_EINVAL, "Null handle.");
+    const Factor& F = h->F;
+    if (perm) std::copy(F.perm.begin(), F.perm.end(), perm);
+    if (colptr) std::copy(F.colptr.begin(), F.colptr.end(), colptr);
+    if (rowidx) std::copy(F.rowidx.begin(), F.rowidx.end(), rowidx);
+    if (vals) std::copy(F.vals.begin(), F.vals.end(), vals);
+    return GBCHOL_OK;
+}
+
+int gbchol_check(gbchol_handle h) {
+    if (!h) return fail(GBCHOL_EINVAL, "Null handle.");
+    DeviceGuard g(h->device);
+    CUDA_TRY(cudaStreamSynchronize(h->last_stream));
+    int32_t st = 0;
+    CUDA_TRY(cudaMemcpy(&st, h->status.p, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (st != 0) {
+        CUDA_TRY(cudaMemset(h->status.p, 0, sizeof(int32_t)));
+        CUDA_TRY(cudaDeviceSynchronize());
+        return fail(GBCHOL_ETIMEOUT, "A device-side wait expired during a solve; results are invalid.");
+    }
+    return GBCHOL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,353 @@
+// Symbolic and numeric sparse LL^T factorisation on the host.
+//
+// Replaces the reference's CHOLMOD calls (src/cholesky_solver.cpp:200-297):
+// cholmod_analyze (ordering + symbolic) and cholmod_factorize (numeric, LL^T,
+// simplicial). The exported factor has exactly the simplicial symbolic
+// pattern (fundamental supernodes only, no amalgamation, so no explicit
+// zeros are added) and is laid out like cholmod_factor_to_sparse: CSC, rows
+// sorted, diagonal first in each column.
+//
+// Published methods followed (no CHOLMOD source used):
+//   * elimination tree: Liu's algorithm with path compression
+//     (J. W. H. Liu, "The role of elimination trees in sparse factorization",
+//     SIAM J. Matrix Anal. Appl. 11, 1990);
+//   * postorder of the elimination tree (same reference);
+//   * row-subtree traversal for the pattern of L (Davis, "Direct Methods for
+//     Sparse Linear Systems", SIAM 2006, section 4.2);
+//   * fundamental supernodes (Liu, Ng & Peyton, SIAM J. Matrix Anal. Appl.
+//     14, 1993);
+//   * multifrontal numeric factorisation (Duff & Reid 1983; Liu, SIAM Review
+//     34, 1992) with dense blocked kernels (dense.cpp).
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+#include "dense.h"
+#include "host.h"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace gbchol {
+
+namespace {
+
+int resolve_threads(int32_t t) {
+    if (t > 0) return t;
+#ifdef _OPENMP
+    return std::max(1, omp_get_max_threads());
+#else
+    return 1;
+#endif
+}
+
+// CSR pattern of the strictly lower triangle of P A P^T: row i lists the
+// columns j < i with a structural entry. Also returns the CSC of the lower
+// triangle with values (diagonal included) for numeric assembly.
+void permuted_lower(const Csc& A, const std::vector<int32_t>& pinv, std::vector<int32_t>& rptr,
+                    std::vector<int32_t>& rcol, std::vector<int32_t>& cptr,
+                    std::vector<int32_t>& crow, std::vector<double>& cval) {
+    const int32_t n = A.n;
+    rptr.assign((size_t)n + 1, 0);
+    cptr.assign((size_t)n + 1, 0);
+    for (int32_t c = 0; c < n; ++c)
+        for (int32_t k = A.colptr[c]; k < A.colptr[c + 1]; ++k) {
+            int32_t r = A.rowidx[k];
+            if (r < c) continue;  // upper part ignored (stype = -1)
+            int32_t pr = pinv[r], pc = pinv[c];
+            int32_t hi = std::max(pr, pc), lo = std::min(pr, pc);
+            cptr[lo + 1]++;
+            if (hi != lo) rptr[hi + 1]++;
+        }
+    for (int32_t i = 0; i < n; ++i) {
+        rptr[i + 1] += rptr[i];
+        cptr[i + 1] += cptr[i];
+    }
+    rcol.resize((size_t)rptr[n]);
+    crow.resize((size_t)cptr[n]);
+    cval.resize((size_t)cptr[n]);
+    std::vector<int32_t> rn(rptr.begin(), rptr.end() - 1), cn(cptr.begin(), cptr.end() - 1);
+    for (int32_t c = 0; c < n; ++c)
+        for (int32_t k = A.colptr[c]; k < A.colptr[c + 1]; ++k) {
+            int32_t r = A.rowidx[k];
+            if (r < c) continue;
+            int32_t pr = pinv[r], pc = pinv[c];
+            int32_t hi = std::max(pr, pc), lo = std::min(pr, pc);
+            int32_t d = cn[lo]++;
+            crow[d] = hi;
+            cval[d] = A.vals[k];
+            if (hi != lo) rcol[rn[hi]++] = lo;
+        }
+}
+
+// Liu's elimination tree from the strictly-lower CSR pattern.
+std::vector<int32_t> etree(int32_t n, const std::vector<int32_t>& rptr,
+                           const std::vector<int32_t>& rcol) {
+    std::vector<int32_t> parent((size_t)n, -1), anc((size_t)n, -1);
+    for (int32_t i = 0; i < n; ++i) {
+        for (int32_t k = rptr[i]; k < rptr[i + 1]; ++k) {
+            int32_t r = rcol[k];
+            while (r != -1 && r < i) {
+                int32_t nx = anc[r];
+                anc[r] = i;
+                if (nx == -1) { parent[r] = i; break; }
+                r = nx;
+            }
+        }
+    }
+    return parent;
+}
+
+// Postorder of a forest: children visited in increasing index order.
+std::vector<int32_t> postorder(const std::vector<int32_t>& parent) {
+    const int32_t n = (int32_t)parent.size();
+    std::vector<int32_t> head((size_t)n, -1), next((size_t)n, -1), post;
+    post.reserve((size_t)n);
+    for (int32_t j = n - 1; j >= 0; --j) {
+        if (parent[j] == -1) continue;
+        next[j] = head[parent[j]];
+        head[parent[j]] = j;
+    }
+    std::vector<int32_t> stack;
+    for (int32_t r = 0; r < n; ++r) {
+        if (parent[r] != -1) continue;
+        stack.push_back(r);
+        while (!stack.empty()) {
+            int32_t p = stack.back();
+            int32_t c = head[p];
+            if (c == -1) {
+                stack.pop_back();
+                post.push_back(p);
+            } else {
+                head[p] = next[c];
+                stack.push_back(c);
+            }
+        }
+    }
+    return post;
+}
+
+}  // namespace
+
+Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string& err) {
+    const int32_t n = A.n;
+    const int threads = resolve_threads(opt.threads);
+    F = Factor();
+    F.n = n;
+    if (n == 0) {
+        F.colptr.assign(1, 0);
+        F.sn_start.assign(1, 0);
+        return ST_OK;
+    }
+
+    // ---- ordering -------------------------------------------------------
+    std::vector<int32_t> perm0;
+    if (opt.use_given_perm) {
+        perm0.assign(opt.perm_in, opt.perm_in + n);
+        std::vector<char> seen((size_t)n, 0);
+        for (int32_t k = 0; k < n; ++k) {
+            if (perm0[k] < 0 || perm0[k] >= n || seen[perm0[k]]) {
+                err = "Invalid permutation.";
+                return ST_INVALID;
+            }
+            seen[perm0[k]] = 1;
+        }
+    } else {
+        // adjacency of the symmetric graph from the strictly lower part
+        std::vector<int32_t> xadj((size_t)n + 1, 0), adj;
+        for (int32_t c = 0; c < n; ++c)
+            for (int32_t k = A.colptr[c]; k < A.colptr[c + 1]; ++k) {
+                int32_t r = A.rowidx[k];
+                if (r <= c) continue;
+                xadj[r + 1]++;
+                xadj[c + 1]++;
+            }
+        for (int32_t i = 0; i < n; ++i) xadj[i + 1] += xadj[i];
+        adj.resize((size_t)xadj[n]);
+        std::vector<int32_t> nx(xadj.begin(), xadj.end() - 1);
+        for (int32_t c = 0; c < n; ++c)
+            for (int32_t k = A.colptr[c]; k < A.colptr[c + 1]; ++k) {
+                int32_t r = A.rowidx[k];
+                if (r <= c) continue;
+                adj[nx[r]++] = c;
+                adj[nx[c]++] = r;
+            }
+        perm0 = nested_dissection(n, xadj, adj);
+    }
+    std::vector<int32_t> pinv((size_t)n);
+    for (int32_t k = 0; k < n; ++k) pinv[perm0[k]] = k;
+
+    std::vector<int32_t> rptr, rcol, cptr, crow;
+    std::vector<double> cval;
+    permuted_lower(A, pinv, rptr, rcol, cptr, crow, cval);
+    std::vector<int32_t> parent = etree(n, rptr, rcol);
+
+    // ---- postorder and final permutation --------------------------------
+    {
+        std::vector<int32_t> post = postorder(parent);
+        F.perm.resize((size_t)n);
+        for (int32_t k = 0; k < n; ++k) F.perm[k] = perm0[post[k]];
+        for (int32_t k = 0; k < n; ++k) pinv[F.perm[k]] = k;
+    }
+    permuted_lower(A, pinv, rptr, rcol, cptr, crow, cval);
+    parent = etree(n, rptr, rcol);
+    F.parent = parent;
+
+    // ---- pattern of L by row subtrees -----------------------------------
+    std::vector<int32_t> mark((size_t)n, -1);
+    std::vector<int64_t> cnt((size_t)n, 1);  // diagonal
+    for (int32_t i = 0; i < n; ++i) {
+        mark[i] = i;
+        for (int32_t k = rptr[i]; k < rptr[i + 1]; ++k) {
+            for (int32_t r = rcol[k]; mark[r] != i; r = parent[r]) {
+                cnt[r]++;
+                mark[r] = i;
+            }
+        }
+    }
+    int64_t total = 0;
+    for (int32_t j = 0; j < n; ++j) total += cnt[j];
+    if (total >= (int64_t)INT32_MAX) {
+        err = "Factor too large: nnz(L) exceeds 2^31-1.";
+        return ST_NOMEM;
+    }
+    F.colptr.resize((size_t)n + 1);
+    F.colptr[0] = 0;
+    for (int32_t j = 0; j < n; ++j) F.colptr[j + 1] = F.colptr[j] + (int32_t)cnt[j];
+    F.rowidx.resize((size_t)total);
+    {
+        std::vector<int32_t> nxt(F.colptr.begin(), F.colptr.end() - 1);
+        std::fill(mark.begin(), mark.end(), -1);
+        for (int32_t i = 0; i < n; ++i) {
+            F.rowidx[nxt[i]++] = i;  // rows arrive in increasing order: diagonal first
+            mark[i] = i;
+            for (int32_t k = rptr[i]; k < rptr[i + 1]; ++k) {
+                for (int32_t r = rcol[k]; mark[r] != i; r = parent[r]) {
+                    F.rowidx[nxt[r]++] = i;
+                    mark[r] = i;
+                }
+            }
+        }
+    }
+
+    // ---- fundamental supernodes -----------------------------------------
+    std::vector<int32_t> nchild((size_t)n, 0);
+    for (int32_t j = 0; j < n; ++j)
+        if (parent[j] >= 0) nchild[parent[j]]++;
+    F.sn_start.clear();
+    F.sn_start.push_back(0);
+    for (int32_t j = 1; j < n; ++j) {
+        bool merge = parent[j - 1] == j && cnt[j - 1] == cnt[j] + 1 && nchild[j] == 1;
+        if (!merge) F.sn_start.push_back(j);
+    }
+    F.sn_start.push_back(n);
+    const int32_t nsn = (int32_t)F.sn_start.size() - 1;
+
+    // ---- multifrontal numeric factorisation -----------------------------
+    F.vals.assign((size_t)total, 0.0);
+    std::vector<int32_t> sn_of((size_t)n);
+    for (int32_t s = 0; s < nsn; ++s)
+        for (int32_t j = F.sn_start[s]; j < F.sn_start[s + 1]; ++j) sn_of[j] = s;
+    std::vector<int32_t> sn_nchild((size_t)nsn, 0);
+    for (int32_t s = 0; s < nsn; ++s) {
+        int32_t last = F.sn_start[s + 1] - 1;
+        if (parent[last] >= 0) sn_nchild[sn_of[parent[last]]]++;
+    }
+    struct Update {
+        int32_t sn;
+        std::vector<double> u;  // m x m, column-major, lower part valid
+    };
+    std::vector<Update> stack;
+    std::vector<int32_t> relpos((size_t)n, -1);
+    std::vector<double> front;
+    double flops = 0.0;
+    for (int32_t s = 0; s < nsn; ++s) {
+        const int32_t f = F.sn_start[s], l1 = F.sn_start[s + 1];
+        const int64_t w = l1 - f;
+        const int32_t* rows = F.rowidx.data() + F.colptr[f];
+        const int64_t Fsz = F.colptr[f + 1] - F.colptr[f];
+        const int64_t m = Fsz - w;
+        for (int64_t i = 0; i < Fsz; ++i) relpos[rows[i]] = (int32_t)i;
+        front.assign((size_t)(Fsz * Fsz), 0.0);
+        // assemble original entries of columns f..l1-1 (lower part)
+        for (int32_t j = f; j < l1; ++j) {
+            double* col = front.data() + (int64_t)(j - f) * Fsz;
+            for (int32_t k = cptr[j]; k < cptr[j + 1]; ++k) col[relpos[crow[k]]] += cval[k];
+        }
+        // extend-add the children's update matrices (top of the stack)
+        for (int32_t c = 0; c < sn_nchild[s]; ++c) {
+            Update& up = stack.back();
+            const int32_t cf = F.sn_start[up.sn];
+            const int32_t cw = F.sn_start[up.sn + 1] - cf;
+            const int32_t* crows = F.rowidx.data() + F.colptr[cf] + cw;
+            const int64_t cm = (F.colptr[cf + 1] - F.colptr[cf]) - cw;
+            for (int64_t jj = 0; jj < cm; ++jj) {
+                double* dst = front.data() + (int64_t)relpos[crows[jj]] * Fsz;
+                const double* src = up.u.data() + jj * cm;
+                for (int64_t ii = jj; ii < cm; ++ii) dst[relpos[crows[ii]]] += src[ii];
+            }
+            stack.pop_back();
+        }
+        // partial dense factorisation of the front
+        int64_t bad = dense::potrf_lower(w, front.data(), Fsz, threads);
+        if (bad >= 0) {
+            err = "Matrix is not positive definite!";
+            return ST_NOT_POSDEF;
+        }
+        if (m > 0) {
+            dense::trsm_right_lower_t(m, w, front.data(), Fsz, front.data() + w, Fsz, threads);
+            dense::gemm_nt_sub(m, m, w, front.data() + w, Fsz, front.data() + w, Fsz,
+                               front.data() + w + w * Fsz, Fsz, true, threads);
+        }
+        flops += (double)w * w * w / 3.0 + (double)m * w * w + (double)m * m * w;
+        // store the columns of L
+        for (int64_t j = 0; j < w; ++j) {
+            double* dst = F.vals.data() + F.colptr[f + j];
+            const double* src = front.data() + j + j * Fsz;
+            for (int64_t i = 0; i < Fsz - j; ++i) dst[i] = src[i];
+        }
+        if (m > 0 && parent[l1 - 1] >= 0) {
+            Update up;
+            up.sn = s;
+            up.u.resize((size_t)(m * m));
+            for (int64_t jj = 0; jj < m; ++jj) {
+                const double* src = front.data() + w + (w + jj) * Fsz;
+                std::copy(src + jj, src + m, up.u.data() + jj * m + jj);
+            }
+            stack.push_back(std::move(up));
+        }
+        for (int64_t i = 0; i < Fsz; ++i) relpos[rows[i]] = -1;
+    }
+    F.flops = flops;
+    return ST_OK;
+}
+
+void cpu_solve(const Factor& F, int32_t nrhs, const double* b, double* x, int32_t threads) {
+    const int32_t n = F.n;
+    if (n == 0 || nrhs <= 0) return;
+    const int nt = resolve_threads(threads);
+    // RHS columns are independent: split them across threads.
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 1) if (nt > 1 && nrhs > 1)
+    for (int32_t k = 0; k < nrhs; ++k) {
+        std::vector<double> y((size_t)n);
+        for (int32_t i = 0; i < n; ++i) y[i] = b[(int64_t)F.perm[i] * nrhs + k];
+        // forward: column-oriented L y = Pb
+        for (int32_t j = 0; j < n; ++j) {
+            const int32_t s = F.colptr[j], e = F.colptr[j + 1];
+            const double yj = y[j] / F.vals[s];
+            y[j] = yj;
+            for (int32_t p = s + 1; p < e; ++p) y[F.rowidx[p]] -= F.vals[p] * yj;
+        }
+        // backward: L^T z = y, row j of L^T is column j of L
+        for (int32_t j = n - 1; j >= 0; --j) {
+            const int32_t s = F.colptr[j], e = F.colptr[j + 1];
+            double acc = y[j];
+            for (int32_t p = s + 1; p < e; ++p) acc -= F.vals[p] * y[F.rowidx[p]];
+            y[j] = acc / F.vals[s];
+        }
+        for (int32_t i = 0; i < n; ++i) x[(int64_t)F.perm[i] * nrhs + k] = y[i];
+    }
+}
+
+}  // namespace gbchol

@@ -1,0 +1,92 @@
+// Host-side sparse preparation, fill-reducing ordering and numeric LL^T
+// factorisation. These stand in for the reference's host pipeline:
+//   - COO/CSR/CSC -> sorted, duplicate-free CSC   (src/cholesky_solver.cpp:8-149)
+//   - CHOLMOD simplicial LL^T with nested-dissection ordering
+//     (src/cholesky_solver.cpp:200-297; CHOLMOD itself is an absent submodule)
+// The output of factorize() is what the reference hands to its GPU code:
+// the permutation Perm and the factor L in CSC form with sorted row indices and
+// the diagonal first in each column (cholmod_factor_to_sparse).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace gbchol {
+
+enum MatrixFormat : int32_t { FMT_CSC = 0, FMT_CSR = 1, FMT_COO = 2 };
+
+// Status codes shared with the C ABI (include/gbchol.h).
+enum Status : int32_t {
+    ST_OK = 0,
+    ST_INVALID = 1,      // bad argument: maps to ValueError
+    ST_NOT_POSDEF = 2,   // factorisation hit a non-positive pivot: ValueError
+    ST_CUDA = 3,         // CUDA runtime error: RuntimeError
+    ST_NOMEM = 4,        // allocation failure: RuntimeError
+    ST_TIMEOUT = 5,      // a device-side wait ran out of budget: RuntimeError
+    ST_STATE = 6,        // call not valid for this handle: RuntimeError
+    ST_INTERNAL = 7,
+};
+
+struct Csc {
+    int32_t n = 0;
+    std::vector<int32_t> colptr;  // n+1
+    std::vector<int32_t> rowidx;  // nnz, sorted within each column
+    std::vector<double> vals;     // nnz
+    int64_t nnz() const { return (int64_t)rowidx.size(); }
+};
+
+// Builds a CSC matrix with row indices sorted inside each column and
+// duplicate entries summed (duplicates summed in input order). Validates all
+// indices. Follows coo_to_csc / csr_to_csc / csc_sort_indices /
+// csc_sum_duplicates (src/cholesky_solver.cpp:8-149).
+Status build_csc(int32_t n, int64_t nnz, const int32_t* ii, const int32_t* jj, const double* x,
+                 int32_t fmt, Csc& out, std::string& err);
+
+// Full symmetric matrix (both triangles, CSR == CSC since symmetric) built
+// from the lower triangle of A (row >= col), which is the only part CHOLMOD
+// reads for stype = -1 (src/cholesky_solver.cpp:211-220). Used by iterative
+// refinement (residual b - A x) and by the gradient.
+void symmetric_from_lower(const Csc& A, Csc& S);
+
+// Nested-dissection fill-reducing ordering of the symmetric graph given in
+// CSR adjacency form (no self loops). Returns perm with perm[k] = original
+// vertex placed at position k (CHOLMOD Perm convention).
+std::vector<int32_t> nested_dissection(int32_t n, const std::vector<int32_t>& xadj,
+                                       const std::vector<int32_t>& adj);
+
+struct Factor {
+    int32_t n = 0;
+    std::vector<int32_t> perm;    // perm[k] = original row at position k
+    std::vector<int32_t> colptr;  // CSC of L: n+1
+    std::vector<int32_t> rowidx;  // rows sorted, diagonal first
+    std::vector<double> vals;
+    std::vector<int32_t> parent;  // elimination tree of P A P^T (-1 = root)
+    std::vector<int32_t> sn_start;// fundamental supernodes: columns [sn_start[s], sn_start[s+1])
+    double flops = 0.0;           // numeric factorisation flop count
+    int64_t nnz() const { return (int64_t)rowidx.size(); }
+};
+
+struct FactorOptions {
+    int32_t threads = 0;          // 0 = all available
+    bool use_given_perm = false;  // take perm from `perm_in` instead of ordering
+    const int32_t* perm_in = nullptr;
+};
+
+// Symbolic + numeric LL^T of P A P^T, A given by its lower triangle (row >=
+// col entries of `A`; the upper part is ignored like CHOLMOD stype = -1).
+// Ordering: nested dissection followed by an elimination-tree postorder.
+// Numeric: supernodal multifrontal with dense blocked kernels. Returns
+// ST_NOT_POSDEF on a non-positive pivot (src/cholesky_solver.cpp:241-242).
+Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string& err);
+
+// Transpose of a CSC pattern+values (gives the CSR of L from its CSC).
+void transpose(int32_t n, const std::vector<int32_t>& colptr, const std::vector<int32_t>& rowidx,
+               const std::vector<double>& vals, std::vector<int32_t>& tptr,
+               std::vector<int32_t>& tidx, std::vector<double>& tvals);
+
+// Host LL^T solve on a factor in FP64 (the CPU-device solve of the reference,
+// src/cholesky_solver.cpp:435-463). b and x are row-major (n, nrhs) arrays;
+// they may alias.
+void cpu_solve(const Factor& F, int32_t nrhs, const double* b, double* x, int32_t threads);
+
+}  // namespace gbchol

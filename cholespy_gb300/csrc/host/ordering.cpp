@@ -1,0 +1,271 @@
+// Nested-dissection fill-reducing ordering (host).
+//
+// The reference orders with CHOLMOD's NESDIS (METIS multilevel nested
+// dissection, src/cholesky_solver.cpp:208-209). CHOLMOD/METIS are not
+// available, so this file implements nested dissection from the published
+// method (George 1973; George & Liu, "Computer Solution of Large Sparse
+// Positive Definite Systems", 1981):
+//   * separators come from the level structure of a breadth-first search
+//     rooted at a pseudo-peripheral vertex (the level set that best balances
+//     size against the two halves), then trimmed so that every separator
+//     vertex touches both halves;
+//   * each disconnected piece is ordered on its own;
+//   * pieces of at most 64 vertices are ordered by exact minimum degree
+//     (bit-set elimination graph).
+// Separator vertices are numbered after the two halves they split, so the
+// resulting permutation puts the top separator last.
+#include "host.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace gbchol {
+
+namespace {
+
+struct NDState {
+    int32_t n;
+    const std::vector<int32_t>& xadj;
+    const std::vector<int32_t>& adj;
+    std::vector<int32_t> verts;   // permutation under construction
+    std::vector<int32_t> tag;     // task label of each vertex
+    std::vector<int32_t> level;   // BFS level scratch
+    std::vector<int32_t> queue;
+    std::vector<int32_t> side;    // 0 = A, 1 = B, 2 = separator (scratch)
+    int32_t next_tag = 1;
+
+    NDState(int32_t n_, const std::vector<int32_t>& xa, const std::vector<int32_t>& ad)
+        : n(n_), xadj(xa), adj(ad), verts(n_), tag(n_, 0), level(n_, -1), queue(n_), side(n_, 0) {}
+
+    // BFS from `root` over vertices with tag t. Returns the number of
+    // vertices reached; fills queue[0..count) in BFS order and level[].
+    int32_t bfs(int32_t root, int32_t t, int32_t* depth_out) {
+        int32_t head = 0, tail = 0;
+        queue[tail++] = root;
+        level[root] = 0;
+        int32_t depth = 0;
+        while (head < tail) {
+            int32_t v = queue[head++];
+            int32_t lv = level[v];
+            depth = lv;
+            for (int32_t k = xadj[v]; k < xadj[v + 1]; ++k) {
+                int32_t u = adj[k];
+                if (tag[u] == t && level[u] < 0) {
+                    level[u] = lv + 1;
+                    queue[tail++] = u;
+                }
+            }
+        }
+        if (depth_out) *depth_out = depth;
+        return tail;
+    }
+    void clear_levels(int32_t count) {
+        for (int32_t i = 0; i < count; ++i) level[queue[i]] = -1;
+    }
+    int32_t degree_in(int32_t v, int32_t t) const {
+        int32_t d = 0;
+        for (int32_t k = xadj[v]; k < xadj[v + 1]; ++k) d += (tag[adj[k]] == t);
+        return d;
+    }
+
+    // Minimum-degree ordering of a piece of at most 64 vertices, written to
+    // verts[lo..hi) in elimination order.
+    void order_small(int32_t lo, int32_t hi, int32_t t) {
+        const int32_t m = hi - lo;
+        if (m <= 1) return;
+        int32_t local[64];
+        uint64_t nb[64];
+        for (int32_t i = 0; i < m; ++i) {
+            local[i] = verts[lo + i];
+            level[local[i]] = i;  // reuse level[] as local index
+        }
+        for (int32_t i = 0; i < m; ++i) {
+            uint64_t b = 0;
+            int32_t v = local[i];
+            for (int32_t k = xadj[v]; k < xadj[v + 1]; ++k) {
+                int32_t u = adj[k];
+                if (tag[u] == t) b |= (uint64_t)1 << level[u];
+            }
+            nb[i] = b;
+        }
+        for (int32_t i = 0; i < m; ++i) level[local[i]] = -1;
+        uint64_t alive = (m == 64) ? ~(uint64_t)0 : (((uint64_t)1 << m) - 1);
+        for (int32_t step = 0; step < m; ++step) {
+            int32_t best = -1, bestd = 1 << 30;
+            for (uint64_t a = alive; a; a &= a - 1) {
+                int32_t i = __builtin_ctzll(a);
+                int32_t d = __builtin_popcountll(nb[i] & alive);
+                if (d < bestd) { bestd = d; best = i; }
+            }
+            uint64_t N = nb[best] & alive & ~((uint64_t)1 << best);
+            for (uint64_t a = N; a; a &= a - 1) {
+                int32_t u = __builtin_ctzll(a);
+                nb[u] |= N;
+                nb[u] &= ~((uint64_t)1 << u);
+            }
+            alive &= ~((uint64_t)1 << best);
+            verts[lo + step] = local[best];
+        }
+    }
+
+    // Finds a pseudo-peripheral vertex of the piece tagged t containing `start`.
+    int32_t pseudo_peripheral(int32_t start, int32_t t, int32_t* count_out) {
+        int32_t root = start, depth = -1;
+        int32_t count = 0;
+        for (int it = 0; it < 8; ++it) {
+            int32_t d;
+            count = bfs(root, t, &d);
+            if (d <= depth) { clear_levels(count); break; }
+            depth = d;
+            // vertex of minimum degree in the last level
+            int32_t cand = root, cd = 1 << 30;
+            for (int32_t i = count - 1; i >= 0 && level[queue[i]] == d; --i) {
+                int32_t dv = degree_in(queue[i], t);
+                if (dv < cd) { cd = dv; cand = queue[i]; }
+            }
+            clear_levels(count);
+            if (cand == root) break;
+            root = cand;
+        }
+        *count_out = count;
+        return root;
+    }
+
+    void run();
+};
+
+struct Task { int32_t lo, hi; };
+
+void NDState::run() {
+    for (int32_t i = 0; i < n; ++i) verts[i] = i;
+    std::vector<Task> stack;
+    stack.push_back({0, n});
+    std::vector<int32_t> buf;
+    while (!stack.empty()) {
+        Task tk = stack.back();
+        stack.pop_back();
+        const int32_t lo = tk.lo, hi = tk.hi, m = hi - lo;
+        if (m <= 0) continue;
+        const int32_t t = next_tag++;
+        for (int32_t i = lo; i < hi; ++i) tag[verts[i]] = t;
+        if (m <= 64) {
+            order_small(lo, hi, t);
+            continue;
+        }
+        // Split off connected components.
+        int32_t cnt = bfs(verts[lo], t, nullptr);
+        if (cnt < m) {
+            // The reached component goes first, the rest becomes another task.
+            buf.assign(queue.begin(), queue.begin() + cnt);
+            clear_levels(cnt);
+            for (int32_t v : buf) side[v] = 1;
+            int32_t w = lo;
+            std::vector<int32_t> rest;
+            rest.reserve((size_t)(m - cnt));
+            for (int32_t i = lo; i < hi; ++i) {
+                int32_t v = verts[i];
+                if (side[v] == 1) verts[w++] = v; else rest.push_back(v);
+            }
+            for (int32_t v : rest) verts[w++] = v;
+            for (int32_t v : buf) side[v] = 0;
+            stack.push_back({lo + cnt, hi});
+            stack.push_back({lo, lo + cnt});
+            continue;
+        }
+        clear_levels(cnt);
+        // Level structure from a pseudo-peripheral vertex.
+        int32_t count;
+        int32_t root = pseudo_peripheral(verts[lo], t, &count);
+        int32_t depth;
+        count = bfs(root, t, &depth);
+        std::vector<int32_t> lvl_size((size_t)depth + 2, 0);
+        for (int32_t i = 0; i < count; ++i) lvl_size[level[queue[i]]]++;
+        int32_t split = -1;
+        if (depth >= 2) {
+            // pick the level minimising |S| among levels that leave at least
+            // a quarter of the piece on each side; ties go to better balance.
+            int64_t best_score = INT64_MAX;
+            int32_t before = 0;
+            for (int32_t l = 0; l <= depth; ++l) {
+                int32_t after = m - before - lvl_size[l];
+                if (l > 0 && l < depth && 4 * (int64_t)before >= m && 4 * (int64_t)after >= m) {
+                    int64_t imb = std::abs(before - after);
+                    int64_t score = (int64_t)lvl_size[l] * 4 * (int64_t)m + imb;
+                    if (score < best_score) { best_score = score; split = l; }
+                }
+                before += lvl_size[l];
+            }
+            if (split < 0) {
+                // fall back to the median level
+                before = 0;
+                for (int32_t l = 0; l <= depth; ++l) {
+                    if (2 * (before + lvl_size[l]) >= m) { split = std::max(1, std::min(l, depth - 1)); break; }
+                    before += lvl_size[l];
+                }
+            }
+        }
+        if (split < 0) {
+            // Too shallow to split (near-clique): minimum-degree-free fallback,
+            // keep BFS order.
+            for (int32_t i = 0; i < count; ++i) verts[lo + i] = queue[i];
+            clear_levels(count);
+            // order in chunks of 64 is meaningless for cliques; keep as is
+            continue;
+        }
+        for (int32_t i = 0; i < count; ++i) {
+            int32_t v = queue[i];
+            int32_t l = level[v];
+            side[v] = l < split ? 0 : (l > split ? 1 : 2);
+        }
+        clear_levels(count);
+        // Trim the separator: a separator vertex with no neighbour on one side
+        // can join the other side.
+        for (int pass = 0; pass < 2; ++pass) {
+            for (int32_t i = lo; i < hi; ++i) {
+                int32_t v = verts[i];
+                if (side[v] != 2) continue;
+                bool hasA = false, hasB = false;
+                for (int32_t k = xadj[v]; k < xadj[v + 1]; ++k) {
+                    int32_t u = adj[k];
+                    if (tag[u] != t) continue;
+                    hasA |= side[u] == 0;
+                    hasB |= side[u] == 1;
+                }
+                if (!hasB) side[v] = 0;
+                else if (!hasA) side[v] = 1;
+            }
+        }
+        int32_t na = 0, nb_ = 0, ns = 0;
+        for (int32_t i = lo; i < hi; ++i) {
+            int32_t s = side[verts[i]];
+            na += s == 0; nb_ += s == 1; ns += s == 2;
+        }
+        buf.resize((size_t)m);
+        int32_t ia = 0, ib = na, is = na + nb_;
+        for (int32_t i = lo; i < hi; ++i) {
+            int32_t v = verts[i];
+            int32_t s = side[v];
+            if (s == 0) buf[ia++] = v; else if (s == 1) buf[ib++] = v; else buf[is++] = v;
+        }
+        std::copy(buf.begin(), buf.begin() + m, verts.begin() + lo);
+        for (int32_t i = lo; i < hi; ++i) side[verts[i]] = 0;
+        if (ns == 0 || na == 0 || nb_ == 0) {
+            // degenerate split: order the piece as is (tiny pieces handled above)
+            if (na + nb_ == 0) continue;
+        }
+        stack.push_back({lo + na, lo + na + nb_});
+        stack.push_back({lo, lo + na});
+        (void)ns;
+    }
+}
+
+}  // namespace
+
+std::vector<int32_t> nested_dissection(int32_t n, const std::vector<int32_t>& xadj,
+                                       const std::vector<int32_t>& adj) {
+    NDState st(n, xadj, adj);
+    st.run();
+    return st.verts;
+}
+
+}  // namespace gbchol

@@ -1,0 +1,196 @@
+// Sparse input preparation (host). Same semantics as the reference's
+// coo_to_csc / csr_to_csc / csc_sort_indices / csc_sum_duplicates
+// (src/cholesky_solver.cpp:8-149): the result is a CSC matrix whose row
+// indices are sorted inside each column and whose duplicate (row, col)
+// entries are summed. Unlike the reference, every index is range-checked and
+// the per-column sort is stable, so duplicates are summed in input order.
+#include "host.h"
+
+#include <algorithm>
+#include <numeric>
+
+namespace gbchol {
+
+namespace {
+
+// Counting-sort placement of (row, col, val) triples into columns, keeping
+// input order inside a column. `row_of(e)` / `col_of(e)` give the entry e.
+template <class RowOf, class ColOf>
+void place_by_column(int32_t n, int64_t nnz, RowOf row_of, ColOf col_of, const double* x,
+                     Csc& out) {
+    out.n = n;
+    out.colptr.assign((size_t)n + 1, 0);
+    for (int64_t e = 0; e < nnz; ++e) out.colptr[(size_t)col_of(e) + 1]++;
+    for (int32_t c = 0; c < n; ++c) out.colptr[c + 1] += out.colptr[c];
+    out.rowidx.resize((size_t)nnz);
+    out.vals.resize((size_t)nnz);
+    std::vector<int32_t> next(out.colptr.begin(), out.colptr.end() - 1);
+    for (int64_t e = 0; e < nnz; ++e) {
+        int32_t c = col_of(e);
+        int32_t dst = next[c]++;
+        out.rowidx[dst] = row_of(e);
+        out.vals[dst] = x[e];
+    }
+}
+
+// Stable sort of each column by row index, then summation of equal rows.
+void sort_and_sum(Csc& A) {
+    const int32_t n = A.n;
+    std::vector<std::pair<int32_t, double>> tmp;
+    int32_t w = 0;
+    int32_t start = 0;
+    for (int32_t c = 0; c < n; ++c) {
+        int32_t end = A.colptr[c + 1];
+        bool sorted = true;
+        for (int32_t k = start + 1; k < end; ++k)
+            if (A.rowidx[k] < A.rowidx[k - 1]) { sorted = false; break; }
+        if (!sorted) {
+            tmp.resize((size_t)(end - start));
+            for (int32_t k = start; k < end; ++k) tmp[k - start] = {A.rowidx[k], A.vals[k]};
+            std::stable_sort(tmp.begin(), tmp.end(),
+                             [](const auto& a, const auto& b) { return a.first < b.first; });
+            for (int32_t k = start; k < end; ++k) {
+                A.rowidx[k] = tmp[k - start].first;
+                A.vals[k] = tmp[k - start].second;
+            }
+        }
+        A.colptr[c] = w;
+        int32_t k = start;
+        while (k < end) {
+            int32_t r = A.rowidx[k];
+            double v = A.vals[k++];
+            while (k < end && A.rowidx[k] == r) v += A.vals[k++];
+            A.rowidx[w] = r;
+            A.vals[w] = v;
+            ++w;
+        }
+        start = end;
+    }
+    A.colptr[n] = w;
+    A.rowidx.resize((size_t)w);
+    A.vals.resize((size_t)w);
+    A.rowidx.shrink_to_fit();
+    A.vals.shrink_to_fit();
+}
+
+}  // namespace
+
+Status build_csc(int32_t n, int64_t nnz, const int32_t* ii, const int32_t* jj, const double* x,
+                 int32_t fmt, Csc& out, std::string& err) {
+    if (n < 0) { err = "The number of rows must be non-negative."; return ST_INVALID; }
+    if (nnz < 0 || nnz >= (int64_t)INT32_MAX) {
+        err = "Number of nonzero entries out of range.";
+        return ST_INVALID;
+    }
+    if (fmt == FMT_COO) {
+        for (int64_t e = 0; e < nnz; ++e) {
+            if (ii[e] < 0 || ii[e] >= n || jj[e] < 0 || jj[e] >= n) {
+                err = "Sparse COO matrix: index out of range.";
+                return ST_INVALID;
+            }
+        }
+        place_by_column(n, nnz, [&](int64_t e) { return ii[e]; },
+                        [&](int64_t e) { return jj[e]; }, x, out);
+    } else if (fmt == FMT_CSR || fmt == FMT_CSC) {
+        const char* what = fmt == FMT_CSR ? "Sparse CSR matrix" : "Sparse CSC matrix";
+        if (ii[0] != 0 || (int64_t)ii[n] != nnz) {
+            err = std::string(what) + ": Invalid pointer array.";
+            return ST_INVALID;
+        }
+        for (int32_t k = 0; k < n; ++k)
+            if (ii[k + 1] < ii[k]) {
+                err = std::string(what) + ": Invalid pointer array.";
+                return ST_INVALID;
+            }
+        for (int64_t e = 0; e < nnz; ++e)
+            if (jj[e] < 0 || jj[e] >= n) {
+                err = std::string(what) + ": index out of range.";
+                return ST_INVALID;
+            }
+        if (fmt == FMT_CSR) {
+            // owner row of each entry
+            std::vector<int32_t> rowof((size_t)nnz);
+            for (int32_t r = 0; r < n; ++r)
+                for (int32_t e = ii[r]; e < ii[r + 1]; ++e) rowof[e] = r;
+            place_by_column(n, nnz, [&](int64_t e) { return rowof[e]; },
+                            [&](int64_t e) { return jj[e]; }, x, out);
+        } else {
+            out.n = n;
+            out.colptr.assign(ii, ii + n + 1);
+            out.rowidx.assign(jj, jj + nnz);
+            out.vals.assign(x, x + nnz);
+        }
+    } else {
+        err = "Unknown matrix type.";
+        return ST_INVALID;
+    }
+    sort_and_sum(out);
+    return ST_OK;
+}
+
+void symmetric_from_lower(const Csc& A, Csc& S) {
+    const int32_t n = A.n;
+    S.n = n;
+    S.colptr.assign((size_t)n + 1, 0);
+    for (int32_t c = 0; c < n; ++c)
+        for (int32_t k = A.colptr[c]; k < A.colptr[c + 1]; ++k) {
+            int32_t r = A.rowidx[k];
+            if (r < c) continue;
+            S.colptr[c + 1]++;
+            if (r != c) S.colptr[r + 1]++;
+        }
+    for (int32_t c = 0; c < n; ++c) S.colptr[c + 1] += S.colptr[c];
+    S.rowidx.resize((size_t)S.colptr[n]);
+    S.vals.resize((size_t)S.colptr[n]);
+    std::vector<int32_t> next(S.colptr.begin(), S.colptr.end() - 1);
+    // Visiting columns in increasing order keeps every column's rows sorted:
+    // mirrored entries (c, r) with c < r arrive while scanning column c < r.
+    for (int32_t c = 0; c < n; ++c)
+        for (int32_t k = A.colptr[c]; k < A.colptr[c + 1]; ++k) {
+            int32_t r = A.rowidx[k];
+            if (r < c) continue;
+            double v = A.vals[k];
+            // entry (r, c) into column c
+            int32_t d = next[c]++;
+            S.rowidx[d] = r;
+            S.vals[d] = v;
+            if (r != c) {  // mirror (c, r) into column r
+                int32_t d2 = next[r]++;
+                S.rowidx[d2] = c;
+                S.vals[d2] = v;
+            }
+        }
+    // Column c receives mirrored rows (< c) interleaved with its own rows
+    // (>= c); restore the sorted order.
+    for (int32_t c = 0; c < n; ++c) {
+        int32_t s = S.colptr[c], e = S.colptr[c + 1];
+        bool sorted = true;
+        for (int32_t k = s + 1; k < e; ++k)
+            if (S.rowidx[k] < S.rowidx[k - 1]) { sorted = false; break; }
+        if (sorted) continue;
+        std::vector<std::pair<int32_t, double>> t((size_t)(e - s));
+        for (int32_t k = s; k < e; ++k) t[k - s] = {S.rowidx[k], S.vals[k]};
+        std::sort(t.begin(), t.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+        for (int32_t k = s; k < e; ++k) { S.rowidx[k] = t[k - s].first; S.vals[k] = t[k - s].second; }
+    }
+}
+
+void transpose(int32_t n, const std::vector<int32_t>& colptr, const std::vector<int32_t>& rowidx,
+               const std::vector<double>& vals, std::vector<int32_t>& tptr,
+               std::vector<int32_t>& tidx, std::vector<double>& tvals) {
+    const size_t nnz = rowidx.size();
+    tptr.assign((size_t)n + 1, 0);
+    for (size_t k = 0; k < nnz; ++k) tptr[(size_t)rowidx[k] + 1]++;
+    for (int32_t r = 0; r < n; ++r) tptr[r + 1] += tptr[r];
+    tidx.resize(nnz);
+    tvals.resize(vals.empty() ? 0 : nnz);
+    std::vector<int32_t> next(tptr.begin(), tptr.end() - 1);
+    for (int32_t c = 0; c < n; ++c)
+        for (int32_t k = colptr[c]; k < colptr[c + 1]; ++k) {
+            int32_t d = next[rowidx[k]]++;
+            tidx[d] = c;
+            if (!vals.empty()) tvals[d] = vals[k];
+        }
+}
+
+}  // namespace gbchol

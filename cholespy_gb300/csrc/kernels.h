@@ -1,0 +1,49 @@
+// Internal launch interface of the gbchol CUDA kernels (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace gbchol {
+
+// ---- level analysis (analysis.cu) ----------------------------------------
+// One warp per row; rows in dependency order (increasing for L, decreasing
+// for L^T). levels[i] = 0 for rows without off-diagonal entries, else
+// 1 + max level of the rows it depends on. Same definition as the
+// reference's analysis_lower / analysis_upper (kernels/kernels.cu:8-60).
+cudaError_t launch_level_analysis(bool lower, int n, const int* rowptr, const int* cols,
+                                  int* levels, int* flags, int epoch, int* max_lvl, int* status,
+                                  cudaStream_t stream);
+
+// ---- row-wise sync-free sweeps (solve_rows.cu) ----------------------------
+// Lower sweep (L y = b[perm]):    out_tmp[row] = (in[perm[row]] - sum L[row,c] tmp[c]) / L[row,row]
+// Upper sweep (L^T x = y):        tmp[row] = (tmp[row] - sum U[row,c] tmp[c]) / U[row,row]
+//                                 out[perm[row]] = tmp[row]   (or += in refinement mode)
+// Same arithmetic as solve_lower / solve_upper (kernels/kernels.cu:64-202).
+struct RowSweepArgs {
+    int n = 0;
+    int nrhs = 0;
+    const int* rowptr = nullptr;
+    const int* cols = nullptr;
+    const void* vals = nullptr;   // T
+    const int* order = nullptr;   // rows sorted by (level, row)
+    const int* perm = nullptr;
+    const void* in = nullptr;     // lower: right-hand side (TIn), read through perm
+    void* tmp = nullptr;          // T, n x nrhs, permuted space
+    void* out = nullptr;          // upper: solution (TOut), written through perm
+    int* flags = nullptr;
+    int epoch = 0;
+    int* status = nullptr;
+    const int* skip = nullptr;    // if non-null and *skip != 0 the sweep does nothing
+};
+
+enum class SweepIO {
+    F32,          // T = float, in/out float
+    F64,          // T = double, in/out double
+    F32_MIXED,    // T = float, in double, out double (x = y): first refinement solve
+    F32_REFINE,   // T = float, in double (residual), out double with x += d
+};
+
+cudaError_t launch_row_sweep(const RowSweepArgs& a, bool lower, SweepIO io, cudaStream_t stream);
+
+}  // namespace gbchol

@@ -1,0 +1,217 @@
+// Row-wise, sync-free sparse triangular sweeps (sm_103a).
+//
+// Same mathematics as the reference's solve_lower / solve_upper
+// (kernels/kernels.cu:64-202): rows are visited in level order, each row
+// waits for the rows it depends on and then publishes its own value through
+// a flag. GB300 design differences:
+//   * one WARP per row instead of one 128-thread block per row, and no
+//     __syncthreads per nonzero: for up to 8 RHS the lanes split the row's
+//     nonzeros (coalesced index/value loads, warp-shuffle reduction); for more
+//     RHS the lanes split the RHS columns, so x loads are coalesced, and the
+//     row's (col, val) pairs are loaded 32 at a time and broadcast by shuffle;
+//   * persistent cooperative grid with a static row assignment instead of a
+//     global atomic ticket (no contended atomic per row);
+//   * flags carry an epoch, so no per-solve memset of the flag array;
+//   * bounded waits (device.cuh).
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+#include "kernels.h"
+#include "launch.h"
+
+namespace gbchol {
+
+namespace {
+
+template <typename T, typename TIn, typename TOut, bool ACCUM>
+struct IO {
+    using t = T;
+    using tin = TIn;
+    using tout = TOut;
+    static constexpr bool accum = ACCUM;
+};
+
+// Writes the solved value of (row, j) in permuted space and, for the upper
+// sweep, to the user array through perm.
+template <class io, bool LOWER>
+__device__ __forceinline__ void emit(const RowSweepArgs& a, int row, int prow, int j,
+                                     typename io::t v) {
+    using T = typename io::t;
+    T* tmp = static_cast<T*>(a.tmp);
+    tmp[(size_t)row * a.nrhs + j] = v;
+    if (!LOWER) {
+        using TO = typename io::tout;
+        TO* out = static_cast<TO*>(a.out);
+        size_t o = (size_t)prow * a.nrhs + j;
+        if (io::accum) out[o] += (TO)v;
+        else out[o] = (TO)v;
+    }
+}
+
+template <class io, bool LOWER>
+__device__ __forceinline__ typename io::t load_rhs(const RowSweepArgs& a, int row, int prow, int j) {
+    using T = typename io::t;
+    if (LOWER) {
+        const typename io::tin* in = static_cast<const typename io::tin*>(a.in);
+        return (T)in[(size_t)prow * a.nrhs + j];
+    }
+    return static_cast<const T*>(a.tmp)[(size_t)row * a.nrhs + j];
+}
+
+// Lanes split the nonzeros of the row; R >= nrhs accumulators per lane.
+template <class io, bool LOWER, int R>
+__global__ void __launch_bounds__(256) sweep_nnz_kernel(RowSweepArgs a) {
+    using T = typename io::t;
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    const T* __restrict__ vals = static_cast<const T*>(a.vals);
+    const T* tmp = static_cast<const T*>(a.tmp);
+    const int nrhs = a.nrhs;
+    if (a.skip && dev::ld_volatile(a.skip)) return;
+    for (int t = warp; t < a.n; t += nwarps) {
+        const int row = a.order[t];
+        const int s = a.rowptr[row], e = a.rowptr[row + 1];
+        const int lo = LOWER ? s : s + 1;
+        const int hi = LOWER ? e - 1 : e;
+        T acc[R];
+#pragma unroll
+        for (int j = 0; j < R; ++j) acc[j] = T(0);
+        for (int k = lo + lane; k < hi; k += 32) {
+            const int col = a.cols[k];
+            const T v = vals[k];
+            if (!dev::wait_geq(a.flags + col, a.epoch, a.status)) continue;
+            const T* xc = tmp + (size_t)col * nrhs;
+#pragma unroll
+            for (int j = 0; j < R; ++j)
+                if (j < nrhs) acc[j] = fma(v, __ldcg(xc + j), acc[j]);
+        }
+        T mine = T(0);
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+            T sj = dev::warp_sum(acc[j]);
+            if (j == lane) mine = sj;
+        }
+        const T diag = vals[LOWER ? e - 1 : s];
+        const int prow = a.perm[row];
+        if (lane < nrhs) {
+            T v = (load_rhs<io, LOWER>(a, row, prow, lane) - mine) / diag;
+            emit<io, LOWER>(a, row, prow, lane, v);
+            __threadfence();
+        }
+        __syncwarp();
+        if (lane == 0) dev::st_release(a.flags + row, a.epoch);
+    }
+}
+
+// Lanes split the RHS columns: G lanes per group (32/G groups take
+// alternating nonzeros), Q RHS columns per lane (nrhs <= G*Q).
+template <class io, bool LOWER, int G, int Q>
+__global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
+    using T = typename io::t;
+    constexpr int NG = 32 / G;
+    const int lane = threadIdx.x & 31;
+    const int grp = lane / G, sub = lane % G;
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    const T* __restrict__ vals = static_cast<const T*>(a.vals);
+    const T* tmp = static_cast<const T*>(a.tmp);
+    const int nrhs = a.nrhs;
+    if (a.skip && dev::ld_volatile(a.skip)) return;
+    for (int t = warp; t < a.n; t += nwarps) {
+        const int row = a.order[t];
+        const int s = a.rowptr[row], e = a.rowptr[row + 1];
+        const int lo = LOWER ? s : s + 1;
+        const int hi = LOWER ? e - 1 : e;
+        T acc[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) acc[q] = T(0);
+        for (int base = lo; base < hi; base += 32) {
+            const int k = base + lane;
+            const int mycol = k < hi ? a.cols[k] : 0;
+            const T myv = k < hi ? vals[k] : T(0);
+            const int cnt = min(32, hi - base);
+            const int steps = (cnt + NG - 1) / NG;
+            for (int st = 0; st < steps; ++st) {
+                const int eidx = st * NG + grp;
+                const bool valid = eidx < cnt;
+                const int col = __shfl_sync(0xffffffffu, mycol, valid ? eidx : 0);
+                const T v = __shfl_sync(0xffffffffu, myv, valid ? eidx : 0);
+                if (!valid) continue;
+                if (!dev::wait_geq(a.flags + col, a.epoch, a.status)) continue;
+                const T* xc = tmp + (size_t)col * nrhs;
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    const int j = sub + q * G;
+                    if (j < nrhs) acc[q] = fma(v, __ldcg(xc + j), acc[q]);
+                }
+            }
+        }
+        if (NG > 1) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+#pragma unroll
+                for (int o = G; o < 32; o <<= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+        }
+        const T diag = vals[LOWER ? e - 1 : s];
+        const int prow = a.perm[row];
+        if (grp == 0) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const int j = sub + q * G;
+                if (j < nrhs) {
+                    T v = (load_rhs<io, LOWER>(a, row, prow, j) - acc[q]) / diag;
+                    emit<io, LOWER>(a, row, prow, j, v);
+                }
+            }
+            __threadfence();
+        }
+        __syncwarp();
+        if (lane == 0) dev::st_release(a.flags + row, a.epoch);
+    }
+}
+
+template <class io, bool LOWER>
+cudaError_t launch_io(const RowSweepArgs& a, cudaStream_t stream) {
+    const void* fn;
+    const int r = a.nrhs;
+    if (r <= 1) fn = (const void*)sweep_nnz_kernel<io, LOWER, 1>;
+    else if (r <= 2) fn = (const void*)sweep_nnz_kernel<io, LOWER, 2>;
+    else if (r <= 4) fn = (const void*)sweep_nnz_kernel<io, LOWER, 4>;
+    else if (r <= 8) fn = (const void*)sweep_nnz_kernel<io, LOWER, 8>;
+    else if (r <= 16) fn = (const void*)sweep_rhs_kernel<io, LOWER, 16, 1>;
+    else if (r <= 32) fn = (const void*)sweep_rhs_kernel<io, LOWER, 32, 1>;
+    else if (r <= 64) fn = (const void*)sweep_rhs_kernel<io, LOWER, 32, 2>;
+    else fn = (const void*)sweep_rhs_kernel<io, LOWER, 32, 4>;
+    int grid = 0;
+    cudaError_t e = coop_grid(fn, 256, 0, &grid);
+    if (e != cudaSuccess) return e;
+    const int need = (a.n + 7) / 8;
+    if (grid > need) grid = need;
+    RowSweepArgs copy = a;
+    void* args[] = {&copy};
+    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, stream);
+}
+
+}  // namespace
+
+cudaError_t launch_row_sweep(const RowSweepArgs& a, bool lower, SweepIO io, cudaStream_t stream) {
+    if (a.n == 0) return cudaSuccess;
+    switch (io) {
+        case SweepIO::F32:
+            return lower ? launch_io<IO<float, float, float, false>, true>(a, stream)
+                         : launch_io<IO<float, float, float, false>, false>(a, stream);
+        case SweepIO::F64:
+            return lower ? launch_io<IO<double, double, double, false>, true>(a, stream)
+                         : launch_io<IO<double, double, double, false>, false>(a, stream);
+        case SweepIO::F32_MIXED:
+            return lower ? launch_io<IO<float, double, double, false>, true>(a, stream)
+                         : launch_io<IO<float, double, double, false>, false>(a, stream);
+        case SweepIO::F32_REFINE:
+            return lower ? launch_io<IO<float, double, double, true>, true>(a, stream)
+                         : launch_io<IO<float, double, double, true>, false>(a, stream);
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace gbchol

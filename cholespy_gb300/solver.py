@@ -1,0 +1,323 @@
+"""Drop-in ``CholeskySolverF`` / ``CholeskySolverD`` / ``MatrixType``.
+
+Mirrors the reference's nanobind module (src/main.cpp:16-136): the same
+constructor ``(n_rows, ii, jj, x, type)`` and ``solve(b, x)``, the same
+argument checks and error messages, and the same asynchronous in-place write
+of ``x``. Arrays may be torch tensors, NumPy arrays or anything exporting
+DLPack / ``__cuda_array_interface__`` (CuPy, JAX, ...). Solves run on the
+GB300 through the gbchol C ABI; the solver lives on the CUDA device of the
+constructor's arrays (the reference always uses device 0,
+src/cuda_driver.cpp:124).
+
+Extensions beyond the reference (keyword-only, off by default):
+``CholeskySolverD(..., refine=True)`` keeps an FP32 factor plus the FP64
+matrix and makes ``solve`` an FP32 solve with FP64-residual iterative
+refinement to ``tol`` (default 1e-10); ``solve_refined`` returns its
+statistics.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _ffi
+
+
+class MatrixType(enum.IntEnum):
+    """Sparse input format (src/cholesky_solver.h:8-12, src/main.cpp:118-121)."""
+
+    CSC = 0
+    CSR = 1
+    COO = 2
+
+
+@dataclass
+class SolverInfo:
+    n: int
+    device: int
+    nnz_a: int
+    nnz_l: int
+    levels_lower: int
+    levels_upper: int
+    n_supernodes: int
+    max_supernode: int
+    factor_flops: float
+    factor_seconds: float
+    analysis_seconds: float
+
+
+@dataclass
+class RefineResult:
+    iterations: int
+    converged: bool
+    max_rel_residual: float
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _device_of(a):
+    """('cuda', index) or ('cpu', 0) for a torch tensor / array-like."""
+    try:
+        torch = _torch()
+        if isinstance(a, torch.Tensor):
+            return (a.device.type, a.device.index or 0)
+    except ImportError:  # pragma: no cover - torch is a hard dependency here
+        pass
+    if isinstance(a, np.ndarray):
+        return ("cpu", 0)
+    if hasattr(a, "__cuda_array_interface__"):
+        return ("cuda", _cuda_index_of(a))
+    if hasattr(a, "__dlpack_device__"):
+        dev_type, dev_id = a.__dlpack_device__()
+        if int(dev_type) in (2, 13):  # kDLCUDA, kDLCUDAManaged
+            return ("cuda", int(dev_id))
+        if int(dev_type) == 1:
+            return ("cpu", 0)
+        return ("other", int(dev_id))
+    return ("cpu", 0)
+
+
+def _cuda_index_of(a):
+    torch = _torch()
+    return torch.as_tensor(a, device="cuda").device.index or 0
+
+
+def _as_torch(a):
+    """Zero-copy torch view of an array-like (DLPack / CUDA array interface)."""
+    torch = _torch()
+    if isinstance(a, torch.Tensor):
+        return a
+    if isinstance(a, np.ndarray):
+        return torch.from_numpy(a)
+    if hasattr(a, "__dlpack__"):
+        return torch.from_dlpack(a)
+    if hasattr(a, "__cuda_array_interface__"):
+        return torch.as_tensor(a, device="cuda")
+    return torch.as_tensor(np.asarray(a))
+
+
+def _host_vector(a, dtype, name):
+    """1-D host copy of a constructor argument, as the reference's D2H copies
+    (src/main.cpp:55-61)."""
+    t = _as_torch(a)
+    if t.dim() != 1:
+        raise ValueError(f"{name} must be a 1-D array.")
+    arr = t.detach().cpu().numpy()
+    if dtype == np.int32:
+        if not np.issubdtype(arr.dtype, np.integer):
+            raise TypeError(f"{name} must be an integer array.")
+        if arr.size and (arr.min() < np.iinfo(np.int32).min or arr.max() > np.iinfo(np.int32).max):
+            raise ValueError(f"{name}: index does not fit in int32.")
+    return np.ascontiguousarray(arr, dtype=dtype)
+
+
+def _ptr(arr: np.ndarray):
+    return C.c_void_p(arr.ctypes.data) if arr.size else C.c_void_p(0)
+
+
+class _CholeskySolver:
+    _precision = 0
+    _torch_dtype_name = "float32"
+
+    def __init__(self, n_rows, ii, jj, x, type, *, refine=False, tol=1e-10, max_iter=10):
+        lib = _ffi.lib()
+        self._h = None
+        n_rows = int(n_rows)
+        if n_rows < 0 or n_rows > np.iinfo(np.uint32).max:
+            raise ValueError("n_rows out of range.")
+        type = MatrixType(int(type))
+        ni, nj, nx = _len(ii), _len(jj), _len(x)
+        # Shape checks of src/main.cpp:28-43 (same messages)
+        if type == MatrixType.COO:
+            if ni != nj:
+                raise ValueError("Sparse COO matrix: the two index arrays should have the same size.")
+            if ni != nx:
+                raise ValueError("Sparse COO matrix: the index and data arrays should have the same size.")
+        elif type == MatrixType.CSR:
+            if nj != nx:
+                raise ValueError("Sparse CSR matrix: the column index and data arrays should have the same size.")
+            if ni != n_rows + 1:
+                raise ValueError("Sparse CSR matrix: Invalid size for row pointer array.")
+        else:
+            if nj != nx:
+                raise ValueError("Sparse CSC matrix: the row index and data arrays should have the same size.")
+            if ni != n_rows + 1:
+                raise ValueError("Sparse CSC matrix: Invalid size for column pointer array.")
+        devs = {_device_of(a)[0] for a in (ii, jj, x)}
+        if len(devs) != 1:
+            raise ValueError("All input tensors should be on the same device!")
+        dev_type = devs.pop()
+        if dev_type != "cuda" and dev_type != "cpu":
+            raise ValueError("Unsupported input device! Only CPU and CUDA arrays are supported.")
+        if dev_type == "cpu":
+            raise ValueError(
+                "The GB300 solver runs on CUDA: pass CUDA arrays (CPU-array solvers are "
+                "not provided by this build).")
+        device = _device_of(x)[1]
+        self._device = device
+        self._refine = bool(refine) and self._precision == 1
+        self._tol = float(tol)
+        self._max_iter = int(max_iter)
+        store = _ffi.STORE_F32 if self._precision == 0 else _ffi.STORE_F64
+        if self._refine:
+            store = _ffi.STORE_F32 | _ffi.STORE_F64 | _ffi.STORE_A64
+        hi = _host_vector(ii, np.int32, "ii")
+        hj = _host_vector(jj, np.int32, "jj")
+        hx = _host_vector(x, np.float64, "x")
+        torch = _torch()
+        h = C.c_void_p()
+        with torch.cuda.device(device):
+            st = lib.gbchol_create(n_rows, int(nx), _ptr(hi), _ptr(hj), _ptr(hx), int(type),
+                                   store, C.byref(h))
+        _ffi.check(st)
+        self._h = h
+        self._n = n_rows
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _ffi.lib().gbchol_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # -- checks of src/main.cpp:83-100 --------------------------------------
+    def _prepare(self, b, x, dtype):
+        torch = _torch()
+        tb, tx = _as_torch(b), _as_torch(x)
+        if tb.dim() != 1 and tb.dim() != 2:
+            raise ValueError("Expected 1D or 2D tensors as input.")
+        if tb.shape[0] != tx.shape[0] or (tb.dim() == 2 and (tx.dim() != 2 or tb.shape[1] != tx.shape[1])):
+            raise ValueError("x and b should have the same dimensions.")
+        db, dx = _device_of(b), _device_of(x)
+        if db[0] != dx[0]:
+            raise ValueError("x and b should be on the same device.")
+        if db[0] == "cpu":
+            raise ValueError("Input device is CPU but the solver was initialized for CUDA.")
+        if db[0] != "cuda":
+            raise ValueError("Unsupported input device! Only CPU and CUDA arrays are supported.")
+        if tb.device.index != self._device or tx.device.index != self._device:
+            raise ValueError("x and b should be on the device the solver was created on.")
+        if tb.dtype != dtype or tx.dtype != dtype:
+            raise TypeError(f"solve(): b and x must be {dtype} arrays (no implicit conversion).")
+        if not tb.is_contiguous() or not tx.is_contiguous():
+            raise TypeError("solve(): b and x must be C-contiguous.")
+        if tb.shape[0] != self._n:
+            raise ValueError("b and x must have n_rows rows.")
+        nrhs = tb.shape[1] if tb.dim() == 2 else 1
+        stream = torch.cuda.current_stream(self._device).cuda_stream
+        return tb, tx, nrhs, stream
+
+    def solve(self, b, x):
+        """Solve A x = b for the right-hand sides in b (vector or (n, n_rhs)),
+        writing x in place (asynchronous on the current CUDA stream)."""
+        torch = _torch()
+        dtype = torch.float32 if self._precision == 0 else torch.float64
+        tb, tx, nrhs, stream = self._prepare(b, x, dtype)
+        if self._refine:
+            self._solve_refined(tb, tx, nrhs, stream, self._tol, self._max_iter, stats=False)
+            return
+        st = _ffi.lib().gbchol_solve(self._h, self._precision, nrhs, C.c_void_p(tb.data_ptr()),
+                                     C.c_void_p(tx.data_ptr()), C.c_void_p(stream))
+        _ffi.check(st)
+
+    def _solve_refined(self, tb, tx, nrhs, stream, tol, max_iter, stats):
+        rs = _ffi.RefineStats()
+        if tb.data_ptr() == tx.data_ptr():
+            raise ValueError("Refined solves need distinct b and x arrays.")
+        st = _ffi.lib().gbchol_solve_refined(
+            self._h, nrhs, C.c_void_p(tb.data_ptr()), C.c_void_p(tx.data_ptr()), float(tol),
+            int(max_iter), C.c_void_p(stream), C.byref(rs) if stats else None)
+        _ffi.check(st)
+        if stats:
+            return RefineResult(int(rs.iterations), bool(rs.converged), float(rs.max_rel_residual))
+        return None
+
+    def check(self):
+        """Synchronise and raise if a device-side wait expired in a solve."""
+        _ffi.check(_ffi.lib().gbchol_check(self._h))
+
+    def reserve(self, n_rhs):
+        """Preallocate scratch for up to n_rhs RHS (before CUDA-graph capture)."""
+        _ffi.check(_ffi.lib().gbchol_reserve(self._h, int(n_rhs)))
+
+    def info(self) -> SolverInfo:
+        inf = _ffi.Info()
+        _ffi.check(_ffi.lib().gbchol_get_info(self._h, C.byref(inf)))
+        return SolverInfo(inf.n, inf.device, inf.nnz_a, inf.nnz_l, inf.levels_lower,
+                          inf.levels_upper, inf.n_supernodes, inf.max_supernode,
+                          inf.factor_flops, inf.factor_seconds, inf.analysis_seconds)
+
+    def levels(self, lower=True):
+        """(row_levels, order, max_lvl) of the analysis of L (lower) or L^T."""
+        n = self._n
+        lev = np.zeros(n, np.int32)
+        order = np.zeros(n, np.int32)
+        mx = C.c_int32(0)
+        _ffi.check(_ffi.lib().gbchol_get_levels(self._h, 1 if lower else 0, _ptr(lev), _ptr(order),
+                                                C.byref(mx)))
+        return lev, order, int(mx.value)
+
+    def factor(self):
+        """Host copy (perm, colptr, rowidx, vals) of the factor L (CSC, diagonal first)."""
+        n = self._n
+        nnz = self.info().nnz_l
+        perm = np.zeros(n, np.int32)
+        colptr = np.zeros(n + 1, np.int32)
+        rowidx = np.zeros(nnz, np.int32)
+        vals = np.zeros(nnz, np.float64)
+        _ffi.check(_ffi.lib().gbchol_get_factor(self._h, _ptr(perm), _ptr(colptr), _ptr(rowidx),
+                                                _ptr(vals)))
+        return perm, colptr, rowidx, vals
+
+    @property
+    def handle(self):
+        return self._h
+
+
+def _len(a):
+    try:
+        return int(a.shape[0])
+    except (AttributeError, IndexError, TypeError):
+        return len(a)
+
+
+class CholeskySolverF(_CholeskySolver):
+    """Single-precision solver implementation (src/docstr.h)."""
+
+    _precision = 0
+
+
+class CholeskySolverD(_CholeskySolver):
+    """Double-precision solver implementation (src/docstr.h).
+
+    ``refine=True`` keeps an FP32 copy of the factor and the FP64 matrix; then
+    ``solve`` runs FP32 solves with FP64-residual iterative refinement to
+    ``tol`` and ``solve_fp64`` the plain FP64 solve.
+    """
+
+    _precision = 1
+
+    def solve_refined(self, b, x, tol=None, max_iter=None) -> RefineResult:
+        """FP32 solve + FP64 iterative refinement; synchronises and returns stats."""
+        if not self._refine:
+            raise RuntimeError("solve_refined needs CholeskySolverD(..., refine=True).")
+        torch = _torch()
+        tb, tx, nrhs, stream = self._prepare(b, x, torch.float64)
+        return self._solve_refined(tb, tx, nrhs, stream, self._tol if tol is None else tol,
+                                   self._max_iter if max_iter is None else max_iter, stats=True)
+
+    def solve_fp64(self, b, x):
+        """Plain FP64 solve regardless of ``refine``."""
+        torch = _torch()
+        tb, tx, nrhs, stream = self._prepare(b, x, torch.float64)
+        st = _ffi.lib().gbchol_solve(self._h, 1, nrhs, C.c_void_p(tb.data_ptr()),
+                                     C.c_void_p(tx.data_ptr()), C.c_void_p(stream))
+        _ffi.check(st)

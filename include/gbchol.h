@@ -1,0 +1,196 @@
+/*
+ * gbchol: GB300-native (sm_103a) sparse Cholesky solve path, C ABI.
+ *
+ * This is the drop-in boundary for the GPU solve path of cholespy
+ * (rgl-epfl/cholespy v2.2.2). Every entry point takes plain pointers and
+ * sizes; the Python edge (cholespy_gb300/_ffi.py) binds them with ctypes, and
+ * any other host language can bind them the same way.
+ *
+ * Conventions
+ *   - Every function returns a gbchol_status (0 = success). On failure the
+ *     message is available from gbchol_last_error() (thread-local).
+ *   - Device pointers are CUDA device (or managed) addresses on the device the
+ *     solver was created on. "stream" is a cudaStream_t (NULL = legacy
+ *     default stream, like the reference's stream 0).
+ *   - Right-hand sides are row-major (n, nrhs) arrays: element (i, k) at
+ *     i * nrhs + k (reference kernels/kernels.cu:87,114,120,189).
+ *   - A solver is not thread-safe: calls on one handle must be serialised,
+ *     and solves on one handle must not overlap on the GPU (they share the
+ *     handle's scratch), like the reference (src/cholesky_solver.h:88-98).
+ */
+#ifndef GBCHOL_H
+#define GBCHOL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbchol_solver* gbchol_handle;
+
+typedef enum {
+    GBCHOL_OK = 0,
+    GBCHOL_EINVAL = 1,      /* invalid argument (Python: ValueError) */
+    GBCHOL_ENOTPOSDEF = 2,  /* not positive definite (Python: ValueError) */
+    GBCHOL_ECUDA = 3,       /* CUDA error (Python: RuntimeError) */
+    GBCHOL_ENOMEM = 4,      /* allocation failure (Python: RuntimeError) */
+    GBCHOL_ETIMEOUT = 5,    /* a bounded device-side wait expired (Python: RuntimeError) */
+    GBCHOL_ESTATE = 6,      /* call not valid for this handle (Python: RuntimeError) */
+    GBCHOL_EINTERNAL = 7
+} gbchol_status;
+
+/* Matrix formats: same values as cholespy.MatrixType (src/cholesky_solver.h:8-12). */
+enum { GBCHOL_CSC = 0, GBCHOL_CSR = 1, GBCHOL_COO = 2 };
+
+/* Storage flags for gbchol_create: which copies the solver keeps on the GPU. */
+enum {
+    GBCHOL_STORE_F32 = 1, /* FP32 factor: CholeskySolverF solves, and the inner solve of refinement */
+    GBCHOL_STORE_F64 = 2, /* FP64 factor: plain CholeskySolverD solves */
+    GBCHOL_STORE_A64 = 4  /* FP64 copy of A: residuals for refinement and the gradient pattern */
+};
+
+/* Maximum RHS count of one solve (src/cholesky_solver.cpp:418-420). */
+#define GBCHOL_MAX_RHS 128
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* gbchol_last_error(void);
+
+/* Library version string. */
+const char* gbchol_version(void);
+
+/*
+ * Factor A on the host and analyse the factor on the current CUDA device.
+ * Replaces CholeskySolver<Float>::CholeskySolver (src/cholesky_solver.cpp:152-198)
+ * with cpu = false, including factorize (:200-297) and both analyze_cuda
+ * calls (:299-376). ii/jj/x are HOST arrays with the meaning of the
+ * reference constructor (src/main.cpp:21-26): COO rows/cols, or CSR row
+ * pointers/cols, or CSC col pointers/rows; x is always float64. Only the lower
+ * triangle (row >= col) of A is used, as CHOLMOD does with stype = -1.
+ * `store` is a mask of GBCHOL_STORE_* flags.
+ */
+int gbchol_create(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t* jj,
+                  const double* x, int32_t matrix_type, int32_t store, gbchol_handle* out);
+
+/*
+ * Analyse an existing factor (the hot-path boundary proper): perm[k] is the
+ * original row at position k (CHOLMOD Perm), L is given in CSC with sorted
+ * rows and the diagonal first in each column (cholmod_factor_to_sparse,
+ * src/cholesky_solver.cpp:247-252). Uploads L and L^T and runs the level
+ * analysis of both (analyze_cuda, src/cholesky_solver.cpp:299-376). Host
+ * arrays. A is not known, so refinement and gradients are unavailable.
+ */
+int gbchol_create_from_factor(int32_t n, const int32_t* perm, const int32_t* colptr,
+                              const int32_t* rowidx, const double* vals, int32_t store,
+                              gbchol_handle* out);
+
+/*
+ * Host-only ordering + numeric LL^T (no GPU use): the replacement of
+ * cholmod_analyze + cholmod_factorize with the reference's settings
+ * (simplicial LL^T, nested dissection; src/cholesky_solver.cpp:200-243),
+ * preceded by the input preparation of src/cholesky_solver.cpp:152-179.
+ * threads = 0 uses every host core. Fails with GBCHOL_ENOTPOSDEF and
+ * "Matrix is not positive definite!" like src/cholesky_solver.cpp:241-242.
+ */
+typedef struct gbchol_host_factor* gbchol_factor_handle;
+
+int gbchol_factorize(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t* jj,
+                     const double* x, int32_t matrix_type, int32_t threads,
+                     gbchol_factor_handle* out);
+
+/* Sizes of a host factor: n, nnz(L), number of fundamental supernodes, flops. */
+int gbchol_factor_info(gbchol_factor_handle f, int32_t* n, int64_t* nnz_l, int32_t* n_supernodes,
+                       double* flops);
+
+/* Copy a host factor out (CSC, diagonal first); any pointer may be NULL. */
+int gbchol_factor_export(gbchol_factor_handle f, int32_t* perm, int32_t* colptr, int32_t* rowidx,
+                         double* vals);
+
+int gbchol_factor_free(gbchol_factor_handle f);
+
+/* Free every device and host buffer of the solver (src/cholesky_solver.cpp:465-486). */
+int gbchol_destroy(gbchol_handle h);
+
+/*
+ * x = A^{-1} b for nrhs right-hand sides, asynchronously on `stream`.
+ * Replaces CholeskySolver<Float>::solve_cuda (src/cholesky_solver.cpp:415-432):
+ * lower sweep tmp = L^{-1} b[perm], upper sweep x[perm] = L^{-T} tmp.
+ * precision: 0 = FP32 (float b/x), 1 = FP64 (double b/x). b and x are device
+ * pointers and may alias. nrhs outside 1..128 fails with GBCHOL_EINVAL and the
+ * reference's message "The number of RHS should be less than 128.".
+ */
+int gbchol_solve(gbchol_handle h, int32_t precision, int32_t nrhs, const void* b, void* x,
+                 void* stream);
+
+/* Statistics of one refined solve. */
+typedef struct {
+    int32_t iterations;       /* refinement steps taken (0 = FP32 solve was enough) */
+    int32_t converged;        /* 1 if max relative residual <= tol */
+    double max_rel_residual;  /* max over RHS of ||b - A x||_2 / ||b||_2 */
+} gbchol_refine_stats;
+
+/*
+ * FP32-factor solve with FP64-residual iterative refinement: x0 = A32^{-1} b,
+ * then r = b - A x in FP64 on the original A, d = A32^{-1} r, x += d (FP64),
+ * until max_k ||r_k||/||b_k|| <= tol or max_iter steps. b, x: FP64 device
+ * arrays (n, nrhs), may not alias. Needs GBCHOL_STORE_F32 | GBCHOL_STORE_A64.
+ * The loop runs without host synchronisation (a device flag ends it); when
+ * `stats` is non-NULL the call synchronises `stream` to fill it.
+ * No counterpart in the reference.
+ */
+int gbchol_solve_refined(gbchol_handle h, int32_t nrhs, const double* b, double* x, double tol,
+                         int32_t max_iter, void* stream, gbchol_refine_stats* stats);
+
+/* Solver facts. */
+typedef struct {
+    int32_t n;
+    int32_t device;
+    int64_t nnz_a;            /* nnz of the symmetric A kept (0 if not kept) */
+    int64_t nnz_l;            /* nnz of L (diagonal included) */
+    int32_t levels_lower;     /* number of levels of L   (max_lvl + 1) */
+    int32_t levels_upper;     /* number of levels of L^T (max_lvl + 1) */
+    int32_t n_supernodes;
+    int32_t max_supernode;
+    double factor_flops;
+    double factor_seconds;    /* host factorisation time */
+    double analysis_seconds;  /* device analysis time incl. uploads */
+    int32_t store;
+} gbchol_info;
+
+int gbchol_get_info(gbchol_handle h, gbchol_info* out);
+
+/*
+ * Copy the analysis results to host arrays of size n: row_levels[i] is the
+ * level of row i and order[] the rows sorted by (level, row), which is the
+ * `levels` array of the reference (src/cholesky_solver.cpp:315-367).
+ * lower = 1 for L, 0 for L^T. max_lvl may be NULL.
+ */
+int gbchol_get_levels(gbchol_handle h, int32_t lower, int32_t* row_levels, int32_t* order,
+                      int32_t* max_lvl);
+
+/*
+ * Copy the factor to host arrays: perm (n), colptr (n+1), rowidx and vals
+ * (nnz_l), CSC with the diagonal first. Any pointer may be NULL.
+ */
+int gbchol_get_factor(gbchol_handle h, int32_t* perm, int32_t* colptr, int32_t* rowidx,
+                      double* vals);
+
+/*
+ * Synchronise the solver's last stream and report the device-side status
+ * word: GBCHOL_ETIMEOUT if a bounded wait expired in an earlier solve (the
+ * word is then cleared).
+ */
+int gbchol_check(gbchol_handle h);
+
+/*
+ * Preallocate scratch for solves of up to nrhs right-hand sides so that later
+ * solves allocate nothing (needed before capturing solves in a CUDA graph).
+ */
+int gbchol_reserve(gbchol_handle h, int32_t nrhs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBCHOL_H */

@@ -1,0 +1,232 @@
+"""GPU parity tests of the drop-in solvers against the oracle.
+
+Ports the reference's own tests (tests/test_cholesky.py: test_solver,
+test_matrices) and adds bit-exact level-analysis checks, sweep parity with
+the oracle's restatement of the reference's kernels on the same factor, and
+iterative refinement to 1e-10."""
+import numpy as np
+import pytest
+
+import oracle
+from helpers import RHS, reference_problem, spsolve_ref, sym_matrix
+
+pytestmark = pytest.mark.gpu
+
+
+def _solver_cls(variant):
+    from cholespy_gb300 import CholeskySolverD, CholeskySolverF
+    return CholeskySolverF if variant == "float" else CholeskySolverD
+
+
+@pytest.mark.parametrize("name", ["cube", "ico3", "ico5"])
+@pytest.mark.parametrize("variant", ["float", "double"])
+def test_solver(cuda, name, variant):
+    """tests/test_cholesky.py:10-44 on CUDA."""
+    from cholespy_gb300 import MatrixType
+    torch = cuda
+    dtype = np.float32 if variant == "float" else np.float64
+    n, vals, idx, b = reference_problem(name, dtype=dtype)
+    x = spsolve_ref(n, vals, idx, b)
+    solver = _solver_cls(variant)(n, torch.tensor(idx[0], device="cuda"),
+                                  torch.tensor(idx[1], device="cuda"),
+                                  torch.tensor(vals, device="cuda"), MatrixType.COO)
+    for n_rhs in RHS:
+        b_t = torch.tensor(b[:, :n_rhs], device="cuda")
+        x_t = torch.zeros_like(b_t)
+        try:
+            solver.solve(b_t, x_t)
+            assert np.allclose(x_t.cpu().numpy(), x[:, :n_rhs])
+        except ValueError as e:
+            assert n_rhs > 128
+            assert str(e) == "The number of RHS should be less than 128."
+    solver.check()
+
+
+def test_matrices(cuda):
+    """tests/test_cholesky.py:46-86: COO, CSR and CSC inputs agree."""
+    import scipy.sparse as sp
+    from cholespy_gb300 import CholeskySolverF, MatrixType
+    torch = cuda
+    n, vals, idx, _ = reference_problem("cube")
+    np.random.seed(45)
+    A_csc = sp.csc_matrix((vals, (idx[0], idx[1])), shape=(n, n))
+    A_csr = sp.csr_matrix((vals, (idx[0], idx[1])), shape=(n, n))
+    b = np.random.random(size=(n, 32)).astype(np.float32)
+    b_t = torch.tensor(b, device="cuda")
+    x_ref = spsolve_ref(n, vals, idx, b)
+    for ii, jj, xx, t in (
+        (idx[0], idx[1], vals, MatrixType.COO),
+        (A_csr.indptr, A_csr.indices, A_csr.data, MatrixType.CSR),
+        (A_csc.indptr, A_csc.indices, A_csc.data, MatrixType.CSC),
+    ):
+        s = CholeskySolverF(n, torch.tensor(ii, device="cuda"), torch.tensor(jj, device="cuda"),
+                            torch.tensor(xx, device="cuda"), t)
+        x_t = torch.zeros_like(b_t)
+        s.solve(b_t, x_t)
+        assert np.allclose(x_t.cpu().numpy(), x_ref)
+
+
+def _make(torch, n, vals, idx, cls):
+    from cholespy_gb300 import MatrixType
+    return cls(n, torch.tensor(idx[0], device="cuda"), torch.tensor(idx[1], device="cuda"),
+               torch.tensor(vals, device="cuda"), MatrixType.COO)
+
+
+def _problems():
+    from cholespy_gb300 import workloads
+    yield "ico4", (lambda: (2562, *workloads.laplacian_coo(*workloads.icosphere(4)[:2], 2.0)))
+    yield "grid64", (lambda: (4096, *workloads.grid2d_coo(64, 10.0, 1.0)))
+    yield "grid3d_16", (lambda: (4096, *workloads.grid3d_coo(16, 1e-3)))
+
+
+PROBLEMS = dict(_problems())
+
+
+@pytest.mark.parametrize("name", list(PROBLEMS))
+def test_levels_bit_exact(cuda, name):
+    """GPU analysis == the reference's analysis (oracle restatement of
+    kernels.cu:8-60 + cholesky_solver.cpp:349-367) on the same factor."""
+    from cholespy_gb300 import CholeskySolverF
+    n, vals, idx = PROBLEMS[name]()
+    s = _make(cuda, n, vals, idx, CholeskySolverF)
+    perm, colptr, rowidx, lv = s.factor()
+    lrp, lci, _ = oracle.csr_of_lower(colptr, rowidx, lv)
+    for lower, (rp, ci) in ((True, (lrp, lci)), (False, (colptr, rowidx))):
+        lev_o, ord_o, mx_o = oracle.levels(rp, ci, lower)
+        lev_g, ord_g, mx_g = s.levels(lower)
+        np.testing.assert_array_equal(lev_g, lev_o)
+        np.testing.assert_array_equal(ord_g, ord_o)
+        assert mx_g == mx_o
+    info = s.info()
+    assert info.levels_lower == oracle.levels(lrp, lci, True)[2] + 1
+
+
+@pytest.mark.parametrize("name", list(PROBLEMS))
+@pytest.mark.parametrize("nrhs", [1, 3, 8, 13, 32, 100, 128])
+def test_sweeps_match_oracle(cuda, name, nrhs):
+    """FP64 solve == oracle FP64 sweeps (rel 1e-12); FP32 solve within 1e-5
+    of the oracle's FP32 sweeps, on the same factor."""
+    from cholespy_gb300 import CholeskySolverD, CholeskySolverF
+    torch = cuda
+    n, vals, idx = PROBLEMS[name]()
+    rng = np.random.default_rng(nrhs)
+    b = rng.standard_normal((n, nrhs))
+    sd = _make(torch, n, vals, idx, CholeskySolverD)
+    perm, colptr, rowidx, lv = sd.factor()
+    xo = oracle.reference_solve(perm, colptr, rowidx, lv, b, np.float64)
+    bt = torch.tensor(b, device="cuda")
+    xt = torch.zeros_like(bt)
+    sd.solve(bt, xt)
+    sd.check()
+    err = np.abs(xt.cpu().numpy() - xo).max() / np.abs(xo).max()
+    assert err <= 1e-12, err
+    sf = _make(torch, n, vals, idx, CholeskySolverF)
+    xo32 = oracle.reference_solve(perm, colptr, rowidx, lv, b.astype(np.float32), np.float32)
+    bt32 = torch.tensor(b.astype(np.float32), device="cuda")
+    xt32 = torch.zeros_like(bt32)
+    sf.solve(bt32, xt32)
+    sf.check()
+    err32 = np.abs(xt32.cpu().numpy().astype(np.float64) - xo32).max() / np.abs(xo32).max()
+    assert err32 <= 1e-5, err32
+
+
+def test_vector_rhs_and_alias(cuda):
+    from cholespy_gb300 import CholeskySolverD
+    torch = cuda
+    n, vals, idx = PROBLEMS["grid64"]()
+    s = _make(torch, n, vals, idx, CholeskySolverD)
+    A = sym_matrix(n, vals, idx)
+    b = np.random.default_rng(0).standard_normal(n)
+    bt = torch.tensor(b, device="cuda")
+    xt = torch.zeros_like(bt)
+    s.solve(bt, xt)
+    x = xt.cpu().numpy()
+    assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-12
+    # b and x may alias (the lower sweep consumes b before x is written)
+    s.solve(bt, bt)
+    np.testing.assert_allclose(bt.cpu().numpy(), x, rtol=1e-13, atol=1e-14)
+
+
+def test_dense_oracle_grid64(cuda):
+    """64x64 5-point Laplacian, A = I + 10 L, one N(0,1) RHS (seed 0):
+    CholeskySolverD against an FP64 dense solve."""
+    from cholespy_gb300 import CholeskySolverD, workloads
+    torch = cuda
+    n, vals, idx, b = workloads.config_grid64()
+    s = _make(torch, n, vals, idx, CholeskySolverD)
+    bt = torch.tensor(b, device="cuda")
+    xt = torch.zeros_like(bt)
+    s.solve(bt, xt)
+    xd = np.linalg.solve(sym_matrix(n, vals, idx).toarray(), b)
+    rel = np.abs(xt.cpu().numpy() - xd).max() / np.abs(xd).max()
+    assert rel < 1e-12, rel
+
+
+@pytest.mark.parametrize("nrhs", [1, 32, 128])
+def test_refined_solve(cuda, nrhs):
+    """FP32 factor + FP64 refinement reaches 1e-10 relative residual."""
+    from cholespy_gb300 import CholeskySolverD, MatrixType, workloads
+    torch = cuda
+    n, vals, idx = 4096, *workloads.grid3d_coo(16, 1e-3)
+    s = CholeskySolverD(n, torch.tensor(idx[0], device="cuda"), torch.tensor(idx[1], device="cuda"),
+                        torch.tensor(vals, device="cuda"), MatrixType.COO, refine=True)
+    b = np.random.default_rng(2).standard_normal((n, nrhs))
+    bt = torch.tensor(b, device="cuda")
+    xt = torch.zeros_like(bt)
+    st = s.solve_refined(bt, xt, tol=1e-10, max_iter=10)
+    assert st.converged and st.max_rel_residual <= 1e-10
+    A = sym_matrix(n, vals, idx)
+    x = xt.cpu().numpy()
+    res = np.linalg.norm(b - A @ x, axis=0) / np.linalg.norm(b, axis=0)
+    assert res.max() <= 1e-10
+    # agrees with the plain FP64 solve
+    x64 = torch.zeros_like(bt)
+    s.solve_fp64(bt, x64)
+    assert np.abs(x64.cpu().numpy() - x).max() / np.abs(x).max() < 1e-9
+    # solve() on a refine=True solver also refines
+    x2 = torch.zeros_like(bt)
+    s.solve(bt, x2)
+    np.testing.assert_allclose(x2.cpu().numpy(), x, rtol=0, atol=1e-12 * np.abs(x).max())
+
+
+def test_errors(cuda):
+    from cholespy_gb300 import CholeskySolverF, MatrixType
+    torch = cuda
+    n, vals, idx, _ = reference_problem("cube")
+    s = _make(torch, n, vals, idx, CholeskySolverF)
+    b = torch.zeros(n, 3, device="cuda")
+    with pytest.raises(ValueError, match="same dimensions"):
+        s.solve(b, torch.zeros(n, 4, device="cuda"))
+    with pytest.raises(ValueError, match="Expected 1D or 2D"):
+        s.solve(torch.zeros(n, 1, 1, device="cuda"), torch.zeros(n, 1, 1, device="cuda"))
+    with pytest.raises(ValueError, match="same device"):
+        s.solve(b, torch.zeros(n, 3))
+    with pytest.raises(TypeError):
+        s.solve(b.double(), torch.zeros(n, 3, device="cuda", dtype=torch.float64))
+    with pytest.raises(ValueError, match="positive definite"):
+        ii = torch.tensor([0, 1, 1, 0], device="cuda")
+        CholeskySolverF(2, ii, torch.tensor([0, 1, 0, 1], device="cuda"),
+                        torch.tensor([1.0, 1.0, 3.0, 3.0], dtype=torch.float64, device="cuda"),
+                        MatrixType.COO)
+    with pytest.raises(ValueError, match="same size"):
+        CholeskySolverF(2, torch.tensor([0], device="cuda"), torch.tensor([0, 1], device="cuda"),
+                        torch.tensor([1.0, 1.0], dtype=torch.float64, device="cuda"), MatrixType.COO)
+
+
+def test_side_stream(cuda):
+    from cholespy_gb300 import CholeskySolverF
+    torch = cuda
+    n, vals, idx = PROBLEMS["ico4"]()
+    s = _make(torch, n, vals, idx, CholeskySolverF)
+    b = torch.rand(n, 16, device="cuda")
+    ref = torch.zeros_like(b)
+    s.solve(b, ref)
+    st = torch.cuda.Stream()
+    st.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(st):
+        x = torch.zeros_like(b)
+        for _ in range(3):
+            s.solve(b, x)
+    torch.cuda.current_stream().wait_stream(st)
+    torch.cuda.synchronize()
+    assert torch.equal(x, ref)

@@ -1,0 +1,113 @@
+"""CPU tests of the product's host factorisation (the CHOLMOD replacement)
+through the C ABI, checked against the oracle's up-looking LL^T on the same
+permutation, and of the input checks."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle
+from cholespy_gb300 import _ffi, workloads
+
+
+def factorize(gblib, n, ii, jj, x, fmt, threads=2):
+    ii = np.ascontiguousarray(ii, np.int32)
+    jj = np.ascontiguousarray(jj, np.int32)
+    x = np.ascontiguousarray(x, np.float64)
+    f = C.c_void_p()
+    st = gblib.gbchol_factorize(n, len(x), ii.ctypes.data, jj.ctypes.data, x.ctypes.data, fmt,
+                                threads, C.byref(f))
+    _ffi.check(st)
+    nn, nnz, nsn, fl = C.c_int32(), C.c_int64(), C.c_int32(), C.c_double()
+    _ffi.check(gblib.gbchol_factor_info(f, C.byref(nn), C.byref(nnz), C.byref(nsn), C.byref(fl)))
+    perm = np.zeros(n, np.int32)
+    colptr = np.zeros(n + 1, np.int32)
+    rowidx = np.zeros(nnz.value, np.int32)
+    vals = np.zeros(nnz.value, np.float64)
+    _ffi.check(gblib.gbchol_factor_export(f, perm.ctypes.data, colptr.ctypes.data,
+                                          rowidx.ctypes.data, vals.ctypes.data))
+    gblib.gbchol_factor_free(f)
+    return perm, colptr, rowidx, vals, nsn.value
+
+
+CASES = {
+    "cube": lambda: (8, *workloads.laplacian_coo(*workloads.cube(), 2.0)),
+    "ico3": lambda: (642, *workloads.laplacian_coo(*workloads.icosphere(3)[:2], 2.0)),
+    "grid24": lambda: (576, *workloads.grid2d_coo(24, 10.0, 1.0)),
+    "grid3d_10": lambda: (1000, *workloads.grid3d_coo(10, 1e-3)),
+}
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_factor_matches_oracle(gblib, case):
+    n, vals, idx = CASES[case]()
+    perm, colptr, rowidx, lv, nsn = factorize(gblib, n, idx[0], idx[1], vals, 2)
+    assert sorted(perm) == list(range(n))
+    cp, ri, av = oracle.build_csc(n, idx[0], idx[1], vals, 2)
+    Lp, Li, Lx = oracle.cholesky(n, cp, ri, av, perm)
+    np.testing.assert_array_equal(colptr, Lp)       # same symbolic pattern
+    np.testing.assert_array_equal(rowidx, Li)
+    np.testing.assert_allclose(lv, Lx, rtol=1e-11, atol=1e-13)
+    # diagonal first in every column
+    assert all(rowidx[colptr[j]] == j for j in range(n))
+    assert 1 <= nsn <= n
+
+
+@pytest.mark.parametrize("fmt", ["COO", "CSR", "CSC"])
+def test_factor_input_formats_agree(gblib, fmt):
+    n, vals, idx = CASES["ico3"]()
+    if fmt == "COO":
+        args = (idx[0], idx[1], vals, 2)
+    elif fmt == "CSR":
+        m = sp.csr_matrix((vals, (idx[0], idx[1])), shape=(n, n))
+        args = (m.indptr, m.indices, m.data, 1)
+    else:
+        m = sp.csc_matrix((vals, (idx[0], idx[1])), shape=(n, n))
+        args = (m.indptr, m.indices, m.data, 0)
+    perm, colptr, rowidx, lv, _ = factorize(gblib, n, *args)
+    p0, c0, r0, v0, _ = factorize(gblib, n, idx[0], idx[1], vals, 2)
+    np.testing.assert_array_equal(perm, p0)
+    np.testing.assert_array_equal(colptr, c0)
+    np.testing.assert_allclose(lv, v0, rtol=1e-13, atol=1e-15)
+
+
+def test_factor_uses_lower_triangle_only(gblib):
+    """CHOLMOD is called with stype = -1: strictly upper entries are ignored."""
+    n, vals, idx = CASES["grid24"]()
+    upper = idx[0] < idx[1]
+    junk = vals.copy()
+    junk[upper] = 123.0
+    a = factorize(gblib, n, idx[0], idx[1], vals, 2)
+    b = factorize(gblib, n, idx[0], idx[1], junk, 2)
+    np.testing.assert_array_equal(a[3], b[3])
+
+
+def test_factor_not_posdef(gblib):
+    vals = np.array([1.0, 3.0, 3.0, 1.0])
+    ii = np.array([0, 1, 0, 1])
+    jj = np.array([0, 0, 1, 1])
+    with pytest.raises(ValueError, match="^Matrix is not positive definite!$"):
+        factorize(gblib, 2, ii, jj, vals, 2)
+
+
+def test_factor_bad_indices(gblib):
+    with pytest.raises(ValueError):
+        factorize(gblib, 3, [0, 3], [0, 1], [1.0, 1.0], 2)
+    with pytest.raises(ValueError):
+        factorize(gblib, 2, [0, 2, 1], [0, 1], [1.0, 1.0], 1)  # non-monotone pointers
+
+
+def test_factor_threads_deterministic(gblib):
+    n, vals, idx = CASES["grid3d_10"]()
+    a = factorize(gblib, n, idx[0], idx[1], vals, 2, threads=1)
+    b = factorize(gblib, n, idx[0], idx[1], vals, 2, threads=4)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_allclose(a[3], b[3], rtol=1e-12, atol=1e-14)
+
+
+def test_nested_dissection_fill_reasonable(gblib):
+    """Fill of the 3-D 7-point grid stays far below the dense bound."""
+    n, vals, idx = 4096, *workloads.grid3d_coo(16, 1e-3)
+    _, colptr, _, _, nsn = factorize(gblib, n, idx[0], idx[1], vals, 2)
+    assert colptr[-1] < 400_000  # METIS-quality ND gives ~3.9e5 on 16^3
