@@ -334,7 +334,8 @@ def run_ours(args, world, rank, local):
                "sample": f"{sample} of {args.nrhs} RHS columns, one FP64 solve "
                          "(cholmod_solve semantics) on the same factor, RHS split over threads"}
 
-    launches = 2 + (args.max_iter + 1) + 2 * args.max_iter
+    lps = info.launches_per_solve
+    launches = lps + (args.max_iter + 1) + args.max_iter * lps
     line = {
         "metric": "RHS-solves/s (FP32 factor + FP64 iterative refinement to 1e-10)",
         "value": value, "unit": "RHS-solves/s", "n_gpus": world, "steps": args.steps,
@@ -343,6 +344,8 @@ def run_ours(args, world, rank, local):
         "config": config_dict(args, n, len(vals), info.nnz_l,
                               {"levels_lower": info.levels_lower, "levels_upper": info.levels_upper,
                                "supernodes": info.n_supernodes, "max_supernode": info.max_supernode,
+                               "top_rows": info.top_rows, "top_units": info.top_units,
+                               "top_blocks": info.top_blocks,
                                "factor_s": info.factor_seconds, "analysis_s": info.analysis_seconds,
                                "ctor_s": t_ctor, "parallelism": f"replicas x{world}"}),
         "refine": {"iterations": stats.iterations, "converged": stats.converged,

@@ -31,6 +31,10 @@ class Info(C.Structure):
         ("factor_seconds", C.c_double),
         ("analysis_seconds", C.c_double),
         ("store", C.c_int32),
+        ("top_rows", C.c_int32),
+        ("top_units", C.c_int32),
+        ("top_blocks", C.c_int64),
+        ("launches_per_solve", C.c_int32),
     ]
 
 

@@ -18,8 +18,10 @@
 
 #include "gbchol.h"
 #include "host/host.h"
+#include "host/plan.h"
 #include "kernels.h"
 #include "refine.h"
+#include "solve_sn.h"
 
 using namespace gbchol;
 
@@ -105,7 +107,16 @@ struct gbchol_solver {
     int64_t nnz_a = 0;
     double t_factor = 0.0, t_analysis = 0.0;
     DevBuf<int32_t> perm;
-    Triangle lower, upper;    // CSR of L (diagonal last), CSR of L^T (diagonal first)
+    Triangle lower, upper;    // level analysis of L (CSR, diagonal last) and L^T
+    // solve plan (see host/plan.cpp)
+    SolvePlan plan;
+    DevBuf<int32_t> lo_rowptr, lo_cols, lo_tasks, up_rowptr, up_cols, up_tasks, sn_rows;
+    DevBuf<float> lo_v32, up_v32, pan32;
+    DevBuf<double> lo_v64, up_v64, pan64;
+    DevBuf<SnUnit> units;
+    DevBuf<SnContrib> contribs;
+    DevBuf<int32_t> uflags;   // units * 4 RHS slices
+    std::vector<int32_t> flags_init;  // 0 for leaf rows, INT_MAX for top rows
     DevBuf<int32_t> a_rowptr, a_cols;
     DevBuf<double> a_vals;    // symmetric A, original ordering
     DevBuf<int32_t> flags, status;
@@ -119,7 +130,13 @@ struct gbchol_solver {
 
     int next_epoch(cudaStream_t s) {
         if (epoch >= INT_MAX - 8) {
-            cudaMemsetAsync(flags.p, 0, sizeof(int32_t) * (size_t)std::max(n, 1), s);
+            if (!flags_init.empty())
+                cudaMemcpyAsync(flags.p, flags_init.data(), sizeof(int32_t) * flags_init.size(),
+                                cudaMemcpyHostToDevice, s);
+            else
+                cudaMemsetAsync(flags.p, 0, sizeof(int32_t) * (size_t)std::max(n, 1), s);
+            if (uflags.p) cudaMemsetAsync(uflags.p, 0, sizeof(int32_t) * uflags.count, s);
+            cudaStreamSynchronize(s);
             epoch = 0;
         }
         return ++epoch;
@@ -207,6 +224,77 @@ int analyze_triangle(gbchol_solver* h, Triangle& t, bool lower) {
     return GBCHOL_OK;
 }
 
+template <typename T>
+cudaError_t upload_cast(DevBuf<T>& dst, const std::vector<double>& src) {
+    std::vector<T> tmp(src.size());
+    for (size_t k = 0; k < src.size(); ++k) tmp[k] = (T)src[k];
+    return dst.upload(tmp.data(), tmp.size());
+}
+
+// Builds the solve plan from the factor and the level orders and uploads it.
+int setup_plan(gbchol_solver* h, const std::vector<int32_t>& rp, const std::vector<int32_t>& ci,
+               const std::vector<double>& rv) {
+    (void)rp; (void)ci; (void)rv;
+    const Factor& F = h->F;
+    const int32_t n = F.n;
+    SolvePlan& P = h->plan;
+    try {
+        build_plan(F, h->lower.order_h, h->upper.order_h, PlanOptions(), P);
+    } catch (const std::exception& ex) {
+        return fail(GBCHOL_EINTERNAL, std::string("solve plan: ") + ex.what());
+    }
+    const bool f32 = h->store & GBCHOL_STORE_F32, f64 = h->store & GBCHOL_STORE_F64;
+    // lower leaf sweep: leaf rows + the leaf part of the top rows
+    CUDA_TRY(h->lo_rowptr.upload(P.lo_rowptr.data(), P.lo_rowptr.size()));
+    CUDA_TRY(h->lo_cols.upload(P.lo_cols.data(), P.lo_cols.size()));
+    CUDA_TRY(h->lo_tasks.upload(P.lo_tasks.data(), P.lo_tasks.size()));
+    if (f32) CUDA_TRY(upload_cast(h->lo_v32, P.lo_vals));
+    if (f64) CUDA_TRY(h->lo_v64.upload(P.lo_vals.data(), P.lo_vals.size()));
+    // upper leaf sweep: columns of L for leaf rows only (top rows: empty)
+    {
+        std::vector<int32_t> uptr((size_t)n + 1, 0), ucol;
+        std::vector<double> uval;
+        for (int32_t j = 0; j < n; ++j)
+            uptr[j + 1] = uptr[j] + (P.row_top[j] ? 0 : F.colptr[j + 1] - F.colptr[j]);
+        ucol.reserve((size_t)uptr[n]);
+        uval.reserve((size_t)uptr[n]);
+        for (int32_t j = 0; j < n; ++j) {
+            if (P.row_top[j]) continue;
+            ucol.insert(ucol.end(), F.rowidx.begin() + F.colptr[j], F.rowidx.begin() + F.colptr[j + 1]);
+            uval.insert(uval.end(), F.vals.begin() + F.colptr[j], F.vals.begin() + F.colptr[j + 1]);
+        }
+        CUDA_TRY(h->up_rowptr.upload(uptr.data(), uptr.size()));
+        CUDA_TRY(h->up_cols.upload(ucol.data(), ucol.size()));
+        if (f32) CUDA_TRY(upload_cast(h->up_v32, uval));
+        if (f64) CUDA_TRY(h->up_v64.upload(uval.data(), uval.size()));
+    }
+    CUDA_TRY(h->up_tasks.upload(P.up_tasks.data(), P.up_tasks.size()));
+    // top region
+    CUDA_TRY(h->sn_rows.upload(P.sn_rows.data(), P.sn_rows.size()));
+    if (f32) CUDA_TRY(upload_cast(h->pan32, P.panels));
+    if (f64) CUDA_TRY(h->pan64.upload(P.panels.data(), P.panels.size()));
+    CUDA_TRY(h->units.upload(P.units.data(), P.units.size()));
+    CUDA_TRY(h->contribs.upload(P.contribs.data(), P.contribs.size()));
+    CUDA_TRY(h->uflags.alloc(std::max<size_t>(1, P.units.size() * 4)));
+    CUDA_TRY(cudaMemset(h->uflags.p, 0, sizeof(int32_t) * h->uflags.count));
+    // row flags: top rows are always "ready" for the row kernels (they are
+    // solved by the supernodal kernel in an earlier launch)
+    h->flags_init.assign((size_t)n, 0);
+    for (int32_t j = 0; j < n; ++j)
+        if (P.row_top[j]) h->flags_init[j] = INT_MAX;
+    CUDA_TRY(cudaMemcpy(h->flags.p, h->flags_init.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    P.panels.clear();
+    P.panels.shrink_to_fit();
+    P.lo_vals.clear();
+    P.lo_vals.shrink_to_fit();
+    // the analysis copies of the triangles are not used by the solves
+    h->lower.v32.release(); h->lower.v64.release();
+    h->upper.v32.release(); h->upper.v64.release();
+    h->lower.rowptr.release(); h->lower.cols.release();
+    h->upper.rowptr.release(); h->upper.cols.release();
+    return GBCHOL_OK;
+}
+
 // Uploads the factor (both triangles) and runs the analysis.
 int setup_device(gbchol_solver* h) {
     auto t0 = std::chrono::steady_clock::now();
@@ -228,22 +316,12 @@ int setup_device(gbchol_solver* h) {
     transpose(n, F.colptr, F.rowidx, F.vals, rp, ci, rv);
     CUDA_TRY(h->lower.rowptr.upload(rp.data(), rp.size()));
     CUDA_TRY(h->lower.cols.upload(ci.data(), ci.size()));
-    if (h->store & GBCHOL_STORE_F64) {
-        CUDA_TRY(h->lower.v64.upload(rv.data(), rv.size()));
-        CUDA_TRY(h->upper.v64.upload(F.vals.data(), F.vals.size()));
-    }
-    if (h->store & GBCHOL_STORE_F32) {
-        // FP64 -> FP32 cast on the host (src/cholesky_solver.cpp:257-271)
-        std::vector<float> f(rv.size());
-        for (size_t k = 0; k < rv.size(); ++k) f[k] = (float)rv[k];
-        CUDA_TRY(h->lower.v32.upload(f.data(), f.size()));
-        for (size_t k = 0; k < F.vals.size(); ++k) f[k] = (float)F.vals[k];
-        CUDA_TRY(h->upper.v32.upload(f.data(), f.size()));
-    }
     if (n > 0) {
         int rc = analyze_triangle(h, h->lower, true);
         if (rc) return rc;
         rc = analyze_triangle(h, h->upper, false);
+        if (rc) return rc;
+        rc = setup_plan(h, rp, ci, rv);
         if (rc) return rc;
     }
     CUDA_TRY(cudaDeviceSynchronize());
@@ -270,19 +348,63 @@ int check_rhs(int32_t nrhs) {
     return GBCHOL_OK;
 }
 
-RowSweepArgs sweep_args(gbchol_solver* h, const Triangle& t, bool f32, int nrhs) {
-    RowSweepArgs a;
-    a.n = h->n;
-    a.nrhs = nrhs;
-    a.rowptr = t.rowptr.p;
-    a.cols = t.cols.p;
-    a.vals = f32 ? (const void*)t.v32.p : (const void*)t.v64.p;
-    a.order = t.order.p;
-    a.perm = h->perm.p;
-    a.tmp = h->tmp.p;
-    a.flags = h->flags.p;
-    a.status = h->status.p;
-    return a;
+// One full solve: leaf rows (lower) -> top units (lower) -> top units
+// (upper) -> leaf rows (upper). `in` is read through perm by the lower leaf
+// kernel; `out` is written through perm by both upper kernels.
+int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in, void* out,
+               const int* skip, cudaStream_t s) {
+    const SolvePlan& P = h->plan;
+    RowSweepArgs lo;
+    lo.n = h->n;
+    lo.ntasks = (int)P.lo_tasks.size();
+    lo.nrhs = nrhs;
+    lo.rowptr = h->lo_rowptr.p;
+    lo.cols = h->lo_cols.p;
+    lo.vals = f32 ? (const void*)h->lo_v32.p : (const void*)h->lo_v64.p;
+    lo.order = h->lo_tasks.p;
+    lo.perm = h->perm.p;
+    lo.in = in;
+    lo.tmp = h->tmp.p;
+    lo.flags = h->flags.p;
+    lo.status = h->status.p;
+    lo.skip = skip;
+    lo.epoch = h->next_epoch(s);
+    CUDA_TRY(launch_row_sweep(lo, true, io, s));
+    SnSweepArgs sn;
+    sn.n_units = (int)P.units.size();
+    sn.nslices = sn_slices(nrhs);
+    sn.nrhs = nrhs;
+    sn.units = h->units.p;
+    sn.contribs = h->contribs.p;
+    sn.sn_rows = h->sn_rows.p;
+    sn.panels = f32 ? (const void*)h->pan32.p : (const void*)h->pan64.p;
+    sn.perm = h->perm.p;
+    sn.tmp = h->tmp.p;
+    sn.uflags = h->uflags.p;
+    sn.status = h->status.p;
+    sn.skip = skip;
+    sn.epoch = h->next_epoch(s);
+    CUDA_TRY(launch_sn_sweep(sn, true, io, s));
+    sn.out = out;
+    sn.epoch = h->next_epoch(s);
+    CUDA_TRY(launch_sn_sweep(sn, false, io, s));
+    RowSweepArgs up = lo;
+    up.ntasks = (int)P.up_tasks.size();
+    up.rowptr = h->up_rowptr.p;
+    up.cols = h->up_cols.p;
+    up.vals = f32 ? (const void*)h->up_v32.p : (const void*)h->up_v64.p;
+    up.order = h->up_tasks.p;
+    up.in = nullptr;
+    up.out = out;
+    up.epoch = h->next_epoch(s);
+    CUDA_TRY(launch_row_sweep(up, false, io, s));
+    return GBCHOL_OK;
+}
+
+// Kernel launches of one run_sweeps call.
+int sweep_launches(const gbchol_solver* h) {
+    const SolvePlan& P = h->plan;
+    return (P.lo_tasks.empty() ? 0 : 1) + (P.units.empty() ? 0 : 2) + (P.up_tasks.empty() ? 0 : 1);
 }
 
 }  // namespace
@@ -436,14 +558,7 @@ int gbchol_solve(gbchol_handle h, int32_t precision, int32_t nrhs, const void* b
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (int rc = ensure_tmp(h, (size_t)h->n * nrhs * (f32 ? sizeof(float) : sizeof(double)))) return rc;
     const SweepIO io = f32 ? SweepIO::F32 : SweepIO::F64;
-    RowSweepArgs lo = sweep_args(h, h->lower, f32, nrhs);
-    lo.in = b;
-    lo.epoch = h->next_epoch(s);
-    CUDA_TRY(launch_row_sweep(lo, true, io, s));
-    RowSweepArgs up = sweep_args(h, h->upper, f32, nrhs);
-    up.out = x;
-    up.epoch = h->next_epoch(s);
-    CUDA_TRY(launch_row_sweep(up, false, io, s));
+    if (int rc = run_sweeps(h, f32, io, nrhs, b, x, nullptr, s)) return rc;
     h->last_stream = s;
     return GBCHOL_OK;
 }
@@ -472,14 +587,7 @@ int gbchol_solve_refined(gbchol_handle h, int32_t nrhs, const double* b, double*
     if (!h->rstate.p) CUDA_TRY(h->rstate.alloc(1));
     CUDA_TRY(cudaMemsetAsync(h->rstate.p, 0, sizeof(RefineState), s));
     // x0 = A32^{-1} b
-    RowSweepArgs lo = sweep_args(h, h->lower, true, nrhs);
-    lo.in = b;
-    lo.epoch = h->next_epoch(s);
-    CUDA_TRY(launch_row_sweep(lo, true, SweepIO::F32_MIXED, s));
-    RowSweepArgs up = sweep_args(h, h->upper, true, nrhs);
-    up.out = x;
-    up.epoch = h->next_epoch(s);
-    CUDA_TRY(launch_row_sweep(up, false, SweepIO::F32_MIXED, s));
+    if (int rc = run_sweeps(h, true, SweepIO::F32_MIXED, nrhs, b, x, nullptr, s)) return rc;
     ResidualArgs ra;
     ra.n = n;
     ra.nrhs = nrhs;
@@ -500,16 +608,7 @@ int gbchol_solve_refined(gbchol_handle h, int32_t nrhs, const double* b, double*
         ra.first = it == 0;
         CUDA_TRY(launch_residual(ra, grid, s));
         if (it == max_iter) break;
-        RowSweepArgs l2 = sweep_args(h, h->lower, true, nrhs);
-        l2.in = h->r64.p;
-        l2.skip = conv;
-        l2.epoch = h->next_epoch(s);
-        CUDA_TRY(launch_row_sweep(l2, true, SweepIO::F32_REFINE, s));
-        RowSweepArgs u2 = sweep_args(h, h->upper, true, nrhs);
-        u2.out = x;
-        u2.skip = conv;
-        u2.epoch = h->next_epoch(s);
-        CUDA_TRY(launch_row_sweep(u2, false, SweepIO::F32_REFINE, s));
+        if (int rc = run_sweeps(h, true, SweepIO::F32_REFINE, nrhs, h->r64.p, x, conv, s)) return rc;
     }
     h->last_stream = s;
     if (stats) {
@@ -541,6 +640,10 @@ int gbchol_get_info(gbchol_handle h, gbchol_info* out) {
     i.factor_seconds = h->t_factor;
     i.analysis_seconds = h->t_analysis;
     i.store = h->store;
+    i.top_rows = h->plan.n_top_rows;
+    i.top_units = (int32_t)h->plan.units.size();
+    i.top_blocks = (int64_t)h->plan.contribs.size();
+    i.launches_per_solve = sweep_launches(h);
     *out = i;
     return GBCHOL_OK;
 }

@@ -1,0 +1,173 @@
+// Solve plan: splits the factor into a leaf region (row-wise sweeps) and a
+// top region (supernodal sweeps on dense panels), and lists the work units
+// and dense contribution blocks of the supernodal sweeps.
+//
+// Top region: every fundamental supernode at least `min_top_width` columns
+// wide, plus all its ancestors (so the region is closed upwards: a top
+// supernode's off-diagonal rows are top rows). Its columns are stored as
+// dense column-major panels of (columns + off-diagonal rows) x columns and
+// cut into chunks of kChunk columns, one work unit each.
+//
+// Lower sweep (L y = b):   leaf rows solve row by row; each top row first
+//   receives b minus its leaf-column terms (row kernel, "partial" task), then
+//   each top unit pulls the dense blocks L[unit rows, source chunk] of every
+//   source chunk whose rows hit it and solves its diagonal block.
+// Upper sweep (L^T x = y): each top unit subtracts L[below rows, unit]^T x
+//   over the rows below its diagonal block (all top rows, solved earlier),
+//   then solves its diagonal block; the leaf rows follow row by row.
+#include "plan.h"
+
+#include <algorithm>
+#include <stdexcept>
+
+namespace gbchol {
+
+void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
+                const std::vector<int32_t>& upper_order, const PlanOptions& opt, SolvePlan& P) {
+    const int32_t n = F.n;
+    P = SolvePlan();
+    P.n = n;
+    P.sn_start = F.sn_start;
+    const int32_t nsn = (int32_t)P.sn_start.size() - 1;
+    std::vector<int32_t> sn_of((size_t)n);
+    for (int32_t s = 0; s < nsn; ++s)
+        for (int32_t j = P.sn_start[s]; j < P.sn_start[s + 1]; ++j) sn_of[j] = s;
+    std::vector<int32_t> sn_parent((size_t)nsn, -1);
+    for (int32_t s = 0; s < nsn; ++s) {
+        int32_t last = P.sn_start[s + 1] - 1;
+        int32_t p = F.colptr[last + 1] - F.colptr[last] > 1 ? F.rowidx[F.colptr[last] + 1] : -1;
+        sn_parent[s] = p >= 0 ? sn_of[p] : -1;
+    }
+    // ---- top region: wide supernodes and their ancestors -------------------
+    P.sn_top.assign((size_t)nsn, 0);
+    for (int32_t s = 0; s < nsn; ++s)
+        if (P.sn_start[s + 1] - P.sn_start[s] >= opt.min_top_width) P.sn_top[s] = 1;
+    for (int32_t s = 0; s < nsn; ++s)  // parents have larger indices (postorder)
+        if (P.sn_top[s] && sn_parent[s] >= 0) P.sn_top[sn_parent[s]] = 1;
+    P.row_top.assign((size_t)n, 0);
+    for (int32_t j = 0; j < n; ++j) P.row_top[j] = P.sn_top[sn_of[j]];
+    for (int32_t j = 0; j < n; ++j) P.n_top_rows += P.row_top[j];
+
+    // ---- panels, row lists and units ---------------------------------------
+    std::vector<int32_t> unit_of_col((size_t)n, -1);
+    std::vector<int32_t> first_unit((size_t)nsn, -1), unit_count((size_t)nsn, 0);
+    std::vector<int64_t> rows_off((size_t)nsn, -1), panel_off((size_t)nsn, -1);
+    for (int32_t s = 0; s < nsn; ++s) {
+        if (!P.sn_top[s]) continue;
+        const int32_t f = P.sn_start[s], l1 = P.sn_start[s + 1], w = l1 - f;
+        const int32_t ld = F.colptr[f + 1] - F.colptr[f];
+        rows_off[s] = (int64_t)P.sn_rows.size();
+        P.sn_rows.insert(P.sn_rows.end(), F.rowidx.begin() + F.colptr[f],
+                         F.rowidx.begin() + F.colptr[f + 1]);
+        panel_off[s] = (int64_t)P.panels.size();
+        P.panels.resize(P.panels.size() + (size_t)ld * w, 0.0);
+        const int32_t* rows = P.sn_rows.data() + rows_off[s];
+        for (int32_t j = 0; j < w; ++j) {
+            const int32_t c = f + j;
+            const int32_t cnt = F.colptr[c + 1] - F.colptr[c];
+            if (cnt != ld - j) throw std::runtime_error("supernode structure mismatch");
+            double* dst = P.panels.data() + panel_off[s] + (int64_t)j * ld + j;
+            for (int32_t t = 0; t < cnt; ++t) {
+                if (F.rowidx[F.colptr[c] + t] != rows[j + t])
+                    throw std::runtime_error("supernode structure mismatch");
+                dst[t] = F.vals[F.colptr[c] + t];
+            }
+        }
+        first_unit[s] = (int32_t)P.units.size();
+        for (int32_t c0 = f; c0 < l1; c0 += kChunk) {
+            SnUnit u{};
+            u.c0 = c0;
+            u.w = std::min(kChunk, l1 - c0);
+            u.ld = ld;
+            u.pos0 = c0 - f;
+            u.panel_col_off = panel_off[s] + (int64_t)(c0 - f) * ld;
+            u.rows_off = rows_off[s];
+            u.upper_dep = -1;
+            for (int32_t c = c0; c < c0 + u.w; ++c) unit_of_col[c] = (int32_t)P.units.size();
+            P.units.push_back(u);
+            unit_count[s]++;
+        }
+    }
+    const int32_t nunits = (int32_t)P.units.size();
+    // upper-sweep dependency: the next chunk of the same supernode, else the
+    // first chunk of the parent supernode (whose completion implies every row
+    // below this supernode's diagonal block is solved)
+    for (int32_t s = 0; s < nsn; ++s) {
+        if (!P.sn_top[s]) continue;
+        for (int32_t k = 0; k < unit_count[s]; ++k) {
+            SnUnit& u = P.units[first_unit[s] + k];
+            if (k + 1 < unit_count[s]) u.upper_dep = first_unit[s] + k + 1;
+            else if (sn_parent[s] >= 0) u.upper_dep = first_unit[sn_parent[s]];
+        }
+    }
+    // lower-sweep contributions, gathered per destination unit in source order
+    std::vector<std::vector<SnContrib>> per_unit((size_t)nunits);
+    for (int32_t s = 0; s < nsn; ++s) {
+        if (!P.sn_top[s]) continue;
+        const int32_t f = P.sn_start[s], w = P.sn_start[s + 1] - f;
+        const int32_t ld = P.units[first_unit[s]].ld;
+        const int32_t* rows = P.sn_rows.data() + rows_off[s];
+        for (int32_t k = 0; k < unit_count[s]; ++k) {
+            const int32_t vu = first_unit[s] + k;
+            const SnUnit& V = P.units[vu];
+            // rows below V's diagonal block, grouped by destination unit
+            int32_t p = V.pos0 + V.w;
+            while (p < ld) {
+                const int32_t dst = unit_of_col[rows[p]];
+                if (dst < 0) throw std::runtime_error("top region not closed upwards");
+                int32_t q = p + 1;
+                while (q < ld && unit_of_col[rows[q]] == dst) ++q;
+                SnContrib c{};
+                c.panel_off = V.panel_col_off + p;
+                c.rows_off = rows_off[s] + p;
+                c.ld = ld;
+                c.xcol = V.c0;
+                c.nr = q - p;
+                c.w = V.w;
+                c.src_unit = vu;
+                per_unit[dst].push_back(c);
+                p = q;
+            }
+        }
+        (void)w;
+    }
+    for (int32_t u = 0; u < nunits; ++u) {
+        P.units[u].contrib_begin = (int32_t)P.contribs.size();
+        P.contribs.insert(P.contribs.end(), per_unit[u].begin(), per_unit[u].end());
+        P.units[u].contrib_end = (int32_t)P.contribs.size();
+    }
+
+    // ---- leaf region -------------------------------------------------------
+    // CSR of L (columns ascending, diagonal last)
+    std::vector<int32_t> rp, ci;
+    std::vector<double> rv;
+    transpose(n, F.colptr, F.rowidx, F.vals, rp, ci, rv);
+    P.lo_rowptr.assign((size_t)n + 1, 0);
+    for (int32_t i = 0; i < n; ++i) {
+        int32_t cnt = 0;
+        if (!P.row_top[i]) cnt = rp[i + 1] - rp[i];
+        else
+            for (int32_t k = rp[i]; k < rp[i + 1]; ++k) cnt += !P.row_top[ci[k]];
+        P.lo_rowptr[i + 1] = P.lo_rowptr[i] + cnt;
+    }
+    P.lo_cols.resize((size_t)P.lo_rowptr[n]);
+    P.lo_vals.resize((size_t)P.lo_rowptr[n]);
+    for (int32_t i = 0; i < n; ++i) {
+        int32_t d = P.lo_rowptr[i];
+        for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
+            if (P.row_top[i] && P.row_top[ci[k]]) continue;
+            P.lo_cols[d] = ci[k];
+            P.lo_vals[d] = rv[k];
+            ++d;
+        }
+        P.max_row_len = std::max(P.max_row_len, P.lo_rowptr[i + 1] - P.lo_rowptr[i]);
+    }
+    for (int32_t r : lower_order)
+        if (!P.row_top[r]) P.lo_tasks.push_back(r);
+    for (int32_t i = 0; i < n; ++i)
+        if (P.row_top[i]) P.lo_tasks.push_back(~i);
+    for (int32_t r : upper_order)
+        if (!P.row_top[r]) P.up_tasks.push_back(r);
+}
+
+}  // namespace gbchol

@@ -1,0 +1,70 @@
+// Solve plan of a factor: the split of L into a row-wise leaf region and a
+// supernodal top region, with the dense panel layout and the work units of
+// the supernodal sweeps. Built on the host once per factor.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "host.h"
+
+namespace gbchol {
+
+constexpr int kChunk = 32;  // columns per supernodal work unit (one warp lane per row)
+
+// One dense block L[rows, cols of a source chunk] applied to a unit in the
+// lower sweep: t[row - c0] -= L_block * x_src.
+struct SnContrib {
+    int64_t panel_off;  // element offset of the block's first (row, col) in the panel array
+    int64_t rows_off;   // offset into sn_rows of the block's first row index
+    int32_t ld;         // leading dimension of the source panel
+    int32_t xcol;       // first column (permuted index) of the source chunk
+    int32_t nr;         // rows of the block (<= kChunk)
+    int32_t w;          // columns of the block (<= kChunk)
+    int32_t src_unit;   // unit producing x_src (-1: same unit)
+    int32_t pad;
+};
+
+// A chunk of <= kChunk consecutive columns of one top-region supernode.
+struct SnUnit {
+    int32_t c0, w;          // columns [c0, c0 + w)
+    int32_t ld;             // rows of the supernode's panel (its columns + off-diagonal rows)
+    int32_t pos0;           // position of column c0 in the supernode's row list
+    int64_t panel_col_off;  // element offset of column c0 (row position 0) in the panel array
+    int64_t rows_off;       // offset of the supernode's row list in sn_rows
+    int32_t contrib_begin;  // lower-sweep contributions [begin, end)
+    int32_t contrib_end;
+    int32_t upper_dep;      // unit whose completion the upper sweep waits for (-1: none)
+    int32_t pad;
+};
+
+struct SolvePlan {
+    int32_t n = 0;
+    // supernodes (fundamental) and the top-region marking
+    std::vector<int32_t> sn_start;
+    std::vector<char> sn_top;
+    std::vector<char> row_top;            // column/row in the top region
+    int32_t n_top_rows = 0;
+    // top region: panels, row lists, units, contributions
+    std::vector<int32_t> sn_rows;         // concatenated row lists of top supernodes
+    std::vector<double> panels;           // column-major panels (FP64; cast for FP32)
+    std::vector<SnUnit> units;            // in lower topological order
+    std::vector<SnContrib> contribs;
+    // leaf region, lower sweep: CSR over all rows. Leaf rows hold their full
+    // row of L (diagonal last); top rows hold only their leaf-column entries.
+    std::vector<int32_t> lo_rowptr, lo_cols;
+    std::vector<double> lo_vals;
+    std::vector<int32_t> lo_tasks;        // leaf rows in level order, then ~row for top rows
+    std::vector<int32_t> up_tasks;        // leaf rows in L^T level order
+    int32_t max_row_len = 0;
+};
+
+struct PlanOptions {
+    int32_t min_top_width = 8;  // supernodes at least this wide (and their ancestors) are top
+};
+
+// Builds the plan from a factor and the level orders of L and L^T (rows
+// sorted by (level, row)).
+void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
+                const std::vector<int32_t>& upper_order, const PlanOptions& opt, SolvePlan& P);
+
+}  // namespace gbchol

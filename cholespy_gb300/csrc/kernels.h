@@ -22,11 +22,13 @@ cudaError_t launch_level_analysis(bool lower, int n, const int* rowptr, const in
 // Same arithmetic as solve_lower / solve_upper (kernels/kernels.cu:64-202).
 struct RowSweepArgs {
     int n = 0;
+    int ntasks = 0;               // entries of `order`
     int nrhs = 0;
     const int* rowptr = nullptr;
     const int* cols = nullptr;
     const void* vals = nullptr;   // T
-    const int* order = nullptr;   // rows sorted by (level, row)
+    const int* order = nullptr;   // rows in dependency order; ~row = partial row (lower
+                                  // sweep only): no diagonal, tmp[row] = in - sum
     const int* perm = nullptr;
     const void* in = nullptr;     // lower: right-hand side (TIn), read through perm
     void* tmp = nullptr;          // T, n x nrhs, permuted space

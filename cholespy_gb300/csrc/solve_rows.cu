@@ -69,11 +69,13 @@ __global__ void __launch_bounds__(256) sweep_nnz_kernel(RowSweepArgs a) {
     const T* tmp = static_cast<const T*>(a.tmp);
     const int nrhs = a.nrhs;
     if (a.skip && dev::ld_volatile(a.skip)) return;
-    for (int t = warp; t < a.n; t += nwarps) {
-        const int row = a.order[t];
+    for (int t = warp; t < a.ntasks; t += nwarps) {
+        const int task = a.order[t];
+        const bool partial = LOWER && task < 0;
+        const int row = partial ? ~task : task;
         const int s = a.rowptr[row], e = a.rowptr[row + 1];
         const int lo = LOWER ? s : s + 1;
-        const int hi = LOWER ? e - 1 : e;
+        const int hi = (LOWER && !partial) ? e - 1 : e;
         T acc[R];
 #pragma unroll
         for (int j = 0; j < R; ++j) acc[j] = T(0);
@@ -92,10 +94,11 @@ __global__ void __launch_bounds__(256) sweep_nnz_kernel(RowSweepArgs a) {
             T sj = dev::warp_sum(acc[j]);
             if (j == lane) mine = sj;
         }
-        const T diag = vals[LOWER ? e - 1 : s];
+        const T diag = partial ? T(1) : vals[LOWER ? e - 1 : s];
         const int prow = a.perm[row];
         if (lane < nrhs) {
-            T v = (load_rhs<io, LOWER>(a, row, prow, lane) - mine) / diag;
+            T v = load_rhs<io, LOWER>(a, row, prow, lane) - mine;
+            if (!partial) v = v / diag;
             emit<io, LOWER>(a, row, prow, lane, v);
             __threadfence();
         }
@@ -118,11 +121,13 @@ __global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
     const T* tmp = static_cast<const T*>(a.tmp);
     const int nrhs = a.nrhs;
     if (a.skip && dev::ld_volatile(a.skip)) return;
-    for (int t = warp; t < a.n; t += nwarps) {
-        const int row = a.order[t];
+    for (int t = warp; t < a.ntasks; t += nwarps) {
+        const int task = a.order[t];
+        const bool partial = LOWER && task < 0;
+        const int row = partial ? ~task : task;
         const int s = a.rowptr[row], e = a.rowptr[row + 1];
         const int lo = LOWER ? s : s + 1;
-        const int hi = LOWER ? e - 1 : e;
+        const int hi = (LOWER && !partial) ? e - 1 : e;
         T acc[Q];
 #pragma unroll
         for (int q = 0; q < Q; ++q) acc[q] = T(0);
@@ -130,15 +135,19 @@ __global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
             const int k = base + lane;
             const int mycol = k < hi ? a.cols[k] : 0;
             const T myv = k < hi ? vals[k] : T(0);
+            // every lane waits for its own entry, then the warp consumes the
+            // 32 entries without further waits (independent loads in flight)
+            if (k < hi) dev::wait_geq(a.flags + mycol, a.epoch, a.status);
+            __syncwarp();
             const int cnt = min(32, hi - base);
             const int steps = (cnt + NG - 1) / NG;
+#pragma unroll 4
             for (int st = 0; st < steps; ++st) {
                 const int eidx = st * NG + grp;
                 const bool valid = eidx < cnt;
                 const int col = __shfl_sync(0xffffffffu, mycol, valid ? eidx : 0);
                 const T v = __shfl_sync(0xffffffffu, myv, valid ? eidx : 0);
                 if (!valid) continue;
-                if (!dev::wait_geq(a.flags + col, a.epoch, a.status)) continue;
                 const T* xc = tmp + (size_t)col * nrhs;
 #pragma unroll
                 for (int q = 0; q < Q; ++q) {
@@ -153,14 +162,15 @@ __global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
 #pragma unroll
                 for (int o = G; o < 32; o <<= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
         }
-        const T diag = vals[LOWER ? e - 1 : s];
+        const T diag = partial ? T(1) : vals[LOWER ? e - 1 : s];
         const int prow = a.perm[row];
         if (grp == 0) {
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
                 const int j = sub + q * G;
                 if (j < nrhs) {
-                    T v = (load_rhs<io, LOWER>(a, row, prow, j) - acc[q]) / diag;
+                    T v = load_rhs<io, LOWER>(a, row, prow, j) - acc[q];
+                    if (!partial) v = v / diag;
                     emit<io, LOWER>(a, row, prow, j, v);
                 }
             }
@@ -186,7 +196,7 @@ cudaError_t launch_io(const RowSweepArgs& a, cudaStream_t stream) {
     int grid = 0;
     cudaError_t e = coop_grid(fn, 256, 0, &grid);
     if (e != cudaSuccess) return e;
-    const int need = (a.n + 7) / 8;
+    const int need = (a.ntasks + 7) / 8;
     if (grid > need) grid = need;
     RowSweepArgs copy = a;
     void* args[] = {&copy};
@@ -196,7 +206,7 @@ cudaError_t launch_io(const RowSweepArgs& a, cudaStream_t stream) {
 }  // namespace
 
 cudaError_t launch_row_sweep(const RowSweepArgs& a, bool lower, SweepIO io, cudaStream_t stream) {
-    if (a.n == 0) return cudaSuccess;
+    if (a.ntasks == 0) return cudaSuccess;
     switch (io) {
         case SweepIO::F32:
             return lower ? launch_io<IO<float, float, float, false>, true>(a, stream)

@@ -47,6 +47,10 @@ class SolverInfo:
     factor_flops: float
     factor_seconds: float
     analysis_seconds: float
+    top_rows: int = 0
+    top_units: int = 0
+    top_blocks: int = 0
+    launches_per_solve: int = 0
 
 
 @dataclass
@@ -253,7 +257,8 @@ class _CholeskySolver:
         _ffi.check(_ffi.lib().gbchol_get_info(self._h, C.byref(inf)))
         return SolverInfo(inf.n, inf.device, inf.nnz_a, inf.nnz_l, inf.levels_lower,
                           inf.levels_upper, inf.n_supernodes, inf.max_supernode,
-                          inf.factor_flops, inf.factor_seconds, inf.analysis_seconds)
+                          inf.factor_flops, inf.factor_seconds, inf.analysis_seconds,
+                          inf.top_rows, inf.top_units, inf.top_blocks, inf.launches_per_solve)
 
     def levels(self, lower=True):
         """(row_levels, order, max_lvl) of the analysis of L (lower) or L^T."""

@@ -156,6 +156,10 @@ typedef struct {
     double factor_seconds;    /* host factorisation time */
     double analysis_seconds;  /* device analysis time incl. uploads */
     int32_t store;
+    int32_t top_rows;         /* rows solved by the supernodal kernels */
+    int32_t top_units;        /* supernodal work units (<= 32 columns each) */
+    int64_t top_blocks;       /* dense contribution blocks of the lower sweep */
+    int32_t launches_per_solve;  /* kernel launches of one gbchol_solve */
 } gbchol_info;
 
 int gbchol_get_info(gbchol_handle h, gbchol_info* out);
