@@ -103,7 +103,8 @@ __global__ void __launch_bounds__(256) sweep_nnz_kernel(RowSweepArgs a) {
             __threadfence();
         }
         __syncwarp();
-        if (lane == 0) dev::st_release(a.flags + row, a.epoch);
+        // partial (top) rows publish nothing: their flags stay "always ready"
+        if (lane == 0 && !partial) dev::st_release(a.flags + row, a.epoch);
     }
 }
 
@@ -177,7 +178,8 @@ __global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
             __threadfence();
         }
         __syncwarp();
-        if (lane == 0) dev::st_release(a.flags + row, a.epoch);
+        // partial (top) rows publish nothing: their flags stay "always ready"
+        if (lane == 0 && !partial) dev::st_release(a.flags + row, a.epoch);
     }
 }
 
