@@ -39,9 +39,25 @@ __global__ void __launch_bounds__(256) level_kernel(int n, const int* __restrict
         const int lo = LOWER ? s : s + 1;
         const int hi = LOWER ? e - 1 : e;
         int lvl = 0;
-        for (int k = lo + lane; k < hi; k += 32) {
-            const int col = cols[k];
-            if (dev::wait_geq(flags + col, epoch, status)) lvl = max(lvl, __ldcg(levels + col) + 1);
+        // flags of 4 entries per lane are loaded together (independent
+        // relaxed loads); only entries not yet published take the bounded
+        // wait; one acquire fence then orders the level reads.
+        for (int base = lo; base < hi; base += 128) {
+            int c[4], f[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int k = base + lane + 32 * u;
+                c[u] = k < hi ? cols[k] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) f[u] = c[u] >= 0 ? dev::ld_volatile(flags + c[u]) : epoch;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (f[u] < epoch) dev::wait_geq(flags + c[u], epoch, status);
+            dev::fence_acquire();
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (c[u] >= 0) lvl = max(lvl, __ldcg(levels + c[u]) + 1);
         }
         lvl = dev::warp_max(lvl);
         local_max = max(local_max, lvl);

@@ -53,6 +53,12 @@ __device__ __forceinline__ bool wait_geq(const int* flag, int target, int* statu
     }
 }
 
+// Acquire fence: after relaxed/volatile loads that observed released flags,
+// orders the following loads after those observations (acquire pattern).
+__device__ __forceinline__ void fence_acquire() {
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
+
 // L2-coherent loads of values produced by other SMs during the same launch.
 template <typename T>
 __device__ __forceinline__ T ld_cg(const T* p) { return __ldcg(p); }

@@ -96,6 +96,8 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
         if (!P.sn_top[s]) continue;
         for (int32_t k = 0; k < unit_count[s]; ++k) {
             SnUnit& u = P.units[first_unit[s] + k];
+            u.sn_w = P.sn_start[s + 1] - P.sn_start[s];
+            u.parent_first_unit = sn_parent[s] >= 0 ? first_unit[sn_parent[s]] : -1;
             if (k + 1 < unit_count[s]) u.upper_dep = first_unit[s] + k + 1;
             else if (sn_parent[s] >= 0) u.upper_dep = first_unit[sn_parent[s]];
         }

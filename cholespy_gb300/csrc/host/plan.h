@@ -33,7 +33,9 @@ struct SnUnit {
     int64_t rows_off;       // offset of the supernode's row list in sn_rows
     int32_t contrib_begin;  // lower-sweep contributions [begin, end)
     int32_t contrib_end;
-    int32_t upper_dep;      // unit whose completion the upper sweep waits for (-1: none)
+    int32_t upper_dep;      // unit whose completion makes every row below the unit final
+    int32_t sn_w;           // width of the unit's supernode
+    int32_t parent_first_unit;  // first chunk of the parent supernode (-1: root)
     int32_t pad;
 };
 

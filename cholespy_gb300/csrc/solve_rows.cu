@@ -79,14 +79,31 @@ __global__ void __launch_bounds__(256) sweep_nnz_kernel(RowSweepArgs a) {
         T acc[R];
 #pragma unroll
         for (int j = 0; j < R; ++j) acc[j] = T(0);
-        for (int k = lo + lane; k < hi; k += 32) {
-            const int col = a.cols[k];
-            const T v = vals[k];
-            if (!dev::wait_geq(a.flags + col, a.epoch, a.status)) continue;
-            const T* xc = tmp + (size_t)col * nrhs;
+        for (int base = lo; base < hi; base += 64) {
+            // two entries per lane: flags checked together, then one fence
+            int c[2];
+            T v[2];
 #pragma unroll
-            for (int j = 0; j < R; ++j)
-                if (j < nrhs) acc[j] = fma(v, __ldcg(xc + j), acc[j]);
+            for (int u = 0; u < 2; ++u) {
+                const int k = base + lane + 32 * u;
+                c[u] = k < hi ? a.cols[k] : -1;
+                v[u] = k < hi ? vals[k] : T(0);
+            }
+            int f[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) f[u] = c[u] >= 0 ? dev::ld_volatile(a.flags + c[u]) : a.epoch;
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+                if (f[u] < a.epoch) dev::wait_geq(a.flags + c[u], a.epoch, a.status);
+            dev::fence_acquire();
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (c[u] < 0) continue;
+                const T* xc = tmp + (size_t)c[u] * nrhs;
+#pragma unroll
+                for (int j = 0; j < R; ++j)
+                    if (j < nrhs) acc[j] = fma(v[u], __ldcg(xc + j), acc[j]);
+            }
         }
         T mine = T(0);
 #pragma unroll
@@ -138,11 +155,13 @@ __global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
             const T myv = k < hi ? vals[k] : T(0);
             // every lane waits for its own entry, then the warp consumes the
             // 32 entries without further waits (independent loads in flight)
-            if (k < hi) dev::wait_geq(a.flags + mycol, a.epoch, a.status);
+            if (k < hi && dev::ld_volatile(a.flags + mycol) < a.epoch)
+                dev::wait_geq(a.flags + mycol, a.epoch, a.status);
+            dev::fence_acquire();
             __syncwarp();
             const int cnt = min(32, hi - base);
             const int steps = (cnt + NG - 1) / NG;
-#pragma unroll 4
+#pragma unroll 8
             for (int st = 0; st < steps; ++st) {
                 const int eidx = st * NG + grp;
                 const bool valid = eidx < cnt;

@@ -3,20 +3,30 @@
 // The reference solves every row in its own block and waits on one flag per
 // nonzero (kernels/kernels.cu:64-202), so a dense supernode of width w costs
 // w global round trips in sequence. Here the top region's columns live in
-// dense column-major panels and are cut into units of <= 32 columns. One CTA
-// handles one (unit, 32-RHS slice) item:
-//   lower sweep: t = (b - leaf terms, prepared by the row kernel); for every
-//     dense block L[unit rows, source chunk] (in source order): wait for the
-//     source unit's flag, stage the block and x_source in shared memory,
-//     t[rows] -= L_block x_source; then solve the 32x32 diagonal block with
-//     warp shuffles (one lane per row) and publish the unit's flag.
-//   upper sweep: wait for the single unit that completes every row below the
-//     unit; t = y - L[below, unit]^T x_below in 32-row blocks; solve the
-//     transposed diagonal block; write x (and x through perm).
+// dense column-major panels cut into units of <= 32 columns, and one CTA
+// handles one (unit, RHS slice) item. The unit's 32 rows map to the 32 lanes.
+//
+// Lower sweep (L y = b): every dense block L[unit rows, source chunk] that
+//   hits the unit (listed in source order) is taken by one of the 8 warps
+//   (block b -> warp b % 8). The warp waits for the source unit's flag,
+//   stages x_source (<= 32 x 32) in its own shared-memory slice, and each
+//   lane accumulates its row of L_block x_source in registers. The rows of a
+//   block are a sorted subset of the unit's rows, so lane p reads block row
+//   inv[p] directly (no scatter). The warps' partial sums are reduced in a
+//   fixed order, subtracted from t (b minus leaf terms), and the 32x32
+//   diagonal block is solved with warp shuffles (one lane per row).
+// Upper sweep (L^T x = y): the rows below the unit's diagonal block are cut
+//   into 32-row blocks: the supernode's off-diagonal rows first (ready once
+//   the parent supernode's first chunk is done; one wait), then the later
+//   chunks of the same supernode from the last one down (one wait each), so
+//   only the newest 32-row block sits on the dependency chain. Lane j holds
+//   column j of the unit and accumulates L[block, j]^T x_block; then the same
+//   fixed-order reduction and a transposed shuffle solve.
 // Items are assigned round-robin in topological order on a cooperatively
-// launched persistent grid, so all CTAs are resident and the smallest
-// unfinished item can always run: no deadlock, no ticket atomic. Waits are
-// bounded (device.cuh). Work per item is deterministic (fixed block order).
+// launched persistent grid: every CTA is resident, so the smallest unfinished
+// item can always run (no deadlock, no ticket atomic). Waits are bounded
+// (device.cuh). Results are deterministic: fixed block-to-warp assignment and
+// fixed reduction order.
 #include <cuda_runtime.h>
 
 #include "device.cuh"
@@ -28,8 +38,9 @@ namespace gbchol {
 
 namespace {
 
-constexpr int kT = 256;  // threads per CTA
-constexpr int kW = kChunk;
+constexpr int kT = 256;    // threads per CTA
+constexpr int kWarps = kT / 32;
+constexpr int kW = kChunk; // 32 rows / columns per unit
 
 template <typename T, typename TOut, bool ACCUM>
 struct SnIO {
@@ -38,153 +49,146 @@ struct SnIO {
     static constexpr bool accum = ACCUM;
 };
 
-template <typename T>
+template <typename T, int KW>
 struct SnSmem {
-    T t[kW][kW + 1];   // accumulator: rows x RHS
-    T L[kW][kW + 1];   // staged block of L
-    T x[kW][kW + 1];   // staged x rows x RHS
-    int rp[kW];        // destination positions of the block's rows
+    T xs[kWarps][kW][KW + 1];  // per-warp staging of x blocks; reused for the reduction
+    T t[kW][KW + 1];           // reduced right-hand side of the unit
+    T d[kW][kW + 1];           // diagonal block
+    int inv[kWarps][kW];       // unit row -> block row (lower sweep)
 };
 
-// Waits (thread 0) for a unit flag, then makes the whole CTA proceed.
-__device__ __forceinline__ void cta_wait(const int* flag, int epoch, int* status) {
-    if (threadIdx.x == 0) dev::wait_geq(flag, epoch, status);
-    __syncthreads();
+// Lane 0 waits for a flag; the warp proceeds together. Loads of data
+// published under the flag use ld.cg (L2), which holds the producer's
+// writes once the flag is observed.
+__device__ __forceinline__ void warp_wait(const int* flag, int epoch, int* status, int lane) {
+    if (lane == 0) dev::wait_geq(flag, epoch, status);
+    __syncwarp();
 }
 
-template <class io, bool LOWER, bool RED>
+template <class io, bool LOWER, int KW>
 __global__ void __launch_bounds__(kT) sn_sweep_kernel(SnSweepArgs a) {
     using T = typename io::t;
-    __shared__ SnSmem<T> sm;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SnSmem<T, KW>& sm = *reinterpret_cast<SnSmem<T, KW>*>(smem_raw);
     if (a.skip && dev::ld_volatile(a.skip)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const T* __restrict__ panels = static_cast<const T*>(a.panels);
     T* tmp = static_cast<T*>(a.tmp);
     const int nrhs = a.nrhs;
     const int nitems = a.n_units * a.nslices;
+    T (*xs)[KW + 1] = sm.xs[warp];
+    if (LOWER) sm.inv[warp][lane] = -1;
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         const int uidx = LOWER ? item / a.nslices : a.n_units - 1 - item / a.nslices;
         const int slice = item % a.nslices;
-        const int k0 = slice * kW;
-        const int kw = min(kW, nrhs - k0);
+        const int k0 = slice * KW;
+        const int kw = min(KW, nrhs - k0);
         const SnUnit U = a.units[uidx];
         const int w = U.w;
-
-        if (!LOWER && U.upper_dep >= 0)
-            cta_wait(a.uflags + (size_t)U.upper_dep * a.nslices + slice, a.epoch, a.status);
-
-        // t <- current values of the unit's rows (lower: b minus leaf terms; upper: y)
-        for (int idx = tid; idx < kW * kW; idx += kT) {
-            const int i = idx >> 5, k = idx & 31;
-            sm.t[i][k] = (i < w && k < kw) ? tmp[(size_t)(U.c0 + i) * nrhs + k0 + k] : T(0);
-        }
+        T acc[KW];
+#pragma unroll
+        for (int k = 0; k < KW; ++k) acc[k] = T(0);
 
         if (LOWER) {
-            int waited = -1;
-            for (int e = U.contrib_begin; e < U.contrib_end; ++e) {
-                const SnContrib C = a.contribs[e];
-                if (C.src_unit != waited) {
-                    cta_wait(a.uflags + (size_t)C.src_unit * a.nslices + slice, a.epoch, a.status);
-                    waited = C.src_unit;
+            const int nb = U.contrib_end - U.contrib_begin;
+            for (int b = warp; b < nb; b += kWarps) {
+                const SnContrib C = a.contribs[U.contrib_begin + b];
+                if (lane < C.nr) sm.inv[warp][a.sn_rows[C.rows_off + lane] - U.c0] = lane;
+                warp_wait(a.uflags + (size_t)C.src_unit * a.nslices + slice, a.epoch, a.status, lane);
+                for (int idx = lane; idx < C.w * KW; idx += 32) {
+                    const int j = idx / KW, k = idx % KW;
+                    xs[j][k] = k < kw ? __ldcg(tmp + (size_t)(C.xcol + j) * nrhs + k0 + k) : T(0);
                 }
-                for (int idx = tid; idx < kW * kW; idx += kT) {
-                    const int i = idx & 31, j = idx >> 5;  // column-major: coalesced over rows
-                    if (i < C.nr && j < C.w) sm.L[i][j] = panels[C.panel_off + i + (size_t)j * C.ld];
-                    const int jj = idx >> 5, k = idx & 31;  // x rows: coalesced over RHS
-                    if (jj < C.w && k < kw)
-                        sm.x[jj][k] = __ldcg(tmp + (size_t)(C.xcol + jj) * nrhs + k0 + k);
-                }
-                if (tid < C.nr) sm.rp[tid] = a.sn_rows[C.rows_off + tid] - U.c0;
-                __syncthreads();
-                if (RED) {
-                    // 8 threads per row split the reduction over the block's columns
-                    const int i = tid >> 3, sub = tid & 7;
-                    for (int k = 0; k < kw; ++k) {
-                        T acc = T(0);
-                        if (i < C.nr)
-                            for (int j = sub; j < C.w; j += 8) acc = fma(sm.L[i][j], sm.x[j][k], acc);
-                        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-                        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-                        acc += __shfl_xor_sync(0xffffffffu, acc, 4);
-                        if (sub == 0 && i < C.nr) sm.t[sm.rp[i]][k] -= acc;
-                    }
-                } else {
+                __syncwarp();
+                const int src = sm.inv[warp][lane];
+                if (src >= 0) {
+                    const T* Lp = panels + C.panel_off + src;
+#pragma unroll 4
+                    for (int j = 0; j < C.w; ++j) {
+                        const T lv = __ldg(Lp + (size_t)j * C.ld);
 #pragma unroll
-                    for (int rr = 0; rr < 4; ++rr) {
-                        const int i = warp + 8 * rr;
-                        if (i < C.nr && lane < kw) {
-                            T acc = T(0);
-                            for (int j = 0; j < C.w; ++j) acc = fma(sm.L[i][j], sm.x[j][lane], acc);
-                            sm.t[sm.rp[i]][lane] -= acc;
-                        }
+                        for (int k = 0; k < KW; ++k) acc[k] = fma(lv, xs[j][k], acc[k]);
                     }
                 }
-                __syncthreads();
+                sm.inv[warp][lane] = -1;
+                __syncwarp();
             }
         } else {
-            const int pbeg = U.pos0 + w;
-            for (int p = pbeg; p < U.ld; p += kW) {
-                const int nr = min(kW, U.ld - p);
-                for (int idx = tid; idx < kW * kW; idx += kT) {
-                    const int i = idx & 31, j = idx >> 5;
-                    if (i < nr && j < w) sm.L[i][j] = panels[U.panel_col_off + p + i + (size_t)j * U.ld];
-                    const int ii = idx >> 5, k = idx & 31;
-                    if (ii < nr && k < kw) {
-                        const int row = a.sn_rows[U.rows_off + p + ii];
-                        sm.x[ii][k] = __ldcg(tmp + (size_t)row * nrhs + k0 + k);
-                    }
-                }
-                __syncthreads();
-                if (RED) {
-                    const int j = tid >> 3, sub = tid & 7;
-                    for (int k = 0; k < kw; ++k) {
-                        T acc = T(0);
-                        if (j < w)
-                            for (int i = sub; i < nr; i += 8) acc = fma(sm.L[i][j], sm.x[i][k], acc);
-                        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-                        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-                        acc += __shfl_xor_sync(0xffffffffu, acc, 4);
-                        if (sub == 0 && j < w) sm.t[j][k] -= acc;
-                    }
+            // block list: off-diagonal rows of the supernode (32-row blocks),
+            // then the later chunks of the supernode, last chunk first
+            const int wj = U.pos0 + w;                      // end of this unit's columns
+            const int sn_w = U.sn_w;                        // supernode width
+            const int nrb = (U.ld - sn_w + kW - 1) / kW;    // off-diagonal row blocks
+            const int nlater = (sn_w - wj + kW - 1) / kW;   // later chunks
+            bool parent_ready = false;
+            for (int b = warp; b < nrb + nlater; b += kWarps) {
+                int p0, nr, dep;
+                if (b < nrb) {
+                    p0 = sn_w + b * kW;
+                    nr = min(kW, U.ld - p0);
+                    dep = U.parent_first_unit;
+                    if (parent_ready) dep = -1;
+                    parent_ready = true;
                 } else {
+                    const int c = nlater - 1 - (b - nrb);  // later chunk index, last first
+                    p0 = wj + c * kW;
+                    nr = min(kW, sn_w - p0);
+                    dep = uidx + 1 + c;
+                }
+                if (dep >= 0) warp_wait(a.uflags + (size_t)dep * a.nslices + slice, a.epoch, a.status, lane);
+                for (int idx = lane; idx < nr * KW; idx += 32) {
+                    const int i = idx / KW, k = idx % KW;
+                    const int row = a.sn_rows[U.rows_off + p0 + i];
+                    xs[i][k] = k < kw ? __ldcg(tmp + (size_t)row * nrhs + k0 + k) : T(0);
+                }
+                __syncwarp();
+                if (lane < w) {
+                    const T* Lp = panels + U.panel_col_off + p0 + (size_t)lane * U.ld;
+#pragma unroll 4
+                    for (int i = 0; i < nr; ++i) {
+                        const T lv = __ldg(Lp + i);
 #pragma unroll
-                    for (int rr = 0; rr < 4; ++rr) {
-                        const int j = warp + 8 * rr;
-                        if (j < w && lane < kw) {
-                            T acc = T(0);
-                            for (int i = 0; i < nr; ++i) acc = fma(sm.L[i][j], sm.x[i][lane], acc);
-                            sm.t[j][lane] -= acc;
-                        }
+                        for (int k = 0; k < KW; ++k) acc[k] = fma(lv, xs[i][k], acc[k]);
                     }
                 }
-                __syncthreads();
+                __syncwarp();
             }
         }
 
-        // diagonal block
+        // fixed-order reduction of the warps' partial sums
+#pragma unroll
+        for (int k = 0; k < KW; ++k) xs[lane][k] = acc[k];
         for (int idx = tid; idx < kW * kW; idx += kT) {
             const int i = idx & 31, j = idx >> 5;
-            if (i < w && j < w) sm.L[i][j] = panels[U.panel_col_off + U.pos0 + i + (size_t)j * U.ld];
+            if (i < w && j < w) sm.d[i][j] = panels[U.panel_col_off + U.pos0 + i + (size_t)j * U.ld];
         }
         __syncthreads();
-        for (int k = warp; k < kw; k += 8) {
+        for (int idx = tid; idx < kW * KW; idx += kT) {
+            const int i = idx / KW, k = idx % KW;
+            T s = T(0);
+#pragma unroll
+            for (int ww = 0; ww < kWarps; ++ww) s += sm.xs[ww][i][k];
+            sm.t[i][k] = (i < w && k < kw) ? tmp[(size_t)(U.c0 + i) * nrhs + k0 + k] - s : T(0);
+        }
+        __syncthreads();
+        // diagonal block: warp per RHS column, lane per row
+        for (int k = warp; k < kw; k += kWarps) {
             T v = sm.t[lane][k];
             if (LOWER) {
                 for (int j = 0; j < w; ++j) {
-                    const T xj = __shfl_sync(0xffffffffu, v, j) / sm.L[j][j];
+                    const T xj = __shfl_sync(0xffffffffu, v, j) / sm.d[j][j];
                     if (lane == j) v = xj;
-                    else if (lane > j) v = fma(-sm.L[lane][j], xj, v);
+                    else if (lane > j && lane < w) v = fma(-sm.d[lane][j], xj, v);
                 }
             } else {
                 for (int j = w - 1; j >= 0; --j) {
-                    const T xj = __shfl_sync(0xffffffffu, v, j) / sm.L[j][j];
+                    const T xj = __shfl_sync(0xffffffffu, v, j) / sm.d[j][j];
                     if (lane == j) v = xj;
-                    else if (lane < j) v = fma(-sm.L[j][lane], xj, v);
+                    else if (lane < j) v = fma(-sm.d[j][lane], xj, v);
                 }
             }
             if (lane < w) {
-                const size_t o = (size_t)(U.c0 + lane) * nrhs + k0 + k;
-                tmp[o] = v;
+                tmp[(size_t)(U.c0 + lane) * nrhs + k0 + k] = v;
                 if (!LOWER) {
                     using TO = typename io::tout;
                     TO* out = static_cast<TO*>(a.out);
@@ -200,19 +204,28 @@ __global__ void __launch_bounds__(kT) sn_sweep_kernel(SnSweepArgs a) {
     }
 }
 
-template <class io, bool LOWER>
-cudaError_t launch_sn_io(const SnSweepArgs& a, cudaStream_t stream) {
-    const bool red = a.nrhs <= 8;
-    const void* fn = red ? (const void*)sn_sweep_kernel<io, LOWER, true>
-                         : (const void*)sn_sweep_kernel<io, LOWER, false>;
+template <class io, bool LOWER, int KW>
+cudaError_t launch_sn_kw(const SnSweepArgs& a, cudaStream_t stream) {
+    using T = typename io::t;
+    const void* fn = (const void*)sn_sweep_kernel<io, LOWER, KW>;
+    const size_t smem = sizeof(SnSmem<T, KW>);
+    // the attribute belongs to the current device's context: set it per launch
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
     int grid = 0;
-    cudaError_t e = coop_grid(fn, kT, 0, &grid);
+    e = coop_grid(fn, kT, smem, &grid);
     if (e != cudaSuccess) return e;
     const int items = a.n_units * a.nslices;
     if (grid > items) grid = items;
     SnSweepArgs copy = a;
     void* args[] = {&copy};
-    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kT), args, 0, stream);
+    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kT), args, smem, stream);
+}
+
+template <class io, bool LOWER>
+cudaError_t launch_sn_io(const SnSweepArgs& a, cudaStream_t stream) {
+    if (a.nrhs <= 8) return launch_sn_kw<io, LOWER, 8>(a, stream);
+    return launch_sn_kw<io, LOWER, 32>(a, stream);
 }
 
 }  // namespace
