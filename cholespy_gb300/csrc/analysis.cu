@@ -7,7 +7,17 @@
 // (kernels/kernels.cu:8-60); the values are fully determined by L, so the
 // result is bit-identical to the reference's on the same factor.
 //
-// GB300 design: the reference runs n blocks of ONE thread each, handing rows
+// Fast path: for a factor whose pattern is closed under fill (every factor
+// produced by a symbolic Cholesky factorisation, CHOLMOD's included), the
+// level of row i of L is the height of i in the elimination tree and the
+// level of row i of L^T its depth: the dependencies of a row form a subtree
+// (L) or an ancestor path (L^T) of the etree along which levels strictly
+// increase. The host derives these candidates in O(n) from parent(j) = first
+// off-diagonal row of column j, and level_verify_kernel checks every row
+// against all of its dependencies in one parallel pass. Only a pattern that
+// fails the check runs the general sync-free kernel below.
+//
+// GB300 design of the general kernel: the reference runs n blocks of ONE thread each, handing rows
 // out through a global atomic ticket and spinning without bound. Here one
 // warp handles a row: its 32 lanes read the row's column indices coalesced,
 // each lane waits (bounded) on its dependency's flag, and a warp max-reduce
@@ -69,7 +79,43 @@ __global__ void __launch_bounds__(256) level_kernel(int n, const int* __restrict
     if (lane == 0 && local_max > 0) atomicMax(max_lvl, local_max);
 }
 
+// Checks a candidate level assignment against every row's dependencies in
+// one fully parallel pass (warp per row, no waits): a labeling that satisfies
+// level[i] == (deps ? 1 + max level[dep] : 0) at every row is the unique
+// longest-path labeling, i.e. exactly what the sequential definition gives.
+template <bool LOWER>
+__global__ void __launch_bounds__(256) level_verify_kernel(int n, const int* __restrict__ rowptr,
+                                                           const int* __restrict__ cols,
+                                                           const int* __restrict__ cand,
+                                                           int* mismatch) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int row = warp; row < n; row += nwarps) {
+        const int s = rowptr[row], e = rowptr[row + 1];
+        const int lo = LOWER ? s : s + 1;
+        const int hi = LOWER ? e - 1 : e;
+        int lvl = 0;
+        for (int k = lo + lane; k < hi; k += 32) lvl = max(lvl, cand[cols[k]] + 1);
+        lvl = dev::warp_max(lvl);
+        if (lane == 0 && lvl != cand[row]) atomicOr(mismatch, 1);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_level_verify(bool lower, int n, const int* rowptr, const int* cols,
+                                const int* cand, int* mismatch, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int grid = (n + 7) / 8;
+    if (grid > sms * 16) grid = sms * 16;
+    if (lower) level_verify_kernel<true><<<grid, 256, 0, stream>>>(n, rowptr, cols, cand, mismatch);
+    else level_verify_kernel<false><<<grid, 256, 0, stream>>>(n, rowptr, cols, cand, mismatch);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_level_analysis(bool lower, int n, const int* rowptr, const int* cols,
                                   int* levels, int* flags, int epoch, int* max_lvl, int* status,

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <chrono>
 #include <climits>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -91,6 +92,7 @@ struct Triangle {
     DevBuf<double> v64;
     std::vector<int32_t> row_levels, order_h;
     int32_t max_lvl = 0;
+    bool general_kernel = false;  // analysis needed the sync-free kernel
 };
 
 }  // namespace
@@ -200,25 +202,62 @@ void sort_by_level(const std::vector<int32_t>& lev, int32_t max_lvl, std::vector
     for (int32_t i = 0; i < n; ++i) order[ptr[lev[i]]++] = i;
 }
 
+// Elimination-tree level candidates: height (L) or depth (L^T) of every
+// node, with parent(j) = first off-diagonal row of column j of L.
+void tree_levels(const Factor& F, bool lower, std::vector<int32_t>& lev) {
+    const int32_t n = F.n;
+    std::vector<int32_t> parent((size_t)n, -1);
+    for (int32_t j = 0; j < n; ++j)
+        if (F.colptr[j + 1] - F.colptr[j] > 1) parent[j] = F.rowidx[F.colptr[j] + 1];
+    lev.assign((size_t)n, 0);
+    if (lower) {
+        for (int32_t j = 0; j < n; ++j)
+            if (parent[j] >= 0) lev[parent[j]] = std::max(lev[parent[j]], lev[j] + 1);
+    } else {
+        for (int32_t j = n - 1; j >= 0; --j)
+            if (parent[j] >= 0) lev[j] = lev[parent[j]] + 1;
+    }
+}
+
 int analyze_triangle(gbchol_solver* h, Triangle& t, bool lower) {
     const int32_t n = h->n;
     DevBuf<int32_t> lev;
     CUDA_TRY(lev.alloc((size_t)n));
-    CUDA_TRY(cudaMemset(h->max_lvl.p, 0, sizeof(int32_t)));
-    int ep = h->next_epoch(nullptr);
-    CUDA_TRY(launch_level_analysis(lower, n, t.rowptr.p, t.cols.p, lev.p, h->flags.p, ep,
-                                   h->max_lvl.p, h->status.p, nullptr));
-    CUDA_TRY(cudaDeviceSynchronize());
-    int32_t st = 0;
-    CUDA_TRY(cudaMemcpy(&st, h->status.p, sizeof(int32_t), cudaMemcpyDeviceToHost));
-    if (st != 0) {
-        cudaMemset(h->status.p, 0, sizeof(int32_t));
-        return fail(GBCHOL_ETIMEOUT, "Level analysis: a device-side wait expired (malformed factor?).");
+    // fast path: etree candidates verified on the GPU against every nonzero
+    const char* force = std::getenv("GBCHOL_SYNCFREE_ANALYSIS");
+    bool verified = false;
+    if (!(force && force[0] == '1')) {
+        tree_levels(h->F, lower, t.row_levels);
+        CUDA_TRY(cudaMemcpy(lev.p, t.row_levels.data(), sizeof(int32_t) * (size_t)n,
+                            cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemset(h->max_lvl.p, 0, sizeof(int32_t)));
+        CUDA_TRY(launch_level_verify(lower, n, t.rowptr.p, t.cols.p, lev.p, h->max_lvl.p, nullptr));
+        int32_t mism = 1;
+        CUDA_TRY(cudaMemcpy(&mism, h->max_lvl.p, sizeof(int32_t), cudaMemcpyDeviceToHost));
+        verified = mism == 0;
+        if (verified) {
+            t.max_lvl = 0;
+            for (int32_t v : t.row_levels) t.max_lvl = std::max(t.max_lvl, v);
+        }
     }
-    t.row_levels.resize((size_t)n);
-    CUDA_TRY(cudaMemcpy(t.row_levels.data(), lev.p, sizeof(int32_t) * (size_t)n,
-                        cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(&t.max_lvl, h->max_lvl.p, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    t.general_kernel = !verified;
+    if (!verified) {
+        CUDA_TRY(cudaMemset(h->max_lvl.p, 0, sizeof(int32_t)));
+        int ep = h->next_epoch(nullptr);
+        CUDA_TRY(launch_level_analysis(lower, n, t.rowptr.p, t.cols.p, lev.p, h->flags.p, ep,
+                                       h->max_lvl.p, h->status.p, nullptr));
+        CUDA_TRY(cudaDeviceSynchronize());
+        int32_t st = 0;
+        CUDA_TRY(cudaMemcpy(&st, h->status.p, sizeof(int32_t), cudaMemcpyDeviceToHost));
+        if (st != 0) {
+            cudaMemset(h->status.p, 0, sizeof(int32_t));
+            return fail(GBCHOL_ETIMEOUT, "Level analysis: a device-side wait expired (malformed factor?).");
+        }
+        t.row_levels.resize((size_t)n);
+        CUDA_TRY(cudaMemcpy(t.row_levels.data(), lev.p, sizeof(int32_t) * (size_t)n,
+                            cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(&t.max_lvl, h->max_lvl.p, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    }
     sort_by_level(t.row_levels, t.max_lvl, t.order_h);
     CUDA_TRY(t.order.upload(t.order_h.data(), (size_t)n));
     return GBCHOL_OK;
@@ -275,7 +314,7 @@ int setup_plan(gbchol_solver* h, const std::vector<int32_t>& rp, const std::vect
     if (f64) CUDA_TRY(h->pan64.upload(P.panels.data(), P.panels.size()));
     CUDA_TRY(h->units.upload(P.units.data(), P.units.size()));
     CUDA_TRY(h->contribs.upload(P.contribs.data(), P.contribs.size()));
-    CUDA_TRY(h->uflags.alloc(std::max<size_t>(1, P.units.size() * 4)));
+    CUDA_TRY(h->uflags.alloc(std::max<size_t>(1, P.units.size() * 8)));  // <= 8 RHS slices
     CUDA_TRY(cudaMemset(h->uflags.p, 0, sizeof(int32_t) * h->uflags.count));
     // row flags: top rows are always "ready" for the row kernels (they are
     // solved by the supernodal kernel in an earlier launch)
@@ -372,7 +411,7 @@ int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in,
     CUDA_TRY(launch_row_sweep(lo, true, io, s));
     SnSweepArgs sn;
     sn.n_units = (int)P.units.size();
-    sn.nslices = sn_slices(nrhs);
+    sn.nslices = sn_slices(nrhs, !f32);
     sn.nrhs = nrhs;
     sn.units = h->units.p;
     sn.contribs = h->contribs.p;

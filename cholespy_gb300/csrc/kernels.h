@@ -15,6 +15,11 @@ cudaError_t launch_level_analysis(bool lower, int n, const int* rowptr, const in
                                   int* levels, int* flags, int epoch, int* max_lvl, int* status,
                                   cudaStream_t stream);
 
+// Parallel check of candidate levels against every row's dependencies;
+// sets *mismatch to 1 if any row disagrees.
+cudaError_t launch_level_verify(bool lower, int n, const int* rowptr, const int* cols,
+                                const int* cand, int* mismatch, cudaStream_t stream);
+
 // ---- row-wise sync-free sweeps (solve_rows.cu) ----------------------------
 // Lower sweep (L y = b[perm]):    out_tmp[row] = (in[perm[row]] - sum L[row,c] tmp[c]) / L[row,row]
 // Upper sweep (L^T x = y):        tmp[row] = (tmp[row] - sum U[row,c] tmp[c]) / U[row,row]

@@ -66,7 +66,7 @@ __device__ __forceinline__ void warp_wait(const int* flag, int epoch, int* statu
 }
 
 template <class io, bool LOWER, int KW>
-__global__ void __launch_bounds__(kT) sn_sweep_kernel(SnSweepArgs a) {
+__global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
     using T = typename io::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SnSmem<T, KW>& sm = *reinterpret_cast<SnSmem<T, KW>*>(smem_raw);
@@ -94,23 +94,32 @@ __global__ void __launch_bounds__(kT) sn_sweep_kernel(SnSweepArgs a) {
             for (int b = warp; b < nb; b += kWarps) {
                 const SnContrib C = a.contribs[U.contrib_begin + b];
                 if (lane < C.nr) sm.inv[warp][a.sn_rows[C.rows_off + lane] - U.c0] = lane;
-                warp_wait(a.uflags + (size_t)C.src_unit * a.nslices + slice, a.epoch, a.status, lane);
-                for (int idx = lane; idx < C.w * KW; idx += 32) {
-                    const int j = idx / KW, k = idx % KW;
-                    xs[j][k] = k < kw ? __ldcg(tmp + (size_t)(C.xcol + j) * nrhs + k0 + k) : T(0);
-                }
                 __syncwarp();
                 const int src = sm.inv[warp][lane];
-                if (src >= 0) {
-                    const T* Lp = panels + C.panel_off + src;
-#pragma unroll 4
-                    for (int j = 0; j < C.w; ++j) {
-                        const T lv = __ldg(Lp + (size_t)j * C.ld);
-#pragma unroll
-                        for (int k = 0; k < KW; ++k) acc[k] = fma(lv, xs[j][k], acc[k]);
-                    }
-                }
                 sm.inv[warp][lane] = -1;
+                // L is constant: its loads go out before the flag wait
+                T lv[kW];
+                const T* Lp = panels + C.panel_off + src;
+#pragma unroll
+                for (int j = 0; j < kW; ++j)
+                    lv[j] = (src >= 0 && j < C.w) ? __ldg(Lp + (size_t)j * C.ld) : T(0);
+                warp_wait(a.uflags + (size_t)C.src_unit * a.nslices + slice, a.epoch, a.status, lane);
+                T xv[KW];
+#pragma unroll
+                for (int u = 0; u < KW; ++u) {
+                    const int idx = lane + 32 * u, j = idx / KW, k = idx % KW;
+                    xv[u] = (j < C.w && k < kw) ? __ldcg(tmp + (size_t)(C.xcol + j) * nrhs + k0 + k) : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < KW; ++u) {
+                    const int idx = lane + 32 * u;
+                    xs[idx / KW][idx % KW] = xv[u];
+                }
+                __syncwarp();
+#pragma unroll
+                for (int j = 0; j < kW; ++j)
+#pragma unroll
+                    for (int k = 0; k < KW; ++k) acc[k] = fma(lv[j], xs[j][k], acc[k]);
                 __syncwarp();
             }
         } else {
@@ -126,8 +135,7 @@ __global__ void __launch_bounds__(kT) sn_sweep_kernel(SnSweepArgs a) {
                 if (b < nrb) {
                     p0 = sn_w + b * kW;
                     nr = min(kW, U.ld - p0);
-                    dep = U.parent_first_unit;
-                    if (parent_ready) dep = -1;
+                    dep = parent_ready ? -1 : U.parent_first_unit;
                     parent_ready = true;
                 } else {
                     const int c = nlater - 1 - (b - nrb);  // later chunk index, last first
@@ -135,22 +143,29 @@ __global__ void __launch_bounds__(kT) sn_sweep_kernel(SnSweepArgs a) {
                     nr = min(kW, sn_w - p0);
                     dep = uidx + 1 + c;
                 }
+                T lv[kW];
+                const T* Lp = panels + U.panel_col_off + p0 + (size_t)lane * U.ld;
+#pragma unroll
+                for (int i = 0; i < kW; ++i) lv[i] = (lane < w && i < nr) ? __ldg(Lp + i) : T(0);
+                const int myrow = lane < nr ? a.sn_rows[U.rows_off + p0 + lane] : 0;
                 if (dep >= 0) warp_wait(a.uflags + (size_t)dep * a.nslices + slice, a.epoch, a.status, lane);
-                for (int idx = lane; idx < nr * KW; idx += 32) {
-                    const int i = idx / KW, k = idx % KW;
-                    const int row = a.sn_rows[U.rows_off + p0 + i];
-                    xs[i][k] = k < kw ? __ldcg(tmp + (size_t)row * nrhs + k0 + k) : T(0);
+                T xv[KW];
+#pragma unroll
+                for (int u = 0; u < KW; ++u) {
+                    const int idx = lane + 32 * u, i = idx / KW, k = idx % KW;
+                    const int row = __shfl_sync(0xffffffffu, myrow, i);
+                    xv[u] = (i < nr && k < kw) ? __ldcg(tmp + (size_t)row * nrhs + k0 + k) : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < KW; ++u) {
+                    const int idx = lane + 32 * u;
+                    xs[idx / KW][idx % KW] = xv[u];
                 }
                 __syncwarp();
-                if (lane < w) {
-                    const T* Lp = panels + U.panel_col_off + p0 + (size_t)lane * U.ld;
-#pragma unroll 4
-                    for (int i = 0; i < nr; ++i) {
-                        const T lv = __ldg(Lp + i);
 #pragma unroll
-                        for (int k = 0; k < KW; ++k) acc[k] = fma(lv, xs[i][k], acc[k]);
-                    }
-                }
+                for (int i = 0; i < kW; ++i)
+#pragma unroll
+                    for (int k = 0; k < KW; ++k) acc[k] = fma(lv[i], xs[i][k], acc[k]);
                 __syncwarp();
             }
         }
@@ -224,13 +239,17 @@ cudaError_t launch_sn_kw(const SnSweepArgs& a, cudaStream_t stream) {
 
 template <class io, bool LOWER>
 cudaError_t launch_sn_io(const SnSweepArgs& a, cudaStream_t stream) {
+    constexpr int wide = sizeof(typename io::t) == 8 ? 16 : 32;
     if (a.nrhs <= 8) return launch_sn_kw<io, LOWER, 8>(a, stream);
-    return launch_sn_kw<io, LOWER, 32>(a, stream);
+    return launch_sn_kw<io, LOWER, wide>(a, stream);
 }
 
 }  // namespace
 
-int sn_slices(int nrhs) { return nrhs <= 8 ? 1 : (nrhs + kW - 1) / kW; }
+int sn_slices(int nrhs, bool f64) {
+    const int wide = f64 ? 16 : 32;
+    return nrhs <= 8 ? 1 : (nrhs + wide - 1) / wide;
+}
 
 cudaError_t launch_sn_sweep(const SnSweepArgs& a, bool lower, SweepIO io, cudaStream_t stream) {
     if (a.n_units == 0) return cudaSuccess;

@@ -9,7 +9,7 @@ namespace gbchol {
 
 struct SnSweepArgs {
     int n_units = 0;
-    int nslices = 1;          // RHS slices of 32 (1 when nrhs <= 8)
+    int nslices = 1;          // RHS slices (see sn_slices)
     int nrhs = 0;
     const SnUnit* units = nullptr;
     const SnContrib* contribs = nullptr;
@@ -24,7 +24,8 @@ struct SnSweepArgs {
     const int* skip = nullptr;
 };
 
-int sn_slices(int nrhs);
+// RHS slices of one sweep: 1 for <= 8 RHS, else 32-wide (FP32) or 16-wide (FP64).
+int sn_slices(int nrhs, bool f64);
 cudaError_t launch_sn_sweep(const SnSweepArgs& a, bool lower, SweepIO io, cudaStream_t stream);
 
 }  // namespace gbchol

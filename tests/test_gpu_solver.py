@@ -230,3 +230,88 @@ def test_side_stream(cuda):
     torch.cuda.current_stream().wait_stream(st)
     torch.cuda.synchronize()
     assert torch.equal(x, ref)
+
+
+def _from_factor(perm, colptr, rowidx, vals, store):
+    import ctypes as C
+    from cholespy_gb300 import _ffi
+    h = C.c_void_p()
+    a = [np.ascontiguousarray(v, dt) for v, dt in ((perm, np.int32), (colptr, np.int32),
+                                                  (rowidx, np.int32), (vals, np.float64))]
+    _ffi.check(_ffi.lib().gbchol_create_from_factor(len(perm), *[x.ctypes.data for x in a], store,
+                                                    C.byref(h)))
+    return h, a
+
+
+def _levels_of(h, n, lower):
+    import ctypes as C
+    from cholespy_gb300 import _ffi
+    lev = np.zeros(n, np.int32)
+    order = np.zeros(n, np.int32)
+    mx = C.c_int32()
+    _ffi.check(_ffi.lib().gbchol_get_levels(h, 1 if lower else 0, lev.ctypes.data, order.ctypes.data,
+                                            C.byref(mx)))
+    return lev, order, mx.value
+
+
+def test_levels_general_kernel(cuda, monkeypatch):
+    """The sync-free level kernel (used when the etree candidates fail the
+    check) also matches the oracle bit for bit."""
+    from cholespy_gb300 import CholeskySolverF
+    monkeypatch.setenv("GBCHOL_SYNCFREE_ANALYSIS", "1")
+    n, vals, idx = PROBLEMS["grid3d_16"]()
+    s = _make(cuda, n, vals, idx, CholeskySolverF)
+    perm, colptr, rowidx, lv = s.factor()
+    lrp, lci, _ = oracle.csr_of_lower(colptr, rowidx, lv)
+    for lower, (rp, ci) in ((True, (lrp, lci)), (False, (colptr, rowidx))):
+        lev_o, ord_o, mx_o = oracle.levels(rp, ci, lower)
+        lev_g, ord_g, mx_g = s.levels(lower)
+        np.testing.assert_array_equal(lev_g, lev_o)
+        np.testing.assert_array_equal(ord_g, ord_o)
+
+
+def test_levels_pattern_not_fill_closed(cuda):
+    """A triangular matrix whose pattern is not closed under fill (entries of
+    a true factor dropped): the etree candidates fail the GPU check and the
+    general kernel produces the reference's levels; the solve still matches
+    the oracle's sweeps on that matrix."""
+    from cholespy_gb300 import _ffi
+    torch = cuda
+    n, vals, idx = PROBLEMS["ico4"]()
+    import scipy.sparse as sp
+    A = sp.csc_matrix((vals, (idx[0], idx[1])), shape=(n, n))
+    A.sum_duplicates()
+    perm = np.arange(n, dtype=np.int32)
+    Lp, Li, Lx = oracle.cholesky(n, A.indptr, A.indices, A.data, perm)
+    # drop every third off-diagonal entry that is not the column's first one
+    keep = np.ones(len(Li), bool)
+    for j in range(n):
+        s, e = Lp[j], Lp[j + 1]
+        for k in range(s + 2, e):
+            if (k % 3) == 0:
+                keep[k] = False
+    cnt = np.array([keep[Lp[j]:Lp[j + 1]].sum() for j in range(n)])
+    Lp2 = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int32)
+    Li2, Lx2 = Li[keep], Lx[keep]
+    h, _keep = _from_factor(perm, Lp2, Li2, Lx2, _ffi.STORE_F64)
+    try:
+        lrp, lci, _ = oracle.csr_of_lower(Lp2, Li2, Lx2)
+        for lower, (rp, ci) in ((True, (lrp, lci)), (False, (Lp2, Li2))):
+            lev_o, ord_o, mx_o = oracle.levels(rp, ci, lower)
+            lev_g, ord_g, mx_g = _levels_of(h, n, lower)
+            np.testing.assert_array_equal(lev_g, lev_o)
+            np.testing.assert_array_equal(ord_g, ord_o)
+            assert mx_g == mx_o
+        b = np.random.default_rng(5).standard_normal((n, 4))
+        xo = oracle.reference_solve(perm, Lp2, Li2, Lx2, b, np.float64)
+        bt = torch.tensor(b, device="cuda")
+        xt = torch.zeros_like(bt)
+        import ctypes as C
+        st = _ffi.lib().gbchol_solve(h, 1, 4, C.c_void_p(bt.data_ptr()), C.c_void_p(xt.data_ptr()),
+                                     C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        _ffi.check(st)
+        _ffi.check(_ffi.lib().gbchol_check(h))
+        err = np.abs(xt.cpu().numpy() - xo).max() / np.abs(xo).max()
+        assert err < 1e-12, err
+    finally:
+        _ffi.lib().gbchol_destroy(h)
