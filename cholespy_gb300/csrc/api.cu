@@ -117,7 +117,11 @@ struct gbchol_solver {
     DevBuf<double> lo_v64, up_v64, pan64;
     DevBuf<SnUnit> units;
     DevBuf<SnContrib> contribs;
-    DevBuf<int32_t> uflags;   // units * 4 RHS slices
+    DevBuf<int32_t> uflags;   // units * RHS slices
+    DevBuf<int32_t> order_lo, order_up;  // units in dependency-level order
+    DevBuf<float> dinv32;
+    DevBuf<double> dinv64;    // inverse diagonal blocks of the units
+    DevBuf<int32_t> counters; // [ticket, exits] per sweep kernel (4 kernels)
     std::vector<int32_t> flags_init;  // 0 for leaf rows, INT_MAX for top rows
     DevBuf<int32_t> a_rowptr, a_cols;
     DevBuf<double> a_vals;    // symmetric A, original ordering
@@ -313,6 +317,14 @@ int setup_plan(gbchol_solver* h, const std::vector<int32_t>& rp, const std::vect
     if (f32) CUDA_TRY(upload_cast(h->pan32, P.panels));
     if (f64) CUDA_TRY(h->pan64.upload(P.panels.data(), P.panels.size()));
     CUDA_TRY(h->units.upload(P.units.data(), P.units.size()));
+    CUDA_TRY(h->order_lo.upload(P.unit_order_lo.data(), P.unit_order_lo.size()));
+    CUDA_TRY(h->order_up.upload(P.unit_order_up.data(), P.unit_order_up.size()));
+    if (f32) CUDA_TRY(upload_cast(h->dinv32, P.dinv));
+    if (f64) CUDA_TRY(h->dinv64.upload(P.dinv.data(), P.dinv.size()));
+    P.dinv.clear();
+    P.dinv.shrink_to_fit();
+    CUDA_TRY(h->counters.alloc(8));
+    CUDA_TRY(cudaMemset(h->counters.p, 0, sizeof(int32_t) * 8));
     CUDA_TRY(h->contribs.upload(P.contribs.data(), P.contribs.size()));
     CUDA_TRY(h->uflags.alloc(std::max<size_t>(1, P.units.size() * 8)));  // <= 8 RHS slices
     CUDA_TRY(cudaMemset(h->uflags.p, 0, sizeof(int32_t) * h->uflags.count));
@@ -387,6 +399,13 @@ int check_rhs(int32_t nrhs) {
     return GBCHOL_OK;
 }
 
+// Rows per ticket of the row kernels (GBCHOL_ROW_CHUNK overrides; tuning).
+int row_chunk() {
+    const char* e = std::getenv("GBCHOL_ROW_CHUNK");
+    int c = e ? std::atoi(e) : 2;
+    return c < 1 ? 1 : (c > 64 ? 64 : c);
+}
+
 // One full solve: leaf rows (lower) -> top units (lower) -> top units
 // (upper) -> leaf rows (upper). `in` is read through perm by the lower leaf
 // kernel; `out` is written through perm by both upper kernels.
@@ -407,6 +426,8 @@ int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in,
     lo.flags = h->flags.p;
     lo.status = h->status.p;
     lo.skip = skip;
+    lo.counters = h->counters.p;
+    lo.chunk = row_chunk();
     lo.epoch = h->next_epoch(s);
     CUDA_TRY(launch_row_sweep(lo, true, io, s));
     SnSweepArgs sn;
@@ -422,9 +443,14 @@ int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in,
     sn.uflags = h->uflags.p;
     sn.status = h->status.p;
     sn.skip = skip;
+    sn.dinv = f32 ? (const void*)h->dinv32.p : (const void*)h->dinv64.p;
+    sn.order = h->order_lo.p;
+    sn.counters = h->counters.p + 2;
     sn.epoch = h->next_epoch(s);
     CUDA_TRY(launch_sn_sweep(sn, true, io, s));
     sn.out = out;
+    sn.order = h->order_up.p;
+    sn.counters = h->counters.p + 4;
     sn.epoch = h->next_epoch(s);
     CUDA_TRY(launch_sn_sweep(sn, false, io, s));
     RowSweepArgs up = lo;
@@ -435,6 +461,7 @@ int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in,
     up.order = h->up_tasks.p;
     up.in = nullptr;
     up.out = out;
+    up.counters = h->counters.p + 6;
     up.epoch = h->next_epoch(s);
     CUDA_TRY(launch_row_sweep(up, false, io, s));
     return GBCHOL_OK;

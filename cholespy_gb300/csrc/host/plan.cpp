@@ -139,6 +139,42 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
         P.units[u].contrib_end = (int32_t)P.contribs.size();
     }
 
+    // inverses of the diagonal blocks (FP64 forward substitution on the
+    // identity), so that a unit's diagonal solve is one 32x32 product
+    P.dinv.assign((size_t)nunits * kChunk * kChunk, 0.0);
+    for (int32_t u = 0; u < nunits; ++u) {
+        const SnUnit& U = P.units[u];
+        const double* D = P.panels.data() + U.panel_col_off + U.pos0;  // D(i,j) = D[i + j*ld]
+        double* X = P.dinv.data() + (size_t)u * kChunk * kChunk;     // X(i,j) = X[i + j*32]
+        for (int32_t j = 0; j < U.w; ++j) {
+            for (int32_t i = j; i < U.w; ++i) {
+                double v = (i == j) ? 1.0 : 0.0;
+                for (int32_t k = j; k < i; ++k) v -= D[i + (size_t)k * U.ld] * X[k + j * kChunk];
+                X[i + j * kChunk] = v / D[i + (size_t)i * U.ld];
+            }
+        }
+    }
+    // dependency levels of the units, for level-ordered dynamic scheduling
+    {
+        std::vector<int32_t> lo((size_t)nunits, 0), up((size_t)nunits, 0);
+        for (int32_t u = 0; u < nunits; ++u)
+            for (int32_t e = P.units[u].contrib_begin; e < P.units[u].contrib_end; ++e)
+                lo[u] = std::max(lo[u], lo[P.contribs[e].src_unit] + 1);
+        for (int32_t u = nunits - 1; u >= 0; --u) {
+            const SnUnit& U = P.units[u];
+            if (U.parent_first_unit >= 0) up[u] = std::max(up[u], up[U.parent_first_unit] + 1);
+            const int32_t nlater = (U.sn_w - (U.pos0 + U.w) + kChunk - 1) / kChunk;
+            for (int32_t c = 0; c < nlater; ++c) up[u] = std::max(up[u], up[u + 1 + c] + 1);
+        }
+        P.unit_order_lo.resize((size_t)nunits);
+        P.unit_order_up.resize((size_t)nunits);
+        for (int32_t u = 0; u < nunits; ++u) P.unit_order_lo[u] = P.unit_order_up[u] = u;
+        std::stable_sort(P.unit_order_lo.begin(), P.unit_order_lo.end(),
+                         [&](int32_t a, int32_t b) { return lo[a] < lo[b]; });
+        std::stable_sort(P.unit_order_up.begin(), P.unit_order_up.end(),
+                         [&](int32_t a, int32_t b) { return up[a] < up[b]; });
+    }
+
     // ---- leaf region -------------------------------------------------------
     // CSR of L (columns ascending, diagonal last)
     std::vector<int32_t> rp, ci;

@@ -51,6 +51,9 @@ struct SolvePlan {
     std::vector<double> panels;           // column-major panels (FP64; cast for FP32)
     std::vector<SnUnit> units;            // in lower topological order
     std::vector<SnContrib> contribs;
+    std::vector<double> dinv;             // per unit: inverse of the diagonal block, 32x32 column-major
+    std::vector<int32_t> unit_order_lo;   // units sorted by lower-sweep dependency level
+    std::vector<int32_t> unit_order_up;   // units sorted by upper-sweep dependency level
     // leaf region, lower sweep: CSR over all rows. Leaf rows hold their full
     // row of L (diagonal last); top rows hold only their leaf-column entries.
     std::vector<int32_t> lo_rowptr, lo_cols;

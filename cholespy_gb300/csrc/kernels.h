@@ -42,6 +42,8 @@ struct RowSweepArgs {
     int epoch = 0;
     int* status = nullptr;
     const int* skip = nullptr;    // if non-null and *skip != 0 the sweep does nothing
+    int* counters = nullptr;      // [ticket, exited warps], zero between launches
+    int chunk = 1;                // consecutive tasks taken per ticket
 };
 
 enum class SweepIO {

@@ -9,8 +9,9 @@
 //     nonzeros (coalesced index/value loads, warp-shuffle reduction); for more
 //     RHS the lanes split the RHS columns, so x loads are coalesced, and the
 //     row's (col, val) pairs are loaded 32 at a time and broadcast by shuffle;
-//   * persistent cooperative grid with a static row assignment instead of a
-//     global atomic ticket (no contended atomic per row);
+//   * persistent grid; warps take rows (in level order) by an atomic ticket,
+//     so a warp only waits on rows with smaller tickets, all taken by running
+//     warps (no deadlock); the last warp out resets the ticket;
 //   * flags carry an epoch, so no per-solve memset of the flag array;
 //   * bounded waits (device.cuh).
 #include <cuda_runtime.h>
@@ -69,7 +70,13 @@ __global__ void __launch_bounds__(256) sweep_nnz_kernel(RowSweepArgs a) {
     const T* tmp = static_cast<const T*>(a.tmp);
     const int nrhs = a.nrhs;
     if (a.skip && dev::ld_volatile(a.skip)) return;
-    for (int t = warp; t < a.ntasks; t += nwarps) {
+    for (;;) {
+        int t0 = 0;
+        if (lane == 0) t0 = atomicAdd(a.counters, 1) * a.chunk;
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= a.ntasks) break;
+        const int tend = min(a.ntasks, t0 + a.chunk);
+        for (int t = t0; t < tend; ++t) {
         const int task = a.order[t];
         const bool partial = LOWER && task < 0;
         const int row = partial ? ~task : task;
@@ -122,6 +129,15 @@ __global__ void __launch_bounds__(256) sweep_nnz_kernel(RowSweepArgs a) {
         __syncwarp();
         // partial (top) rows publish nothing: their flags stay "always ready"
         if (lane == 0 && !partial) dev::st_release(a.flags + row, a.epoch);
+        }
+    }
+    // the last warp out resets the ticket for the next launch
+    if (lane == 0) {
+        __threadfence();
+        if (atomicAdd(a.counters + 1, 1) == nwarps - 1) {
+            a.counters[0] = 0;
+            a.counters[1] = 0;
+        }
     }
 }
 
@@ -139,7 +155,13 @@ __global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
     const T* tmp = static_cast<const T*>(a.tmp);
     const int nrhs = a.nrhs;
     if (a.skip && dev::ld_volatile(a.skip)) return;
-    for (int t = warp; t < a.ntasks; t += nwarps) {
+    for (;;) {
+        int t0 = 0;
+        if (lane == 0) t0 = atomicAdd(a.counters, 1) * a.chunk;
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= a.ntasks) break;
+        const int tend = min(a.ntasks, t0 + a.chunk);
+        for (int t = t0; t < tend; ++t) {
         const int task = a.order[t];
         const bool partial = LOWER && task < 0;
         const int row = partial ? ~task : task;
@@ -199,6 +221,15 @@ __global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
         __syncwarp();
         // partial (top) rows publish nothing: their flags stay "always ready"
         if (lane == 0 && !partial) dev::st_release(a.flags + row, a.epoch);
+        }
+    }
+    // the last warp out resets the ticket for the next launch
+    if (lane == 0) {
+        __threadfence();
+        if (atomicAdd(a.counters + 1, 1) == nwarps - 1) {
+            a.counters[0] = 0;
+            a.counters[1] = 0;
+        }
     }
 }
 
@@ -215,13 +246,13 @@ cudaError_t launch_io(const RowSweepArgs& a, cudaStream_t stream) {
     else if (r <= 64) fn = (const void*)sweep_rhs_kernel<io, LOWER, 32, 2>;
     else fn = (const void*)sweep_rhs_kernel<io, LOWER, 32, 4>;
     int grid = 0;
-    cudaError_t e = coop_grid(fn, 256, 0, &grid);
+    cudaError_t e = coop_grid(fn, 256, 0, &grid);  // resident blocks: a persistent grid
     if (e != cudaSuccess) return e;
-    const int need = (a.ntasks + 7) / 8;
+    const int need = (a.ntasks + 8 * a.chunk - 1) / (8 * a.chunk);
     if (grid > need) grid = need;
     RowSweepArgs copy = a;
     void* args[] = {&copy};
-    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, stream);
+    return cudaLaunchKernel(fn, dim3(grid), dim3(256), args, 0, stream);
 }
 
 }  // namespace

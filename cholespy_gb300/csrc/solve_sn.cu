@@ -22,9 +22,12 @@
 //   only the newest 32-row block sits on the dependency chain. Lane j holds
 //   column j of the unit and accumulates L[block, j]^T x_block; then the same
 //   fixed-order reduction and a transposed shuffle solve.
-// Items are assigned round-robin in topological order on a cooperatively
-// launched persistent grid: every CTA is resident, so the smallest unfinished
-// item can always run (no deadlock, no ticket atomic). Waits are bounded
+// The diagonal solve of a unit is one product with the precomputed inverse
+// of its 32x32 diagonal block (no 32-step substitution on the dependency
+// chain). Items are handed out by an atomic ticket in dependency-level order
+// to a persistent grid: a CTA only waits on items with smaller tickets, all
+// of which were taken by running CTAs, so there is no deadlock; the last CTA
+// to leave resets the counters for the next launch. Waits are bounded
 // (device.cuh). Results are deterministic: fixed block-to-warp assignment and
 // fixed reduction order.
 #include <cuda_runtime.h>
@@ -78,8 +81,14 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
     const int nitems = a.n_units * a.nslices;
     T (*xs)[KW + 1] = sm.xs[warp];
     if (LOWER) sm.inv[warp][lane] = -1;
-    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int uidx = LOWER ? item / a.nslices : a.n_units - 1 - item / a.nslices;
+    __shared__ int ticket;
+    for (;;) {
+        if (tid == 0) ticket = atomicAdd(a.counters, 1);
+        __syncthreads();
+        const int item = ticket;
+        __syncthreads();
+        if (item >= nitems) break;
+        const int uidx = a.order[item / a.nslices];
         const int slice = item % a.nslices;
         const int k0 = slice * KW;
         const int kw = min(KW, nrhs - k0);
@@ -173,10 +182,8 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
         // fixed-order reduction of the warps' partial sums
 #pragma unroll
         for (int k = 0; k < KW; ++k) xs[lane][k] = acc[k];
-        for (int idx = tid; idx < kW * kW; idx += kT) {
-            const int i = idx & 31, j = idx >> 5;
-            if (i < w && j < w) sm.d[i][j] = panels[U.panel_col_off + U.pos0 + i + (size_t)j * U.ld];
-        }
+        const T* __restrict__ dinv = static_cast<const T*>(a.dinv) + (size_t)uidx * kW * kW;
+        for (int idx = tid; idx < kW * kW; idx += kT) sm.d[idx & 31][idx >> 5] = dinv[idx];
         __syncthreads();
         for (int idx = tid; idx < kW * KW; idx += kT) {
             const int i = idx / KW, k = idx % KW;
@@ -186,21 +193,15 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
             sm.t[i][k] = (i < w && k < kw) ? tmp[(size_t)(U.c0 + i) * nrhs + k0 + k] - s : T(0);
         }
         __syncthreads();
-        // diagonal block: warp per RHS column, lane per row
+        // diagonal block: x = D^{-1} t (lower) or D^{-T} t (upper); lane = row
         for (int k = warp; k < kw; k += kWarps) {
-            T v = sm.t[lane][k];
+            T v = T(0);
             if (LOWER) {
-                for (int j = 0; j < w; ++j) {
-                    const T xj = __shfl_sync(0xffffffffu, v, j) / sm.d[j][j];
-                    if (lane == j) v = xj;
-                    else if (lane > j && lane < w) v = fma(-sm.d[lane][j], xj, v);
-                }
+#pragma unroll 8
+                for (int j = 0; j < kW; ++j) v = fma(sm.d[lane][j], sm.t[j][k], v);
             } else {
-                for (int j = w - 1; j >= 0; --j) {
-                    const T xj = __shfl_sync(0xffffffffu, v, j) / sm.d[j][j];
-                    if (lane == j) v = xj;
-                    else if (lane < j) v = fma(-sm.d[j][lane], xj, v);
-                }
+#pragma unroll 8
+                for (int j = 0; j < kW; ++j) v = fma(sm.d[j][lane], sm.t[j][k], v);
             }
             if (lane < w) {
                 tmp[(size_t)(U.c0 + lane) * nrhs + k0 + k] = v;
@@ -217,6 +218,14 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
         __syncthreads();
         if (tid == 0) dev::st_release(a.uflags + (size_t)uidx * a.nslices + slice, a.epoch);
     }
+    // the last CTA out resets the ticket for the next launch
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(a.counters + 1, 1) == (int)gridDim.x - 1) {
+            a.counters[0] = 0;
+            a.counters[1] = 0;
+        }
+    }
 }
 
 template <class io, bool LOWER, int KW>
@@ -228,13 +237,12 @@ cudaError_t launch_sn_kw(const SnSweepArgs& a, cudaStream_t stream) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int grid = 0;
-    e = coop_grid(fn, kT, smem, &grid);
+    e = coop_grid(fn, kT, smem, &grid);  // resident CTAs: a persistent grid
     if (e != cudaSuccess) return e;
     const int items = a.n_units * a.nslices;
     if (grid > items) grid = items;
-    SnSweepArgs copy = a;
-    void* args[] = {&copy};
-    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kT), args, smem, stream);
+    sn_sweep_kernel<io, LOWER, KW><<<grid, kT, smem, stream>>>(a);
+    return cudaGetLastError();
 }
 
 template <class io, bool LOWER>

@@ -18,6 +18,9 @@ struct SnSweepArgs {
     const int32_t* perm = nullptr;
     void* tmp = nullptr;            // T, n x nrhs, permuted space
     void* out = nullptr;            // upper: solution through perm (TOut)
+    const int32_t* order = nullptr; // units in dependency-level order for this sweep
+    const void* dinv = nullptr;     // T, per unit 32x32 inverse diagonal block (column-major)
+    int* counters = nullptr;        // [ticket, exited CTAs], zero between launches
     int* uflags = nullptr;          // n_units * nslices completion flags
     int epoch = 0;
     int* status = nullptr;
