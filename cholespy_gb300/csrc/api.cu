@@ -113,8 +113,9 @@ struct gbchol_solver {
     // solve plan (see host/plan.cpp)
     SolvePlan plan;
     DevBuf<int32_t> lo_rowptr, lo_cols, lo_tasks, up_rowptr, up_cols, up_tasks, sn_rows;
-    DevBuf<float> lo_v32, up_v32, pan32;
-    DevBuf<double> lo_v64, up_v64, pan64;
+    DevBuf<int32_t> upt_rowptr, upt_cols, upt_tasks;
+    DevBuf<float> lo_v32, up_v32, pan32, upt_v32;
+    DevBuf<double> lo_v64, up_v64, pan64, upt_v64;
     DevBuf<SnUnit> units;
     DevBuf<SnContrib> contribs;
     DevBuf<int32_t> uflags;   // units * RHS slices
@@ -293,24 +294,20 @@ int setup_plan(gbchol_solver* h, const std::vector<int32_t>& rp, const std::vect
     CUDA_TRY(h->lo_tasks.upload(P.lo_tasks.data(), P.lo_tasks.size()));
     if (f32) CUDA_TRY(upload_cast(h->lo_v32, P.lo_vals));
     if (f64) CUDA_TRY(h->lo_v64.upload(P.lo_vals.data(), P.lo_vals.size()));
-    // upper leaf sweep: columns of L for leaf rows only (top rows: empty)
-    {
-        std::vector<int32_t> uptr((size_t)n + 1, 0), ucol;
-        std::vector<double> uval;
-        for (int32_t j = 0; j < n; ++j)
-            uptr[j + 1] = uptr[j] + (P.row_top[j] ? 0 : F.colptr[j + 1] - F.colptr[j]);
-        ucol.reserve((size_t)uptr[n]);
-        uval.reserve((size_t)uptr[n]);
-        for (int32_t j = 0; j < n; ++j) {
-            if (P.row_top[j]) continue;
-            ucol.insert(ucol.end(), F.rowidx.begin() + F.colptr[j], F.rowidx.begin() + F.colptr[j + 1]);
-            uval.insert(uval.end(), F.vals.begin() + F.colptr[j], F.vals.begin() + F.colptr[j + 1]);
-        }
-        CUDA_TRY(h->up_rowptr.upload(uptr.data(), uptr.size()));
-        CUDA_TRY(h->up_cols.upload(ucol.data(), ucol.size()));
-        if (f32) CUDA_TRY(upload_cast(h->up_v32, uval));
-        if (f64) CUDA_TRY(h->up_v64.upload(uval.data(), uval.size()));
-    }
+    // upper leaf sweep: top-row part (partial pass) and diagonal + leaf part
+    CUDA_TRY(h->upt_rowptr.upload(P.upt_rowptr.data(), P.upt_rowptr.size()));
+    CUDA_TRY(h->upt_cols.upload(P.upt_cols.data(), P.upt_cols.size()));
+    CUDA_TRY(h->upt_tasks.upload(P.upt_tasks.data(), P.upt_tasks.size()));
+    if (f32) CUDA_TRY(upload_cast(h->upt_v32, P.upt_vals));
+    if (f64) CUDA_TRY(h->upt_v64.upload(P.upt_vals.data(), P.upt_vals.size()));
+    CUDA_TRY(h->up_rowptr.upload(P.upl_rowptr.data(), P.upl_rowptr.size()));
+    CUDA_TRY(h->up_cols.upload(P.upl_cols.data(), P.upl_cols.size()));
+    if (f32) CUDA_TRY(upload_cast(h->up_v32, P.upl_vals));
+    if (f64) CUDA_TRY(h->up_v64.upload(P.upl_vals.data(), P.upl_vals.size()));
+    P.upt_vals.clear();
+    P.upt_vals.shrink_to_fit();
+    P.upl_vals.clear();
+    P.upl_vals.shrink_to_fit();
     CUDA_TRY(h->up_tasks.upload(P.up_tasks.data(), P.up_tasks.size()));
     // top region
     CUDA_TRY(h->sn_rows.upload(P.sn_rows.data(), P.sn_rows.size()));
@@ -323,8 +320,8 @@ int setup_plan(gbchol_solver* h, const std::vector<int32_t>& rp, const std::vect
     if (f64) CUDA_TRY(h->dinv64.upload(P.dinv.data(), P.dinv.size()));
     P.dinv.clear();
     P.dinv.shrink_to_fit();
-    CUDA_TRY(h->counters.alloc(8));
-    CUDA_TRY(cudaMemset(h->counters.p, 0, sizeof(int32_t) * 8));
+    CUDA_TRY(h->counters.alloc(10));
+    CUDA_TRY(cudaMemset(h->counters.p, 0, sizeof(int32_t) * 10));
     CUDA_TRY(h->contribs.upload(P.contribs.data(), P.contribs.size()));
     CUDA_TRY(h->uflags.alloc(std::max<size_t>(1, P.units.size() * 8)));  // <= 8 RHS slices
     CUDA_TRY(cudaMemset(h->uflags.p, 0, sizeof(int32_t) * h->uflags.count));
@@ -453,6 +450,17 @@ int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in,
     sn.counters = h->counters.p + 4;
     sn.epoch = h->next_epoch(s);
     CUDA_TRY(launch_sn_sweep(sn, false, io, s));
+    RowSweepArgs pt = lo;  // top-row terms of the leaf rows: no waits
+    pt.ntasks = (int)P.upt_tasks.size();
+    pt.rowptr = h->upt_rowptr.p;
+    pt.cols = h->upt_cols.p;
+    pt.vals = f32 ? (const void*)h->upt_v32.p : (const void*)h->upt_v64.p;
+    pt.order = h->upt_tasks.p;
+    pt.in = nullptr;
+    pt.out = out;
+    pt.counters = h->counters.p + 8;
+    pt.epoch = h->next_epoch(s);
+    CUDA_TRY(launch_row_sweep(pt, false, io, s));
     RowSweepArgs up = lo;
     up.ntasks = (int)P.up_tasks.size();
     up.rowptr = h->up_rowptr.p;
@@ -470,7 +478,8 @@ int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in,
 // Kernel launches of one run_sweeps call.
 int sweep_launches(const gbchol_solver* h) {
     const SolvePlan& P = h->plan;
-    return (P.lo_tasks.empty() ? 0 : 1) + (P.units.empty() ? 0 : 2) + (P.up_tasks.empty() ? 0 : 1);
+    return (P.lo_tasks.empty() ? 0 : 1) + (P.units.empty() ? 0 : 2) + (P.upt_tasks.empty() ? 0 : 1) +
+           (P.up_tasks.empty() ? 0 : 1);
 }
 
 }  // namespace

@@ -206,6 +206,39 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
         if (P.row_top[i]) P.lo_tasks.push_back(~i);
     for (int32_t r : upper_order)
         if (!P.row_top[r]) P.up_tasks.push_back(r);
+    // upper sweep: split every leaf column of L into its top-row entries and
+    // its diagonal + leaf-row entries (top columns: both empty)
+    P.upt_rowptr.assign((size_t)n + 1, 0);
+    P.upl_rowptr.assign((size_t)n + 1, 0);
+    for (int32_t j = 0; j < n; ++j) {
+        int32_t nt = 0, nl = 0;
+        if (!P.row_top[j]) {
+            nl = 1;
+            for (int32_t k = F.colptr[j] + 1; k < F.colptr[j + 1]; ++k)
+                (P.row_top[F.rowidx[k]] ? nt : nl)++;
+        }
+        P.upt_rowptr[j + 1] = P.upt_rowptr[j] + nt;
+        P.upl_rowptr[j + 1] = P.upl_rowptr[j] + nl;
+        if (nt > 0) P.upt_tasks.push_back(~j);
+    }
+    P.upt_cols.resize((size_t)P.upt_rowptr[n]);
+    P.upt_vals.resize((size_t)P.upt_rowptr[n]);
+    P.upl_cols.resize((size_t)P.upl_rowptr[n]);
+    P.upl_vals.resize((size_t)P.upl_rowptr[n]);
+    for (int32_t j = 0; j < n; ++j) {
+        if (P.row_top[j]) continue;
+        int32_t dt = P.upt_rowptr[j], dl = P.upl_rowptr[j];
+        for (int32_t k = F.colptr[j]; k < F.colptr[j + 1]; ++k) {
+            const int32_t r = F.rowidx[k];
+            if (k > F.colptr[j] && P.row_top[r]) {
+                P.upt_cols[dt] = r;
+                P.upt_vals[dt++] = F.vals[k];
+            } else {
+                P.upl_cols[dl] = r;
+                P.upl_vals[dl++] = F.vals[k];
+            }
+        }
+    }
 }
 
 }  // namespace gbchol

@@ -60,6 +60,13 @@ struct SolvePlan {
     std::vector<double> lo_vals;
     std::vector<int32_t> lo_tasks;        // leaf rows in level order, then ~row for top rows
     std::vector<int32_t> up_tasks;        // leaf rows in L^T level order
+    // upper sweep, leaf rows: columns of L split into the top-row part
+    // (final before the leaf sweep starts: one wait-free "partial" pass) and
+    // the diagonal + leaf-row part (the chained row sweep)
+    std::vector<int32_t> upt_rowptr, upt_cols, upt_tasks;
+    std::vector<double> upt_vals;
+    std::vector<int32_t> upl_rowptr, upl_cols;
+    std::vector<double> upl_vals;
     int32_t max_row_len = 0;
 };
 

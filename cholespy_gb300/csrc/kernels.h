@@ -32,8 +32,8 @@ struct RowSweepArgs {
     const int* rowptr = nullptr;
     const int* cols = nullptr;
     const void* vals = nullptr;   // T
-    const int* order = nullptr;   // rows in dependency order; ~row = partial row (lower
-                                  // sweep only): no diagonal, tmp[row] = in - sum
+    const int* order = nullptr;   // rows in dependency order; ~row = partial row: no
+                                  // diagonal, tmp[row] = (lower: in, upper: tmp) - sum
     const int* perm = nullptr;
     const void* in = nullptr;     // lower: right-hand side (TIn), read through perm
     void* tmp = nullptr;          // T, n x nrhs, permuted space

@@ -36,11 +36,11 @@ struct IO {
 // sweep, to the user array through perm.
 template <class io, bool LOWER>
 __device__ __forceinline__ void emit(const RowSweepArgs& a, int row, int prow, int j,
-                                     typename io::t v) {
+                                     typename io::t v, bool partial) {
     using T = typename io::t;
     T* tmp = static_cast<T*>(a.tmp);
     tmp[(size_t)row * a.nrhs + j] = v;
-    if (!LOWER) {
+    if (!LOWER && !partial) {
         using TO = typename io::tout;
         TO* out = static_cast<TO*>(a.out);
         size_t o = (size_t)prow * a.nrhs + j;
@@ -78,10 +78,10 @@ __global__ void __launch_bounds__(256) sweep_nnz_kernel(RowSweepArgs a) {
         const int tend = min(a.ntasks, t0 + a.chunk);
         for (int t = t0; t < tend; ++t) {
         const int task = a.order[t];
-        const bool partial = LOWER && task < 0;
+        const bool partial = task < 0;
         const int row = partial ? ~task : task;
         const int s = a.rowptr[row], e = a.rowptr[row + 1];
-        const int lo = LOWER ? s : s + 1;
+        const int lo = (LOWER || partial) ? s : s + 1;
         const int hi = (LOWER && !partial) ? e - 1 : e;
         T acc[R];
 #pragma unroll
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) sweep_nnz_kernel(RowSweepArgs a) {
         if (lane < nrhs) {
             T v = load_rhs<io, LOWER>(a, row, prow, lane) - mine;
             if (!partial) v = v / diag;
-            emit<io, LOWER>(a, row, prow, lane, v);
+            emit<io, LOWER>(a, row, prow, lane, v, partial);
             __threadfence();
         }
         __syncwarp();
@@ -163,10 +163,10 @@ __global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
         const int tend = min(a.ntasks, t0 + a.chunk);
         for (int t = t0; t < tend; ++t) {
         const int task = a.order[t];
-        const bool partial = LOWER && task < 0;
+        const bool partial = task < 0;
         const int row = partial ? ~task : task;
         const int s = a.rowptr[row], e = a.rowptr[row + 1];
-        const int lo = LOWER ? s : s + 1;
+        const int lo = (LOWER || partial) ? s : s + 1;
         const int hi = (LOWER && !partial) ? e - 1 : e;
         T acc[Q];
 #pragma unroll
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
                 if (j < nrhs) {
                     T v = load_rhs<io, LOWER>(a, row, prow, j) - acc[q];
                     if (!partial) v = v / diag;
-                    emit<io, LOWER>(a, row, prow, j, v);
+                    emit<io, LOWER>(a, row, prow, j, v, partial);
                 }
             }
             __threadfence();
