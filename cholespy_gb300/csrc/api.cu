@@ -399,7 +399,7 @@ int check_rhs(int32_t nrhs) {
 // Rows per ticket of the row kernels (GBCHOL_ROW_CHUNK overrides; tuning).
 int row_chunk() {
     const char* e = std::getenv("GBCHOL_ROW_CHUNK");
-    int c = e ? std::atoi(e) : 2;
+    int c = e ? std::atoi(e) : 1;
     return c < 1 ? 1 : (c > 64 ? 64 : c);
 }
 

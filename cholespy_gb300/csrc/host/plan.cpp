@@ -204,8 +204,29 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
         if (!P.row_top[r]) P.lo_tasks.push_back(r);
     for (int32_t i = 0; i < n; ++i)
         if (P.row_top[i]) P.lo_tasks.push_back(~i);
-    for (int32_t r : upper_order)
-        if (!P.row_top[r]) P.up_tasks.push_back(r);
+    // upper leaf sweep: order by depth below the top region (number of leaf
+    // ancestors), so every leaf subtree advances one level per step whatever
+    // the depth of the top node it hangs from
+    {
+        std::vector<int32_t> parent((size_t)n, -1), ldepth((size_t)n, 0);
+        for (int32_t j = 0; j < n; ++j)
+            if (F.colptr[j + 1] - F.colptr[j] > 1) parent[j] = F.rowidx[F.colptr[j] + 1];
+        int32_t maxd = 0;
+        for (int32_t j = n - 1; j >= 0; --j) {
+            if (P.row_top[j]) continue;
+            const int32_t p = parent[j];
+            ldepth[j] = (p >= 0 && !P.row_top[p]) ? ldepth[p] + 1 : 0;
+            maxd = std::max(maxd, ldepth[j]);
+        }
+        std::vector<int32_t> cnt((size_t)maxd + 2, 0);
+        for (int32_t j = 0; j < n; ++j)
+            if (!P.row_top[j]) cnt[(size_t)ldepth[j] + 1]++;
+        for (int32_t d = 0; d <= maxd; ++d) cnt[(size_t)d + 1] += cnt[d];
+        P.up_tasks.assign((size_t)cnt[(size_t)maxd + 1], 0);
+        for (int32_t j = 0; j < n; ++j)
+            if (!P.row_top[j]) P.up_tasks[cnt[ldepth[j]]++] = j;
+    }
+    (void)upper_order;
     // upper sweep: split every leaf column of L into its top-row entries and
     // its diagonal + leaf-row entries (top columns: both empty)
     P.upt_rowptr.assign((size_t)n + 1, 0);

@@ -124,11 +124,14 @@ __global__ void __launch_bounds__(256) sweep_nnz_kernel(RowSweepArgs a) {
             T v = load_rhs<io, LOWER>(a, row, prow, lane) - mine;
             if (!partial) v = v / diag;
             emit<io, LOWER>(a, row, prow, lane, v, partial);
-            __threadfence();
         }
         __syncwarp();
-        // partial (top) rows publish nothing: their flags stay "always ready"
-        if (lane == 0 && !partial) dev::st_release(a.flags + row, a.epoch);
+        // partial (top) rows publish nothing: their flags stay "always ready";
+        // the warp barrier orders the lanes' writes before lane 0's release
+        if (lane == 0 && !partial) {
+            __threadfence();
+            dev::st_release(a.flags + row, a.epoch);
+        }
         }
     }
     // the last warp out resets the ticket for the next launch
@@ -216,11 +219,14 @@ __global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
                     emit<io, LOWER>(a, row, prow, j, v, partial);
                 }
             }
-            __threadfence();
         }
         __syncwarp();
-        // partial (top) rows publish nothing: their flags stay "always ready"
-        if (lane == 0 && !partial) dev::st_release(a.flags + row, a.epoch);
+        // partial (top) rows publish nothing: their flags stay "always ready";
+        // the warp barrier orders the lanes' writes before lane 0's release
+        if (lane == 0 && !partial) {
+            __threadfence();
+            dev::st_release(a.flags + row, a.epoch);
+        }
         }
     }
     // the last warp out resets the ticket for the next launch

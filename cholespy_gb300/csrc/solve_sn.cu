@@ -94,6 +94,16 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
         const int kw = min(KW, nrhs - k0);
         const SnUnit U = a.units[uidx];
         const int w = U.w;
+        // off the dependency chain: the unit's current right-hand side and
+        // its inverse diagonal block go to shared memory first
+        {
+            const T* __restrict__ dinv = static_cast<const T*>(a.dinv) + (size_t)uidx * kW * kW;
+            for (int idx = tid; idx < kW * kW; idx += kT) sm.d[idx & 31][idx >> 5] = dinv[idx];
+            for (int idx = tid; idx < kW * KW; idx += kT) {
+                const int i = idx / KW, k = idx % KW;
+                sm.t[i][k] = (i < w && k < kw) ? tmp[(size_t)(U.c0 + i) * nrhs + k0 + k] : T(0);
+            }
+        }
         T acc[KW];
 #pragma unroll
         for (int k = 0; k < KW; ++k) acc[k] = T(0);
@@ -182,15 +192,13 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
         // fixed-order reduction of the warps' partial sums
 #pragma unroll
         for (int k = 0; k < KW; ++k) xs[lane][k] = acc[k];
-        const T* __restrict__ dinv = static_cast<const T*>(a.dinv) + (size_t)uidx * kW * kW;
-        for (int idx = tid; idx < kW * kW; idx += kT) sm.d[idx & 31][idx >> 5] = dinv[idx];
         __syncthreads();
         for (int idx = tid; idx < kW * KW; idx += kT) {
             const int i = idx / KW, k = idx % KW;
             T s = T(0);
 #pragma unroll
             for (int ww = 0; ww < kWarps; ++ww) s += sm.xs[ww][i][k];
-            sm.t[i][k] = (i < w && k < kw) ? tmp[(size_t)(U.c0 + i) * nrhs + k0 + k] - s : T(0);
+            sm.t[i][k] -= s;
         }
         __syncthreads();
         // diagonal block: x = D^{-1} t (lower) or D^{-T} t (upper); lane = row
@@ -214,9 +222,12 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
                 }
             }
         }
-        __threadfence();
+        // the barrier orders the CTA's writes before thread 0's release
         __syncthreads();
-        if (tid == 0) dev::st_release(a.uflags + (size_t)uidx * a.nslices + slice, a.epoch);
+        if (tid == 0) {
+            __threadfence();
+            dev::st_release(a.uflags + (size_t)uidx * a.nslices + slice, a.epoch);
+        }
     }
     // the last CTA out resets the ticket for the next launch
     if (tid == 0) {
