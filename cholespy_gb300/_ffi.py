@@ -66,6 +66,12 @@ def _declare(lib):
                                          C.POINTER(D)]),
         "gbchol_factor_export": (C.c_int, [P, P, P, P, P]),
         "gbchol_factor_free": (C.c_int, [P]),
+        "gbchol_batch_create": (C.c_int, [I32, P, P, I32, C.POINTER(P)]),
+        "gbchol_batch_set_io": (C.c_int, [P, P, P]),
+        "gbchol_batch_solve": (C.c_int, [P, P]),
+        "gbchol_batch_info": (C.c_int, [P, C.POINTER(I32), C.POINTER(I64), C.POINTER(I64)]),
+        "gbchol_batch_check": (C.c_int, [P, P]),
+        "gbchol_batch_destroy": (C.c_int, [P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

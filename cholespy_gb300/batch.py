@@ -1,0 +1,106 @@
+"""Batched solves: many factors of uneven sizes and RHS counts in one
+persistent launch per sweep phase (gbchol_batch_* in include/gbchol.h).
+
+    batch = BatchSolver([s0, s1, ...], nrhs=[r0, r1, ...])
+    batch.solve(bs, xs)          # bs[k], xs[k]: CUDA tensors (n_k, r_k)
+    g = batch.capture(bs, xs)    # CUDA graph of the bound solve
+    g.replay()
+
+No counterpart in the reference (each of its solvers is solved separately).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from . import _ffi
+from .solver import CholeskySolverD, CholeskySolverF
+
+
+class BatchSolver:
+    def __init__(self, solvers, nrhs):
+        if not solvers:
+            raise ValueError("A batch needs at least one solver.")
+        kinds = {type(s) for s in solvers}
+        if kinds == {CholeskySolverF}:
+            self._precision = 0
+        elif kinds <= {CholeskySolverD}:
+            self._precision = 1
+        else:
+            raise ValueError("A batch holds solvers of one precision.")
+        if len(nrhs) != len(solvers):
+            raise ValueError("One RHS count per solver.")
+        self._solvers = list(solvers)          # keep the factors alive
+        self._nrhs = [int(r) for r in nrhs]
+        self._device = solvers[0]._device
+        arr = (C.c_void_p * len(solvers))(*[s.handle.value for s in solvers])
+        rr = (C.c_int32 * len(solvers))(*self._nrhs)
+        h = C.c_void_p()
+        _ffi.check(_ffi.lib().gbchol_batch_create(len(solvers), arr, rr, self._precision, C.byref(h)))
+        self._h = h
+        self._bound = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _ffi.lib().gbchol_batch_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def _check_io(self, bs, xs):
+        import torch
+        dt = torch.float32 if self._precision == 0 else torch.float64
+        if len(bs) != len(self._solvers) or len(xs) != len(self._solvers):
+            raise ValueError("One b and one x per solver.")
+        for s, r, b, x in zip(self._solvers, self._nrhs, bs, xs):
+            for t in (b, x):
+                if not t.is_cuda or t.device.index != self._device:
+                    raise ValueError("Batch arrays must be CUDA tensors on the solvers' device.")
+                if t.dtype != dt or not t.is_contiguous():
+                    raise TypeError(f"Batch arrays must be C-contiguous {dt}.")
+                shape = tuple(t.shape)
+                if shape != (s._n, r) and not (r == 1 and shape == (s._n,)):
+                    raise ValueError("b and x of system k must have shape (n_k, nrhs_k).")
+
+    def bind(self, bs, xs):
+        """Bind the per-system device arrays (uploads the descriptor tables)."""
+        self._check_io(bs, xs)
+        key = tuple((b.data_ptr(), x.data_ptr()) for b, x in zip(bs, xs))
+        if key == self._bound:
+            return
+        n = len(bs)
+        bp = (C.c_void_p * n)(*[b.data_ptr() for b in bs])
+        xp = (C.c_void_p * n)(*[x.data_ptr() for x in xs])
+        _ffi.check(_ffi.lib().gbchol_batch_set_io(self._h, bp, xp))
+        self._keep = (list(bs), list(xs))
+        self._bound = key
+
+    def solve(self, bs=None, xs=None):
+        """Solve every system (asynchronously on the current CUDA stream)."""
+        import torch
+        if bs is not None:
+            self.bind(bs, xs)
+        stream = torch.cuda.current_stream(self._device).cuda_stream
+        _ffi.check(_ffi.lib().gbchol_batch_solve(self._h, C.c_void_p(stream)))
+
+    def check(self):
+        import torch
+        stream = torch.cuda.current_stream(self._device).cuda_stream
+        _ffi.check(_ffi.lib().gbchol_batch_check(self._h, C.c_void_p(stream)))
+
+    def info(self):
+        la, z, r = C.c_int32(), C.c_int64(), C.c_int64()
+        _ffi.check(_ffi.lib().gbchol_batch_info(self._h, C.byref(la), C.byref(z), C.byref(r)))
+        return {"launches": la.value, "nnz_l": z.value, "rows": r.value}
+
+    def capture(self, bs, xs):
+        """CUDA graph of one batched solve on the given arrays (replay() to run)."""
+        import torch
+        self.bind(bs, xs)
+        self.solve()  # warm up outside capture
+        torch.cuda.synchronize(self._device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.solve()
+        return g

@@ -17,138 +17,20 @@
 #include <string>
 #include <vector>
 
-#include "gbchol.h"
-#include "host/host.h"
-#include "host/plan.h"
-#include "kernels.h"
-#include "refine.h"
-#include "solve_sn.h"
+#include "solver_impl.h"
 
 using namespace gbchol;
 
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
 
+namespace gbchol {
 int fail(int code, const std::string& msg) {
     g_last_error = msg;
     return code;
 }
-
-struct DeviceGuard {
-    int prev = -1;
-    bool changed = false;
-    explicit DeviceGuard(int dev) {
-        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) {
-            changed = cudaSetDevice(dev) == cudaSuccess;
-        }
-    }
-    ~DeviceGuard() {
-        if (changed) cudaSetDevice(prev);
-    }
-};
-
-#define CUDA_TRY(expr)                                                                     \
-    do {                                                                                   \
-        cudaError_t _e = (expr);                                                           \
-        if (_e != cudaSuccess)                                                             \
-            return fail(_e == cudaErrorMemoryAllocation ? GBCHOL_ENOMEM : GBCHOL_ECUDA,    \
-                        std::string("CUDA error: ") + cudaGetErrorString(_e) + " (" #expr   \
-                                                                               ")");        \
-    } while (0)
-
-template <typename T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t count = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf&) = delete;
-    DevBuf& operator=(const DevBuf&) = delete;
-    ~DevBuf() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        count = 0;
-    }
-    cudaError_t alloc(size_t n) {
-        release();
-        if (n == 0) n = 1;
-        cudaError_t e = cudaMalloc(&p, n * sizeof(T));
-        if (e == cudaSuccess) count = n;
-        else p = nullptr;
-        return e;
-    }
-    cudaError_t upload(const T* h, size_t n) {
-        cudaError_t e = alloc(n);
-        if (e != cudaSuccess || n == 0) return e;
-        return cudaMemcpy(p, h, n * sizeof(T), cudaMemcpyHostToDevice);
-    }
-};
-
-// One triangle (L or L^T) in CSR form with its level analysis.
-struct Triangle {
-    DevBuf<int32_t> rowptr, cols, order;
-    DevBuf<float> v32;
-    DevBuf<double> v64;
-    std::vector<int32_t> row_levels, order_h;
-    int32_t max_lvl = 0;
-    bool general_kernel = false;  // analysis needed the sync-free kernel
-};
-
-}  // namespace
-
-struct gbchol_host_factor {
-    Factor F;
-};
-
-struct gbchol_solver {
-    int device = 0;
-    int32_t n = 0;
-    int32_t store = 0;
-    Factor F;                 // host copy of the factor
-    int64_t nnz_a = 0;
-    double t_factor = 0.0, t_analysis = 0.0;
-    DevBuf<int32_t> perm;
-    Triangle lower, upper;    // level analysis of L (CSR, diagonal last) and L^T
-    // solve plan (see host/plan.cpp)
-    SolvePlan plan;
-    DevBuf<int32_t> lo_rowptr, lo_cols, lo_tasks, up_rowptr, up_cols, up_tasks, sn_rows;
-    DevBuf<int32_t> upt_rowptr, upt_cols, upt_tasks;
-    DevBuf<float> lo_v32, up_v32, pan32, upt_v32;
-    DevBuf<double> lo_v64, up_v64, pan64, upt_v64;
-    DevBuf<SnUnit> units;
-    DevBuf<SnContrib> contribs;
-    DevBuf<int32_t> uflags;   // units * RHS slices
-    DevBuf<int32_t> order_lo, order_up;  // units in dependency-level order
-    DevBuf<float> dinv32;
-    DevBuf<double> dinv64;    // inverse diagonal blocks of the units
-    DevBuf<int32_t> counters; // [ticket, exits] per sweep kernel (4 kernels)
-    std::vector<int32_t> flags_init;  // 0 for leaf rows, INT_MAX for top rows
-    DevBuf<int32_t> a_rowptr, a_cols;
-    DevBuf<double> a_vals;    // symmetric A, original ordering
-    DevBuf<int32_t> flags, status;
-    DevBuf<int32_t> max_lvl;
-    int epoch = 0;
-    DevBuf<unsigned char> tmp;      // permuted-space work array
-    DevBuf<double> r64;             // refinement residual
-    DevBuf<double> partials;        // refinement block partial sums
-    DevBuf<RefineState> rstate;
-    cudaStream_t last_stream = nullptr;
-
-    int next_epoch(cudaStream_t s) {
-        if (epoch >= INT_MAX - 8) {
-            if (!flags_init.empty())
-                cudaMemcpyAsync(flags.p, flags_init.data(), sizeof(int32_t) * flags_init.size(),
-                                cudaMemcpyHostToDevice, s);
-            else
-                cudaMemsetAsync(flags.p, 0, sizeof(int32_t) * (size_t)std::max(n, 1), s);
-            if (uflags.p) cudaMemsetAsync(uflags.p, 0, sizeof(int32_t) * uflags.count, s);
-            cudaStreamSynchronize(s);
-            epoch = 0;
-        }
-        return ++epoch;
-    }
-};
+}  // namespace gbchol
 
 namespace {
 
@@ -322,6 +204,12 @@ int setup_plan(gbchol_solver* h, const std::vector<int32_t>& rp, const std::vect
     P.dinv.shrink_to_fit();
     CUDA_TRY(h->counters.alloc(10));
     CUDA_TRY(cudaMemset(h->counters.p, 0, sizeof(int32_t) * 10));
+    {
+        // solve sweeps count epochs from 1 on the device; row flags start at
+        // 0 (leaf rows) or INT_MAX (top rows, always ready for the row kernels)
+        const int32_t one = 1;
+        CUDA_TRY(h->dev_epoch.upload(&one, 1));
+    }
     CUDA_TRY(h->contribs.upload(P.contribs.data(), P.contribs.size()));
     CUDA_TRY(h->uflags.alloc(std::max<size_t>(1, P.units.size() * 8)));  // <= 8 RHS slices
     CUDA_TRY(cudaMemset(h->uflags.p, 0, sizeof(int32_t) * h->uflags.count));
@@ -396,12 +284,15 @@ int check_rhs(int32_t nrhs) {
     return GBCHOL_OK;
 }
 
-// Rows per ticket of the row kernels (GBCHOL_ROW_CHUNK overrides; tuning).
-int row_chunk() {
+}  // namespace
+
+int gbchol::row_chunk() {
     const char* e = std::getenv("GBCHOL_ROW_CHUNK");
     int c = e ? std::atoi(e) : 1;
     return c < 1 ? 1 : (c > 64 ? 64 : c);
 }
+
+namespace {
 
 // One full solve: leaf rows (lower) -> top units (lower) -> top units
 // (upper) -> leaf rows (upper). `in` is read through perm by the lower leaf
@@ -409,68 +300,65 @@ int row_chunk() {
 int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in, void* out,
                const int* skip, cudaStream_t s) {
     const SolvePlan& P = h->plan;
+    RowSys rs;
+    rs.perm = h->perm.p;
+    rs.tmp = h->tmp.p;
+    rs.flags = h->flags.p;
+    rs.nrhs = nrhs;
     RowSweepArgs lo;
-    lo.n = h->n;
+    lo.sys0 = rs;
+    lo.sys0.rowptr = h->lo_rowptr.p;
+    lo.sys0.cols = h->lo_cols.p;
+    lo.sys0.vals = f32 ? (const void*)h->lo_v32.p : (const void*)h->lo_v64.p;
+    lo.sys0.in = in;
+    lo.tasks = h->lo_tasks.p;
     lo.ntasks = (int)P.lo_tasks.size();
-    lo.nrhs = nrhs;
-    lo.rowptr = h->lo_rowptr.p;
-    lo.cols = h->lo_cols.p;
-    lo.vals = f32 ? (const void*)h->lo_v32.p : (const void*)h->lo_v64.p;
-    lo.order = h->lo_tasks.p;
-    lo.perm = h->perm.p;
-    lo.in = in;
-    lo.tmp = h->tmp.p;
-    lo.flags = h->flags.p;
     lo.status = h->status.p;
     lo.skip = skip;
     lo.counters = h->counters.p;
     lo.chunk = row_chunk();
-    lo.epoch = h->next_epoch(s);
+    lo.max_nrhs = nrhs;
+    lo.epoch = h->dev_epoch.p;
     CUDA_TRY(launch_row_sweep(lo, true, io, s));
     SnSweepArgs sn;
-    sn.n_units = (int)P.units.size();
-    sn.nslices = sn_slices(nrhs, !f32);
-    sn.nrhs = nrhs;
-    sn.units = h->units.p;
-    sn.contribs = h->contribs.p;
-    sn.sn_rows = h->sn_rows.p;
-    sn.panels = f32 ? (const void*)h->pan32.p : (const void*)h->pan64.p;
-    sn.perm = h->perm.p;
-    sn.tmp = h->tmp.p;
-    sn.uflags = h->uflags.p;
+    sn.sys0.units = h->units.p;
+    sn.sys0.contribs = h->contribs.p;
+    sn.sys0.sn_rows = h->sn_rows.p;
+    sn.sys0.panels = f32 ? (const void*)h->pan32.p : (const void*)h->pan64.p;
+    sn.sys0.dinv = f32 ? (const void*)h->dinv32.p : (const void*)h->dinv64.p;
+    sn.sys0.perm = h->perm.p;
+    sn.sys0.tmp = h->tmp.p;
+    sn.sys0.uflags = h->uflags.p;
+    sn.sys0.nrhs = nrhs;
+    sn.sys0.nslices = sn_slices(nrhs, !f32);
+    sn.nitems = (int)P.units.size() * sn.sys0.nslices;
     sn.status = h->status.p;
     sn.skip = skip;
-    sn.dinv = f32 ? (const void*)h->dinv32.p : (const void*)h->dinv64.p;
     sn.order = h->order_lo.p;
     sn.counters = h->counters.p + 2;
-    sn.epoch = h->next_epoch(s);
+    sn.epoch = h->dev_epoch.p;
     CUDA_TRY(launch_sn_sweep(sn, true, io, s));
-    sn.out = out;
+    sn.sys0.out = out;
     sn.order = h->order_up.p;
     sn.counters = h->counters.p + 4;
-    sn.epoch = h->next_epoch(s);
     CUDA_TRY(launch_sn_sweep(sn, false, io, s));
     RowSweepArgs pt = lo;  // top-row terms of the leaf rows: no waits
+    pt.sys0.rowptr = h->upt_rowptr.p;
+    pt.sys0.cols = h->upt_cols.p;
+    pt.sys0.vals = f32 ? (const void*)h->upt_v32.p : (const void*)h->upt_v64.p;
+    pt.sys0.in = nullptr;
+    pt.sys0.out = out;
+    pt.tasks = h->upt_tasks.p;
     pt.ntasks = (int)P.upt_tasks.size();
-    pt.rowptr = h->upt_rowptr.p;
-    pt.cols = h->upt_cols.p;
-    pt.vals = f32 ? (const void*)h->upt_v32.p : (const void*)h->upt_v64.p;
-    pt.order = h->upt_tasks.p;
-    pt.in = nullptr;
-    pt.out = out;
     pt.counters = h->counters.p + 8;
-    pt.epoch = h->next_epoch(s);
     CUDA_TRY(launch_row_sweep(pt, false, io, s));
-    RowSweepArgs up = lo;
+    RowSweepArgs up = pt;
+    up.sys0.rowptr = h->up_rowptr.p;
+    up.sys0.cols = h->up_cols.p;
+    up.sys0.vals = f32 ? (const void*)h->up_v32.p : (const void*)h->up_v64.p;
+    up.tasks = h->up_tasks.p;
     up.ntasks = (int)P.up_tasks.size();
-    up.rowptr = h->up_rowptr.p;
-    up.cols = h->up_cols.p;
-    up.vals = f32 ? (const void*)h->up_v32.p : (const void*)h->up_v64.p;
-    up.order = h->up_tasks.p;
-    up.in = nullptr;
-    up.out = out;
     up.counters = h->counters.p + 6;
-    up.epoch = h->next_epoch(s);
     CUDA_TRY(launch_row_sweep(up, false, io, s));
     return GBCHOL_OK;
 }

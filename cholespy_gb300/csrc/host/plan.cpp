@@ -166,6 +166,8 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
             const int32_t nlater = (U.sn_w - (U.pos0 + U.w) + kChunk - 1) / kChunk;
             for (int32_t c = 0; c < nlater; ++c) up[u] = std::max(up[u], up[u + 1 + c] + 1);
         }
+        P.unit_level_lo = lo;
+        P.unit_level_up = up;
         P.unit_order_lo.resize((size_t)nunits);
         P.unit_order_up.resize((size_t)nunits);
         for (int32_t u = 0; u < nunits; ++u) P.unit_order_lo[u] = P.unit_order_up[u] = u;
@@ -200,10 +202,27 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
         }
         P.max_row_len = std::max(P.max_row_len, P.lo_rowptr[i + 1] - P.lo_rowptr[i]);
     }
-    for (int32_t r : lower_order)
-        if (!P.row_top[r]) P.lo_tasks.push_back(r);
-    for (int32_t i = 0; i < n; ++i)
-        if (P.row_top[i]) P.lo_tasks.push_back(~i);
+    {
+        // leaf rows by their level in L (= etree height: their dependencies
+        // are all leaf rows), then the partial tasks of the top rows
+        std::vector<int32_t> parent((size_t)n, -1), height((size_t)n, 0);
+        for (int32_t j = 0; j < n; ++j)
+            if (F.colptr[j + 1] - F.colptr[j] > 1) parent[j] = F.rowidx[F.colptr[j] + 1];
+        for (int32_t j = 0; j < n; ++j)
+            if (parent[j] >= 0) height[parent[j]] = std::max(height[parent[j]], height[j] + 1);
+        int32_t maxh = 0;
+        for (int32_t r : lower_order)
+            if (!P.row_top[r]) {
+                P.lo_tasks.push_back(r);
+                P.lo_task_key.push_back(height[r]);
+                maxh = std::max(maxh, height[r]);
+            }
+        for (int32_t i = 0; i < n; ++i)
+            if (P.row_top[i]) {
+                P.lo_tasks.push_back(~i);
+                P.lo_task_key.push_back(maxh + 1);
+            }
+    }
     // upper leaf sweep: order by depth below the top region (number of leaf
     // ancestors), so every leaf subtree advances one level per step whatever
     // the depth of the top node it hangs from
@@ -223,8 +242,12 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
             if (!P.row_top[j]) cnt[(size_t)ldepth[j] + 1]++;
         for (int32_t d = 0; d <= maxd; ++d) cnt[(size_t)d + 1] += cnt[d];
         P.up_tasks.assign((size_t)cnt[(size_t)maxd + 1], 0);
+        P.up_task_key.assign(P.up_tasks.size(), 0);
         for (int32_t j = 0; j < n; ++j)
-            if (!P.row_top[j]) P.up_tasks[cnt[ldepth[j]]++] = j;
+            if (!P.row_top[j]) {
+                P.up_task_key[cnt[ldepth[j]]] = ldepth[j];
+                P.up_tasks[cnt[ldepth[j]]++] = j;
+            }
     }
     (void)upper_order;
     // upper sweep: split every leaf column of L into its top-row entries and

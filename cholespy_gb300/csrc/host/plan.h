@@ -54,12 +54,15 @@ struct SolvePlan {
     std::vector<double> dinv;             // per unit: inverse of the diagonal block, 32x32 column-major
     std::vector<int32_t> unit_order_lo;   // units sorted by lower-sweep dependency level
     std::vector<int32_t> unit_order_up;   // units sorted by upper-sweep dependency level
+    std::vector<int32_t> unit_level_lo, unit_level_up;  // those levels, per unit
     // leaf region, lower sweep: CSR over all rows. Leaf rows hold their full
     // row of L (diagonal last); top rows hold only their leaf-column entries.
     std::vector<int32_t> lo_rowptr, lo_cols;
     std::vector<double> lo_vals;
     std::vector<int32_t> lo_tasks;        // leaf rows in level order, then ~row for top rows
-    std::vector<int32_t> up_tasks;        // leaf rows in L^T level order
+    std::vector<int32_t> lo_task_key;     // dependency level of each lower task (for merging)
+    std::vector<int32_t> up_tasks;        // leaf rows by depth below the top region
+    std::vector<int32_t> up_task_key;     // that depth, per task
     // upper sweep, leaf rows: columns of L split into the top-row part
     // (final before the leaf sweep starts: one wait-free "partial" pass) and
     // the diagonal + leaf-row part (the chained row sweep)

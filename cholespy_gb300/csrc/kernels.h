@@ -21,29 +21,40 @@ cudaError_t launch_level_verify(bool lower, int n, const int* rowptr, const int*
                                 const int* cand, int* mismatch, cudaStream_t stream);
 
 // ---- row-wise sync-free sweeps (solve_rows.cu) ----------------------------
-// Lower sweep (L y = b[perm]):    out_tmp[row] = (in[perm[row]] - sum L[row,c] tmp[c]) / L[row,row]
+// Lower sweep (L y = b[perm]):    tmp[row] = (in[perm[row]] - sum L[row,c] tmp[c]) / L[row,row]
 // Upper sweep (L^T x = y):        tmp[row] = (tmp[row] - sum U[row,c] tmp[c]) / U[row,row]
 //                                 out[perm[row]] = tmp[row]   (or += in refinement mode)
 // Same arithmetic as solve_lower / solve_upper (kernels/kernels.cu:64-202).
-struct RowSweepArgs {
-    int n = 0;
-    int ntasks = 0;               // entries of `order`
-    int nrhs = 0;
+// A "partial" task (~row) has no diagonal: tmp[row] = (lower: in[perm[row]],
+// upper: tmp[row]) - sum, and publishes nothing.
+
+// One system of a row sweep (several for a batch).
+struct RowSys {
     const int* rowptr = nullptr;
     const int* cols = nullptr;
     const void* vals = nullptr;   // T
-    const int* order = nullptr;   // rows in dependency order; ~row = partial row: no
-                                  // diagonal, tmp[row] = (lower: in, upper: tmp) - sum
     const int* perm = nullptr;
     const void* in = nullptr;     // lower: right-hand side (TIn), read through perm
     void* tmp = nullptr;          // T, n x nrhs, permuted space
     void* out = nullptr;          // upper: solution (TOut), written through perm
-    int* flags = nullptr;
-    int epoch = 0;
+    int* flags = nullptr;         // row completion flags (epoch-valued)
+    int nrhs = 0;
+    int pad = 0;
+};
+
+struct RowSweepArgs {
+    RowSys sys0;                  // the system when task_sys is null
+    const RowSys* sys = nullptr;  // device table of systems (batched sweep)
+    const int* tasks = nullptr;   // task codes in dependency order: row, or ~row (partial)
+    const int* task_sys = nullptr;// system of each task (batched sweep), else null
+    int ntasks = 0;
+    int* epoch = nullptr;         // device sweep counter: read at start, +1 by the last warp out
     int* status = nullptr;
     const int* skip = nullptr;    // if non-null and *skip != 0 the sweep does nothing
     int* counters = nullptr;      // [ticket, exited warps], zero between launches
     int chunk = 1;                // consecutive tasks taken per ticket
+    int max_nrhs = 0;             // largest nrhs over the systems (kernel variant choice)
+    int batched_variant = 0;      // 1: one variant for every nrhs (per-system dispatch)
 };
 
 enum class SweepIO {

@@ -125,9 +125,16 @@ cudaError_t launch_residual(const ResidualArgs& a, int grid, cudaStream_t stream
 }
 
 int residual_grid(int n) {
+    static int cached_dev = -1, cached_sms = 0;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (dev == cached_dev) {
+        sms = cached_sms;
+    } else {
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cached_dev = dev;
+        cached_sms = sms;
+    }
     int need = (n + kWarps - 1) / kWarps;
     int g = sms * 8;
     return need < g ? (need > 0 ? need : 1) : g;

@@ -9,10 +9,16 @@
 //     nonzeros (coalesced index/value loads, warp-shuffle reduction); for more
 //     RHS the lanes split the RHS columns, so x loads are coalesced, and the
 //     row's (col, val) pairs are loaded 32 at a time and broadcast by shuffle;
-//   * persistent grid; warps take rows (in level order) by an atomic ticket,
-//     so a warp only waits on rows with smaller tickets, all taken by running
+//   * flags of a batch of entries are read together with relaxed loads and
+//     one acquire fence (no dependent acquire per nonzero);
+//   * persistent grid; warps take tasks (in level order) by an atomic ticket,
+//     so a warp only waits on tasks with smaller tickets, all taken by running
 //     warps (no deadlock); the last warp out resets the ticket;
-//   * flags carry an epoch, so no per-solve memset of the flag array;
+//   * one launch can sweep many systems (a batch): each task names its
+//     system, whose arrays come from a descriptor table;
+//   * flags carry an epoch kept in device memory (read at kernel start,
+//     advanced by the last warp out), so no per-solve memset of the flags
+//     and the sweeps can be captured in a CUDA graph and replayed;
 //   * bounded waits (device.cuh).
 #include <cuda_runtime.h>
 
@@ -35,129 +41,170 @@ struct IO {
 // Writes the solved value of (row, j) in permuted space and, for the upper
 // sweep, to the user array through perm.
 template <class io, bool LOWER>
-__device__ __forceinline__ void emit(const RowSweepArgs& a, int row, int prow, int j,
-                                     typename io::t v, bool partial) {
+__device__ __forceinline__ void emit(const RowSys& d, int row, int prow, int j, typename io::t v,
+                                     bool partial) {
     using T = typename io::t;
-    T* tmp = static_cast<T*>(a.tmp);
-    tmp[(size_t)row * a.nrhs + j] = v;
+    static_cast<T*>(d.tmp)[(size_t)row * d.nrhs + j] = v;
     if (!LOWER && !partial) {
         using TO = typename io::tout;
-        TO* out = static_cast<TO*>(a.out);
-        size_t o = (size_t)prow * a.nrhs + j;
+        TO* out = static_cast<TO*>(d.out);
+        const size_t o = (size_t)prow * d.nrhs + j;
         if (io::accum) out[o] += (TO)v;
         else out[o] = (TO)v;
     }
 }
 
 template <class io, bool LOWER>
-__device__ __forceinline__ typename io::t load_rhs(const RowSweepArgs& a, int row, int prow, int j) {
+__device__ __forceinline__ typename io::t load_rhs(const RowSys& d, int row, int prow, int j) {
     using T = typename io::t;
-    if (LOWER) {
-        const typename io::tin* in = static_cast<const typename io::tin*>(a.in);
-        return (T)in[(size_t)prow * a.nrhs + j];
-    }
-    return static_cast<const T*>(a.tmp)[(size_t)row * a.nrhs + j];
+    if (LOWER) return (T) static_cast<const typename io::tin*>(d.in)[(size_t)prow * d.nrhs + j];
+    return static_cast<const T*>(d.tmp)[(size_t)row * d.nrhs + j];
 }
 
 // Lanes split the nonzeros of the row; R >= nrhs accumulators per lane.
 template <class io, bool LOWER, int R>
-__global__ void __launch_bounds__(256) sweep_nnz_kernel(RowSweepArgs a) {
+__device__ __forceinline__ void row_nnz(const RowSys& d, int task, int epoch, int* status, int lane) {
     using T = typename io::t;
-    const int lane = threadIdx.x & 31;
-    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-    const T* __restrict__ vals = static_cast<const T*>(a.vals);
-    const T* tmp = static_cast<const T*>(a.tmp);
-    const int nrhs = a.nrhs;
-    if (a.skip && dev::ld_volatile(a.skip)) return;
-    for (;;) {
-        int t0 = 0;
-        if (lane == 0) t0 = atomicAdd(a.counters, 1) * a.chunk;
-        t0 = __shfl_sync(0xffffffffu, t0, 0);
-        if (t0 >= a.ntasks) break;
-        const int tend = min(a.ntasks, t0 + a.chunk);
-        for (int t = t0; t < tend; ++t) {
-        const int task = a.order[t];
-        const bool partial = task < 0;
-        const int row = partial ? ~task : task;
-        const int s = a.rowptr[row], e = a.rowptr[row + 1];
-        const int lo = (LOWER || partial) ? s : s + 1;
-        const int hi = (LOWER && !partial) ? e - 1 : e;
-        T acc[R];
+    const T* __restrict__ vals = static_cast<const T*>(d.vals);
+    const T* tmp = static_cast<const T*>(d.tmp);
+    const int nrhs = d.nrhs;
+    const bool partial = task < 0;
+    const int row = partial ? ~task : task;
+    const int s = d.rowptr[row], e = d.rowptr[row + 1];
+    const int lo = (LOWER || partial) ? s : s + 1;
+    const int hi = (LOWER && !partial) ? e - 1 : e;
+    T acc[R];
 #pragma unroll
-        for (int j = 0; j < R; ++j) acc[j] = T(0);
-        for (int base = lo; base < hi; base += 64) {
-            // two entries per lane: flags checked together, then one fence
-            int c[2];
-            T v[2];
+    for (int j = 0; j < R; ++j) acc[j] = T(0);
+    for (int base = lo; base < hi; base += 64) {
+        // two entries per lane: flags checked together, then one fence
+        int c[2];
+        T v[2];
 #pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                const int k = base + lane + 32 * u;
-                c[u] = k < hi ? a.cols[k] : -1;
-                v[u] = k < hi ? vals[k] : T(0);
-            }
-            int f[2];
-#pragma unroll
-            for (int u = 0; u < 2; ++u) f[u] = c[u] >= 0 ? dev::ld_volatile(a.flags + c[u]) : a.epoch;
-#pragma unroll
-            for (int u = 0; u < 2; ++u)
-                if (f[u] < a.epoch) dev::wait_geq(a.flags + c[u], a.epoch, a.status);
-            dev::fence_acquire();
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                if (c[u] < 0) continue;
-                const T* xc = tmp + (size_t)c[u] * nrhs;
-#pragma unroll
-                for (int j = 0; j < R; ++j)
-                    if (j < nrhs) acc[j] = fma(v[u], __ldcg(xc + j), acc[j]);
-            }
+        for (int u = 0; u < 2; ++u) {
+            const int k = base + lane + 32 * u;
+            c[u] = k < hi ? d.cols[k] : -1;
+            v[u] = k < hi ? vals[k] : T(0);
         }
-        T mine = T(0);
+        int f[2];
 #pragma unroll
-        for (int j = 0; j < R; ++j) {
-            T sj = dev::warp_sum(acc[j]);
-            if (j == lane) mine = sj;
-        }
-        const T diag = partial ? T(1) : vals[LOWER ? e - 1 : s];
-        const int prow = a.perm[row];
-        if (lane < nrhs) {
-            T v = load_rhs<io, LOWER>(a, row, prow, lane) - mine;
-            if (!partial) v = v / diag;
-            emit<io, LOWER>(a, row, prow, lane, v, partial);
-        }
-        __syncwarp();
-        // partial (top) rows publish nothing: their flags stay "always ready";
-        // the warp barrier orders the lanes' writes before lane 0's release
-        if (lane == 0 && !partial) {
-            __threadfence();
-            dev::st_release(a.flags + row, a.epoch);
-        }
+        for (int u = 0; u < 2; ++u) f[u] = c[u] >= 0 ? dev::ld_volatile(d.flags + c[u]) : epoch;
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+            if (f[u] < epoch) dev::wait_geq(d.flags + c[u], epoch, status);
+        dev::fence_acquire();
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (c[u] < 0) continue;
+            const T* xc = tmp + (size_t)c[u] * nrhs;
+#pragma unroll
+            for (int j = 0; j < R; ++j)
+                if (j < nrhs) acc[j] = fma(v[u], __ldcg(xc + j), acc[j]);
         }
     }
-    // the last warp out resets the ticket for the next launch
-    if (lane == 0) {
+    T mine = T(0);
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        T sj = dev::warp_sum(acc[j]);
+        if (j == lane) mine = sj;
+    }
+    const T diag = partial ? T(1) : vals[LOWER ? e - 1 : s];
+    const int prow = d.perm[row];
+    if (lane < nrhs) {
+        T v = load_rhs<io, LOWER>(d, row, prow, lane) - mine;
+        if (!partial) v = v / diag;
+        emit<io, LOWER>(d, row, prow, lane, v, partial);
+    }
+    // partial rows publish nothing; the warp barrier orders the lanes'
+    // writes before lane 0's release
+    __syncwarp();
+    if (lane == 0 && !partial) {
         __threadfence();
-        if (atomicAdd(a.counters + 1, 1) == nwarps - 1) {
-            a.counters[0] = 0;
-            a.counters[1] = 0;
-        }
+        dev::st_release(d.flags + row, epoch);
     }
 }
 
 // Lanes split the RHS columns: G lanes per group (32/G groups take
 // alternating nonzeros), Q RHS columns per lane (nrhs <= G*Q).
 template <class io, bool LOWER, int G, int Q>
-__global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
+__device__ __forceinline__ void row_rhs(const RowSys& d, int task, int epoch, int* status, int lane) {
     using T = typename io::t;
     constexpr int NG = 32 / G;
-    const int lane = threadIdx.x & 31;
     const int grp = lane / G, sub = lane % G;
-    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const T* __restrict__ vals = static_cast<const T*>(d.vals);
+    const T* tmp = static_cast<const T*>(d.tmp);
+    const int nrhs = d.nrhs;
+    const bool partial = task < 0;
+    const int row = partial ? ~task : task;
+    const int s = d.rowptr[row], e = d.rowptr[row + 1];
+    const int lo = (LOWER || partial) ? s : s + 1;
+    const int hi = (LOWER && !partial) ? e - 1 : e;
+    T acc[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) acc[q] = T(0);
+    for (int base = lo; base < hi; base += 32) {
+        const int k = base + lane;
+        const int mycol = k < hi ? d.cols[k] : 0;
+        const T myv = k < hi ? vals[k] : T(0);
+        // every lane waits for its own entry, then the warp consumes the 32
+        // entries without further waits (independent loads in flight)
+        if (k < hi && dev::ld_volatile(d.flags + mycol) < epoch)
+            dev::wait_geq(d.flags + mycol, epoch, status);
+        dev::fence_acquire();
+        __syncwarp();
+        const int cnt = min(32, hi - base);
+        const int steps = (cnt + NG - 1) / NG;
+#pragma unroll 8
+        for (int st = 0; st < steps; ++st) {
+            const int eidx = st * NG + grp;
+            const bool valid = eidx < cnt;
+            const int col = __shfl_sync(0xffffffffu, mycol, valid ? eidx : 0);
+            const T v = __shfl_sync(0xffffffffu, myv, valid ? eidx : 0);
+            if (!valid) continue;
+            const T* xc = tmp + (size_t)col * nrhs;
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const int j = sub + q * G;
+                if (j < nrhs) acc[q] = fma(v, __ldcg(xc + j), acc[q]);
+            }
+        }
+    }
+    if (NG > 1) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+#pragma unroll
+            for (int o = G; o < 32; o <<= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+    }
+    const T diag = partial ? T(1) : vals[LOWER ? e - 1 : s];
+    const int prow = d.perm[row];
+    if (grp == 0) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int j = sub + q * G;
+            if (j < nrhs) {
+                T v = load_rhs<io, LOWER>(d, row, prow, j) - acc[q];
+                if (!partial) v = v / diag;
+                emit<io, LOWER>(d, row, prow, j, v, partial);
+            }
+        }
+    }
+    __syncwarp();
+    if (lane == 0 && !partial) {
+        __threadfence();
+        dev::st_release(d.flags + row, epoch);
+    }
+}
+
+// MODE 1/2/4/8: nonzero-split with that many accumulators; 16: RHS-split
+// 16 lanes; 32/64/128: RHS-split 32 lanes x 1/2/4 columns; 0: per-system
+// choice (batched sweeps with mixed RHS counts).
+template <class io, bool LOWER, int MODE>
+__global__ void __launch_bounds__(256) row_sweep_kernel(RowSweepArgs a) {
+    const int lane = threadIdx.x & 31;
     const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-    const T* __restrict__ vals = static_cast<const T*>(a.vals);
-    const T* tmp = static_cast<const T*>(a.tmp);
-    const int nrhs = a.nrhs;
     if (a.skip && dev::ld_volatile(a.skip)) return;
+    // every warp reads the sweep's epoch before the last warp out bumps it
+    const int epoch = dev::ld_volatile(a.epoch);
     for (;;) {
         int t0 = 0;
         if (lane == 0) t0 = atomicAdd(a.counters, 1) * a.chunk;
@@ -165,76 +212,30 @@ __global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
         if (t0 >= a.ntasks) break;
         const int tend = min(a.ntasks, t0 + a.chunk);
         for (int t = t0; t < tend; ++t) {
-        const int task = a.order[t];
-        const bool partial = task < 0;
-        const int row = partial ? ~task : task;
-        const int s = a.rowptr[row], e = a.rowptr[row + 1];
-        const int lo = (LOWER || partial) ? s : s + 1;
-        const int hi = (LOWER && !partial) ? e - 1 : e;
-        T acc[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) acc[q] = T(0);
-        for (int base = lo; base < hi; base += 32) {
-            const int k = base + lane;
-            const int mycol = k < hi ? a.cols[k] : 0;
-            const T myv = k < hi ? vals[k] : T(0);
-            // every lane waits for its own entry, then the warp consumes the
-            // 32 entries without further waits (independent loads in flight)
-            if (k < hi && dev::ld_volatile(a.flags + mycol) < a.epoch)
-                dev::wait_geq(a.flags + mycol, a.epoch, a.status);
-            dev::fence_acquire();
-            __syncwarp();
-            const int cnt = min(32, hi - base);
-            const int steps = (cnt + NG - 1) / NG;
-#pragma unroll 8
-            for (int st = 0; st < steps; ++st) {
-                const int eidx = st * NG + grp;
-                const bool valid = eidx < cnt;
-                const int col = __shfl_sync(0xffffffffu, mycol, valid ? eidx : 0);
-                const T v = __shfl_sync(0xffffffffu, myv, valid ? eidx : 0);
-                if (!valid) continue;
-                const T* xc = tmp + (size_t)col * nrhs;
-#pragma unroll
-                for (int q = 0; q < Q; ++q) {
-                    const int j = sub + q * G;
-                    if (j < nrhs) acc[q] = fma(v, __ldcg(xc + j), acc[q]);
-                }
+            const int task = a.tasks[t];
+            const RowSys d = a.task_sys ? a.sys[a.task_sys[t]] : a.sys0;
+            if (MODE == 1) row_nnz<io, LOWER, 1>(d, task, epoch, a.status, lane);
+            else if (MODE == 2) row_nnz<io, LOWER, 2>(d, task, epoch, a.status, lane);
+            else if (MODE == 4) row_nnz<io, LOWER, 4>(d, task, epoch, a.status, lane);
+            else if (MODE == 8) row_nnz<io, LOWER, 8>(d, task, epoch, a.status, lane);
+            else if (MODE == 16) row_rhs<io, LOWER, 16, 1>(d, task, epoch, a.status, lane);
+            else if (MODE == 32) row_rhs<io, LOWER, 32, 1>(d, task, epoch, a.status, lane);
+            else if (MODE == 64) row_rhs<io, LOWER, 32, 2>(d, task, epoch, a.status, lane);
+            else if (MODE == 128) row_rhs<io, LOWER, 32, 4>(d, task, epoch, a.status, lane);
+            else {
+                if (d.nrhs <= 8) row_nnz<io, LOWER, 8>(d, task, epoch, a.status, lane);
+                else row_rhs<io, LOWER, 32, 4>(d, task, epoch, a.status, lane);
             }
-        }
-        if (NG > 1) {
-#pragma unroll
-            for (int q = 0; q < Q; ++q)
-#pragma unroll
-                for (int o = G; o < 32; o <<= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
-        }
-        const T diag = partial ? T(1) : vals[LOWER ? e - 1 : s];
-        const int prow = a.perm[row];
-        if (grp == 0) {
-#pragma unroll
-            for (int q = 0; q < Q; ++q) {
-                const int j = sub + q * G;
-                if (j < nrhs) {
-                    T v = load_rhs<io, LOWER>(a, row, prow, j) - acc[q];
-                    if (!partial) v = v / diag;
-                    emit<io, LOWER>(a, row, prow, j, v, partial);
-                }
-            }
-        }
-        __syncwarp();
-        // partial (top) rows publish nothing: their flags stay "always ready";
-        // the warp barrier orders the lanes' writes before lane 0's release
-        if (lane == 0 && !partial) {
-            __threadfence();
-            dev::st_release(a.flags + row, a.epoch);
-        }
         }
     }
-    // the last warp out resets the ticket for the next launch
+    // the last warp out resets the ticket and advances the epoch for the
+    // next launch (the launch boundary orders these writes)
     if (lane == 0) {
         __threadfence();
         if (atomicAdd(a.counters + 1, 1) == nwarps - 1) {
             a.counters[0] = 0;
             a.counters[1] = 0;
+            *a.epoch = epoch + 1;
         }
     }
 }
@@ -242,15 +243,16 @@ __global__ void __launch_bounds__(256) sweep_rhs_kernel(RowSweepArgs a) {
 template <class io, bool LOWER>
 cudaError_t launch_io(const RowSweepArgs& a, cudaStream_t stream) {
     const void* fn;
-    const int r = a.nrhs;
-    if (r <= 1) fn = (const void*)sweep_nnz_kernel<io, LOWER, 1>;
-    else if (r <= 2) fn = (const void*)sweep_nnz_kernel<io, LOWER, 2>;
-    else if (r <= 4) fn = (const void*)sweep_nnz_kernel<io, LOWER, 4>;
-    else if (r <= 8) fn = (const void*)sweep_nnz_kernel<io, LOWER, 8>;
-    else if (r <= 16) fn = (const void*)sweep_rhs_kernel<io, LOWER, 16, 1>;
-    else if (r <= 32) fn = (const void*)sweep_rhs_kernel<io, LOWER, 32, 1>;
-    else if (r <= 64) fn = (const void*)sweep_rhs_kernel<io, LOWER, 32, 2>;
-    else fn = (const void*)sweep_rhs_kernel<io, LOWER, 32, 4>;
+    const int r = a.max_nrhs;
+    if (a.batched_variant) fn = (const void*)row_sweep_kernel<io, LOWER, 0>;
+    else if (r <= 1) fn = (const void*)row_sweep_kernel<io, LOWER, 1>;
+    else if (r <= 2) fn = (const void*)row_sweep_kernel<io, LOWER, 2>;
+    else if (r <= 4) fn = (const void*)row_sweep_kernel<io, LOWER, 4>;
+    else if (r <= 8) fn = (const void*)row_sweep_kernel<io, LOWER, 8>;
+    else if (r <= 16) fn = (const void*)row_sweep_kernel<io, LOWER, 16>;
+    else if (r <= 32) fn = (const void*)row_sweep_kernel<io, LOWER, 32>;
+    else if (r <= 64) fn = (const void*)row_sweep_kernel<io, LOWER, 64>;
+    else fn = (const void*)row_sweep_kernel<io, LOWER, 128>;
     int grid = 0;
     cudaError_t e = coop_grid(fn, 256, 0, &grid);  // resident blocks: a persistent grid
     if (e != cudaSuccess) return e;

@@ -75,29 +75,46 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
     SnSmem<T, KW>& sm = *reinterpret_cast<SnSmem<T, KW>*>(smem_raw);
     if (a.skip && dev::ld_volatile(a.skip)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const T* __restrict__ panels = static_cast<const T*>(a.panels);
-    T* tmp = static_cast<T*>(a.tmp);
-    const int nrhs = a.nrhs;
-    const int nitems = a.n_units * a.nslices;
+    const int nitems = a.nitems;
+    // every CTA reads the sweep's epoch before the last CTA out bumps it
+    const int epoch = dev::ld_volatile(a.epoch);
     T (*xs)[KW + 1] = sm.xs[warp];
     if (LOWER) sm.inv[warp][lane] = -1;
-    __shared__ int ticket;
+    __shared__ int ticket, s_uidx, s_slice;
+    __shared__ SnSys dsm;
     for (;;) {
-        if (tid == 0) ticket = atomicAdd(a.counters, 1);
+        if (tid == 0) {
+            const int it = atomicAdd(a.counters, 1);
+            ticket = it;
+            if (it < nitems) {
+                if (a.item_sys) {
+                    dsm = a.sys[a.item_sys[it]];
+                    const int code = a.item_code[it];
+                    s_uidx = code >> 3;
+                    s_slice = code & 7;
+                } else {
+                    dsm = a.sys0;
+                    s_uidx = a.order[it / a.sys0.nslices];
+                    s_slice = it % a.sys0.nslices;
+                }
+            }
+        }
         __syncthreads();
-        const int item = ticket;
-        __syncthreads();
-        if (item >= nitems) break;
-        const int uidx = a.order[item / a.nslices];
-        const int slice = item % a.nslices;
+        // thread 0 rewrites these only after the end-of-item barrier
+        if (ticket >= nitems) break;
+        const SnSys& d = dsm;
+        const int uidx = s_uidx, slice = s_slice;
+        const T* __restrict__ panels = static_cast<const T*>(d.panels);
+        T* tmp = static_cast<T*>(d.tmp);
+        const int nrhs = d.nrhs;
         const int k0 = slice * KW;
         const int kw = min(KW, nrhs - k0);
-        const SnUnit U = a.units[uidx];
+        const SnUnit U = d.units[uidx];
         const int w = U.w;
         // off the dependency chain: the unit's current right-hand side and
         // its inverse diagonal block go to shared memory first
         {
-            const T* __restrict__ dinv = static_cast<const T*>(a.dinv) + (size_t)uidx * kW * kW;
+            const T* __restrict__ dinv = static_cast<const T*>(d.dinv) + (size_t)uidx * kW * kW;
             for (int idx = tid; idx < kW * kW; idx += kT) sm.d[idx & 31][idx >> 5] = dinv[idx];
             for (int idx = tid; idx < kW * KW; idx += kT) {
                 const int i = idx / KW, k = idx % KW;
@@ -111,8 +128,8 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
         if (LOWER) {
             const int nb = U.contrib_end - U.contrib_begin;
             for (int b = warp; b < nb; b += kWarps) {
-                const SnContrib C = a.contribs[U.contrib_begin + b];
-                if (lane < C.nr) sm.inv[warp][a.sn_rows[C.rows_off + lane] - U.c0] = lane;
+                const SnContrib C = d.contribs[U.contrib_begin + b];
+                if (lane < C.nr) sm.inv[warp][d.sn_rows[C.rows_off + lane] - U.c0] = lane;
                 __syncwarp();
                 const int src = sm.inv[warp][lane];
                 sm.inv[warp][lane] = -1;
@@ -122,7 +139,7 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
 #pragma unroll
                 for (int j = 0; j < kW; ++j)
                     lv[j] = (src >= 0 && j < C.w) ? __ldg(Lp + (size_t)j * C.ld) : T(0);
-                warp_wait(a.uflags + (size_t)C.src_unit * a.nslices + slice, a.epoch, a.status, lane);
+                warp_wait(d.uflags + (size_t)C.src_unit * d.nslices + slice, epoch, a.status, lane);
                 T xv[KW];
 #pragma unroll
                 for (int u = 0; u < KW; ++u) {
@@ -166,8 +183,8 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
                 const T* Lp = panels + U.panel_col_off + p0 + (size_t)lane * U.ld;
 #pragma unroll
                 for (int i = 0; i < kW; ++i) lv[i] = (lane < w && i < nr) ? __ldg(Lp + i) : T(0);
-                const int myrow = lane < nr ? a.sn_rows[U.rows_off + p0 + lane] : 0;
-                if (dep >= 0) warp_wait(a.uflags + (size_t)dep * a.nslices + slice, a.epoch, a.status, lane);
+                const int myrow = lane < nr ? d.sn_rows[U.rows_off + p0 + lane] : 0;
+                if (dep >= 0) warp_wait(d.uflags + (size_t)dep * d.nslices + slice, epoch, a.status, lane);
                 T xv[KW];
 #pragma unroll
                 for (int u = 0; u < KW; ++u) {
@@ -215,8 +232,8 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
                 tmp[(size_t)(U.c0 + lane) * nrhs + k0 + k] = v;
                 if (!LOWER) {
                     using TO = typename io::tout;
-                    TO* out = static_cast<TO*>(a.out);
-                    const size_t oo = (size_t)a.perm[U.c0 + lane] * nrhs + k0 + k;
+                    TO* out = static_cast<TO*>(d.out);
+                    const size_t oo = (size_t)d.perm[U.c0 + lane] * nrhs + k0 + k;
                     if (io::accum) out[oo] += (TO)v;
                     else out[oo] = (TO)v;
                 }
@@ -226,15 +243,17 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
         __syncthreads();
         if (tid == 0) {
             __threadfence();
-            dev::st_release(a.uflags + (size_t)uidx * a.nslices + slice, a.epoch);
+            dev::st_release(d.uflags + (size_t)uidx * d.nslices + slice, epoch);
         }
     }
-    // the last CTA out resets the ticket for the next launch
+    // the last CTA out resets the ticket and advances the epoch for the next
+    // launch (the launch boundary orders these writes)
     if (tid == 0) {
         __threadfence();
         if (atomicAdd(a.counters + 1, 1) == (int)gridDim.x - 1) {
             a.counters[0] = 0;
             a.counters[1] = 0;
+            *a.epoch = epoch + 1;
         }
     }
 }
@@ -244,14 +263,10 @@ cudaError_t launch_sn_kw(const SnSweepArgs& a, cudaStream_t stream) {
     using T = typename io::t;
     const void* fn = (const void*)sn_sweep_kernel<io, LOWER, KW>;
     const size_t smem = sizeof(SnSmem<T, KW>);
-    // the attribute belongs to the current device's context: set it per launch
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     int grid = 0;
-    e = coop_grid(fn, kT, smem, &grid);  // resident CTAs: a persistent grid
+    cudaError_t e = coop_grid(fn, kT, smem, &grid);  // resident CTAs: a persistent grid
     if (e != cudaSuccess) return e;
-    const int items = a.n_units * a.nslices;
-    if (grid > items) grid = items;
+    if (grid > a.nitems) grid = a.nitems;
     sn_sweep_kernel<io, LOWER, KW><<<grid, kT, smem, stream>>>(a);
     return cudaGetLastError();
 }
@@ -259,7 +274,7 @@ cudaError_t launch_sn_kw(const SnSweepArgs& a, cudaStream_t stream) {
 template <class io, bool LOWER>
 cudaError_t launch_sn_io(const SnSweepArgs& a, cudaStream_t stream) {
     constexpr int wide = sizeof(typename io::t) == 8 ? 16 : 32;
-    if (a.nrhs <= 8) return launch_sn_kw<io, LOWER, 8>(a, stream);
+    if (!a.wide && a.sys0.nrhs <= 8) return launch_sn_kw<io, LOWER, 8>(a, stream);
     return launch_sn_kw<io, LOWER, wide>(a, stream);
 }
 
@@ -271,7 +286,7 @@ int sn_slices(int nrhs, bool f64) {
 }
 
 cudaError_t launch_sn_sweep(const SnSweepArgs& a, bool lower, SweepIO io, cudaStream_t stream) {
-    if (a.n_units == 0) return cudaSuccess;
+    if (a.nitems == 0) return cudaSuccess;
     switch (io) {
         case SweepIO::F32:
             return lower ? launch_sn_io<SnIO<float, float, false>, true>(a, stream)

@@ -7,24 +7,33 @@
 
 namespace gbchol {
 
-struct SnSweepArgs {
-    int n_units = 0;
-    int nslices = 1;          // RHS slices (see sn_slices)
-    int nrhs = 0;
+// One system of a supernodal sweep (several for a batch).
+struct SnSys {
     const SnUnit* units = nullptr;
     const SnContrib* contribs = nullptr;
     const int32_t* sn_rows = nullptr;
     const void* panels = nullptr;   // T
+    const void* dinv = nullptr;     // T, per unit 32x32 inverse diagonal block (column-major)
     const int32_t* perm = nullptr;
     void* tmp = nullptr;            // T, n x nrhs, permuted space
     void* out = nullptr;            // upper: solution through perm (TOut)
-    const int32_t* order = nullptr; // units in dependency-level order for this sweep
-    const void* dinv = nullptr;     // T, per unit 32x32 inverse diagonal block (column-major)
-    int* counters = nullptr;        // [ticket, exited CTAs], zero between launches
     int* uflags = nullptr;          // n_units * nslices completion flags
-    int epoch = 0;
+    int nrhs = 0;
+    int nslices = 1;                // RHS slices (see sn_slices)
+};
+
+struct SnSweepArgs {
+    SnSys sys0;                     // the system when item_sys is null
+    const SnSys* sys = nullptr;     // device table of systems (batched sweep)
+    const int32_t* order = nullptr; // single system: units in dependency-level order
+    const int32_t* item_sys = nullptr;   // batched: system of each item
+    const int32_t* item_code = nullptr;  // batched: (unit << 3) | RHS slice of each item
+    int nitems = 0;
+    int wide = 0;                   // 1: use the wide-RHS variant for every system (batched)
+    int* epoch = nullptr;           // device sweep counter: read at start, +1 by the last CTA out
     int* status = nullptr;
     const int* skip = nullptr;
+    int* counters = nullptr;        // [ticket, exited CTAs], zero between launches
 };
 
 // RHS slices of one sweep: 1 for <= 8 RHS, else 32-wide (FP32) or 16-wide (FP64).

@@ -193,6 +193,33 @@ int gbchol_check(gbchol_handle h);
  */
 int gbchol_reserve(gbchol_handle h, int32_t nrhs);
 
+/*
+ * Batched solves: `count` solvers (same device) solved together, system s
+ * with nrhs[s] right-hand sides, by one persistent launch per sweep phase.
+ * precision 0 = FP32, 1 = FP64 (every solver must keep that factor). The
+ * solvers must outlive the batch. The batch owns its scratch, so a bound
+ * batch solve allocates nothing and synchronises nothing: it can be
+ * captured in a CUDA graph and replayed. No counterpart in the reference.
+ */
+typedef struct gbchol_batch_s* gbchol_batch;
+
+int gbchol_batch_create(int32_t count, const gbchol_handle* solvers, const int32_t* nrhs,
+                        int32_t precision, gbchol_batch* out);
+
+/* Bind the device arrays of every system: bs[s], xs[s] are (n_s, nrhs[s]). */
+int gbchol_batch_set_io(gbchol_batch b, const void* const* bs, void* const* xs);
+
+/* x_s = A_s^{-1} b_s for every system, asynchronously on `stream`. */
+int gbchol_batch_solve(gbchol_batch b, void* stream);
+
+/* Kernel launches per batched solve, total nnz(L) and rows of the batch. */
+int gbchol_batch_info(gbchol_batch b, int32_t* launches, int64_t* nnz_l, int64_t* rows);
+
+/* Synchronise `stream` and report an expired device-side wait (GBCHOL_ETIMEOUT). */
+int gbchol_batch_check(gbchol_batch b, void* stream);
+
+int gbchol_batch_destroy(gbchol_batch b);
+
 #ifdef __cplusplus
 }
 #endif
