@@ -7,12 +7,13 @@
 //     blocks over n rows, D2H of the levels, host counting sort :349-367);
 //   * solve: src/cholesky_solver.cpp:378-432 (memset of the row flags and
 //     the block ticket, n blocks of 128 threads, lower then upper sweep).
-// It is used to pin the product's level analysis against the reference's own
+// It is used to compare the product's level analysis with the reference's own
 // analysis kernels and to time the reference's GPU solve on the same factor.
 // Inputs are validated first: the reference kernels wait without bound, so
 // they only ever see well-formed factors here.
 #include <cuda.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstdint>
 #include <cstring>
@@ -33,9 +34,20 @@ bool ck(CUresult r, const char* what) {
 
 struct Tri {
     CUdeviceptr rows = 0, cols = 0, data = 0, levels = 0;
-    std::vector<int32_t> lev, order;
-    int32_t max_lvl = 0;
+    std::vector<int32_t> lev, order;       // as produced by the reference's analysis kernel
+    std::vector<int32_t> lev_seq, order_seq;  // the sequential definition of the same quantity
+    int32_t max_lvl = 0, max_lvl_seq = 0;
 };
+
+// Counting sort of rows by level, stable in row id (src/cholesky_solver.cpp:349-367).
+void sort_levels(const std::vector<int32_t>& lev, int32_t max_lvl, std::vector<int32_t>& order) {
+    const int32_t n = (int32_t)lev.size();
+    std::vector<int32_t> ptr(max_lvl + 2, 0);
+    for (int32_t i = 0; i < n; ++i) ptr[1 + lev[i]]++;
+    for (int32_t l = 0; l <= max_lvl; ++l) ptr[l + 1] += ptr[l];
+    order.resize(n);
+    for (int32_t i = 0; i < n; ++i) order[ptr[lev[i]]++] = i;
+}
 
 struct RefGpu {
     CUcontext ctx = nullptr;
@@ -84,13 +96,35 @@ bool analyze(RefGpu* g, Tri& t, bool lower) {
     t.lev.resize(n);
     ck(cuMemcpyDtoH(t.lev.data(), level_ind, n * sizeof(int)), "DtoH");
     ck(cuMemcpyDtoH(&t.max_lvl, max_lvl, sizeof(int)), "DtoH");
-    // counting sort by level, stable in row id (:349-367)
-    std::vector<int32_t> ptr(t.max_lvl + 2, 0);
-    for (int32_t i = 0; i < n; ++i) ptr[1 + t.lev[i]]++;
-    for (int32_t l = 0; l <= t.max_lvl; ++l) ptr[l + 1] += ptr[l];
-    t.order.resize(n);
-    for (int32_t i = 0; i < n; ++i) t.order[ptr[t.lev[i]]++] = i;
-    bool ok = upload(&t.levels, t.order.data(), n);
+    sort_levels(t.lev, t.max_lvl, t.order);
+    // The reference's analysis kernels store row_levels[row] and then
+    // analyzed_rows[row] with no fence between them (kernels/kernels.cu:
+    // 28-29, 55-56), so a waiting row can observe the flag before the level
+    // and read a stale 0. On GB300 this was observed to give some rows too
+    // low a level. A too-low level can put a row ahead of its dependency in
+    // the solve's ticket order, and the solve kernels wait without bound, so
+    // the solves below are driven by the sequential definition of the same
+    // levels instead (levels[] of the correct analysis; no change to the
+    // kernels). The kernel's own output is kept for comparison.
+    {
+        std::vector<int32_t> rp(n + 1), ci;
+        ck(cuMemcpyDtoH(rp.data(), t.rows, (n + 1) * sizeof(int)), "DtoH");
+        ci.resize(rp[n]);
+        if (rp[n]) ck(cuMemcpyDtoH(ci.data(), t.cols, rp[n] * sizeof(int)), "DtoH");
+        t.lev_seq.assign(n, 0);
+        t.max_lvl_seq = 0;
+        for (int32_t k = 0; k < n; ++k) {
+            const int32_t row = lower ? k : n - 1 - k;
+            const int32_t s0 = rp[row], e0 = rp[row + 1];
+            int32_t l = 0;
+            for (int32_t q = lower ? s0 : s0 + 1; q < (lower ? e0 - 1 : e0); ++q)
+                l = std::max(l, t.lev_seq[ci[q]] + 1);
+            t.lev_seq[row] = l;
+            t.max_lvl_seq = std::max(t.max_lvl_seq, l);
+        }
+        sort_levels(t.lev_seq, t.max_lvl_seq, t.order_seq);
+    }
+    bool ok = upload(&t.levels, t.order_seq.data(), n);
     cuMemFree(level_ind);
     cuMemFree(max_lvl);
     return ok;
@@ -198,12 +232,16 @@ int refgpu_create(const char* cubin, int32_t n, const int32_t* perm, const int32
     return 0;
 }
 
-int refgpu_levels(void* p, int32_t lower, int32_t* row_levels, int32_t* order, int32_t* max_lvl) {
+// which = 0: the reference analysis kernel's output; 1: sequential definition.
+int refgpu_levels(void* p, int32_t lower, int32_t which, int32_t* row_levels, int32_t* order,
+                  int32_t* max_lvl) {
     RefGpu* g = static_cast<RefGpu*>(p);
     const Tri& t = lower ? g->lo : g->up;
-    std::memcpy(row_levels, t.lev.data(), sizeof(int32_t) * g->n);
-    std::memcpy(order, t.order.data(), sizeof(int32_t) * g->n);
-    *max_lvl = t.max_lvl;
+    const std::vector<int32_t>& lev = which ? t.lev_seq : t.lev;
+    const std::vector<int32_t>& ord = which ? t.order_seq : t.order;
+    std::memcpy(row_levels, lev.data(), sizeof(int32_t) * g->n);
+    std::memcpy(order, ord.data(), sizeof(int32_t) * g->n);
+    *max_lvl = which ? t.max_lvl_seq : t.max_lvl;
     return 0;
 }
 

@@ -25,7 +25,7 @@ def lib():
         L.refgpu_create.restype = C.c_int
         L.refgpu_create.argtypes = [C.c_char_p, I32, P, P, P, P, I32, C.POINTER(P)]
         L.refgpu_levels.restype = C.c_int
-        L.refgpu_levels.argtypes = [P, I32, P, P, C.POINTER(I32)]
+        L.refgpu_levels.argtypes = [P, I32, I32, P, P, C.POINTER(I32)]
         L.refgpu_solve.restype = C.c_int
         L.refgpu_solve.argtypes = [P, I32, U64, U64, U64]
         L.refgpu_destroy.restype = None
@@ -52,11 +52,14 @@ class RefGpuSolver:
             raise RuntimeError(L.refgpu_last_error().decode())
         self._h = h
 
-    def levels(self, lower=True):
+    def levels(self, lower=True, kernel=True):
+        """(row_levels, order, max_lvl): the reference analysis kernel's output
+        (kernel=True) or the sequential definition it computes (kernel=False)."""
         lev = np.zeros(self.n, np.int32)
         order = np.zeros(self.n, np.int32)
         mx = C.c_int32()
-        lib().refgpu_levels(self._h, 1 if lower else 0, lev.ctypes.data, order.ctypes.data, C.byref(mx))
+        lib().refgpu_levels(self._h, 1 if lower else 0, 0 if kernel else 1, lev.ctypes.data,
+                            order.ctypes.data, C.byref(mx))
         return lev, order, mx.value
 
     def solve(self, b, x, stream=0):
