@@ -72,6 +72,7 @@ def _declare(lib):
         "gbchol_batch_info": (C.c_int, [P, C.POINTER(I32), C.POINTER(I64), C.POINTER(I64)]),
         "gbchol_batch_check": (C.c_int, [P, P]),
         "gbchol_batch_destroy": (C.c_int, [P]),
+        "gbchol_grad_values": (C.c_int, [I32, I64, I32, P, P, P, P, P, I32, I32, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

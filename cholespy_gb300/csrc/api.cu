@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "grad.h"
 #include "solver_impl.h"
 
 using namespace gbchol;
@@ -582,6 +583,27 @@ int gbchol_solve_refined(gbchol_handle h, int32_t nrhs, const double* b, double*
         stats->converged = hs.converged;
         stats->max_rel_residual = hs.max_rel;
     }
+    return GBCHOL_OK;
+}
+
+int gbchol_grad_values(int32_t precision, int64_t nnz, int32_t nrhs, const int32_t* rows,
+                       const int32_t* cols, const void* grad_b, const void* x, void* grad_vals,
+                       int32_t out_precision, int32_t symmetric, void* stream) {
+    if (nnz < 0 || nrhs < 1 || nrhs > GBCHOL_MAX_RHS) return fail(GBCHOL_EINVAL, "Invalid sizes.");
+    if ((precision != 0 && precision != 1) || (out_precision != 0 && out_precision != 1))
+        return fail(GBCHOL_EINVAL, "precision must be 0 or 1.");
+    if (nnz > 0 && (!rows || !cols || !grad_b || !x || !grad_vals))
+        return fail(GBCHOL_EINVAL, "Null array.");
+    GradArgs a;
+    a.nnz = nnz;
+    a.nrhs = nrhs;
+    a.symmetric = symmetric ? 1 : 0;
+    a.rows = rows;
+    a.cols = cols;
+    a.grad_b = grad_b;
+    a.x = x;
+    a.grad_vals = grad_vals;
+    CUDA_TRY(launch_grad_values(a, precision == 0, out_precision == 0, static_cast<cudaStream_t>(stream)));
     return GBCHOL_OK;
 }
 

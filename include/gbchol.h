@@ -142,6 +142,22 @@ typedef struct {
 int gbchol_solve_refined(gbchol_handle h, int32_t nrhs, const double* b, double* x, double tol,
                          int32_t max_iter, void* stream, gbchol_refine_stats* stats);
 
+/*
+ * Gradient of a loss with respect to the stored entries of A, given the
+ * backward-solve result grad_b = A^{-1} grad_x and the solution x (device
+ * arrays (n, nrhs), FP32 if precision = 0 else FP64). rows/cols: device
+ * arrays of the nnz entries' (row, col) in the original ordering. Writes
+ * grad_vals (FP32 if out_precision = 0 else FP64), one value per entry:
+ *   symmetric = 1: dL/dA of the symmetric matrix, -1/2 (gb_r x_c + gb_c x_r)
+ *                  on off-diagonal entries, -gb_r x_r on the diagonal;
+ *   symmetric = 0: the exact gradient of the lower-triangle-only forward
+ *                  (entries above the diagonal get 0, below -(gb_r x_c + gb_c x_r)).
+ * Sums over the RHS columns. No counterpart in the reference.
+ */
+int gbchol_grad_values(int32_t precision, int64_t nnz, int32_t nrhs, const int32_t* rows,
+                       const int32_t* cols, const void* grad_b, const void* x, void* grad_vals,
+                       int32_t out_precision, int32_t symmetric, void* stream);
+
 /* Solver facts. */
 typedef struct {
     int32_t n;
