@@ -102,7 +102,19 @@ __global__ void __launch_bounds__(256) level_verify_kernel(int n, const int* __r
     }
 }
 
+// One warp waits (bounded) on a flag that nothing sets: exercises the
+// timeout path of every sync-free kernel without hanging anything.
+__global__ void selftest_wait_kernel(const int* flag, int* status, unsigned long long limit_ns) {
+    if (threadIdx.x == 0) dev::wait_geq(flag, 1, status, limit_ns);
+}
+
 }  // namespace
+
+cudaError_t launch_selftest_wait(const int* flag, int* status, unsigned long long limit_ns,
+                                 cudaStream_t stream) {
+    selftest_wait_kernel<<<1, 32, 0, stream>>>(flag, status, limit_ns);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_level_verify(bool lower, int n, const int* rowptr, const int* cols,
                                 const int* cand, int* mismatch, cudaStream_t stream) {

@@ -298,12 +298,15 @@ namespace {
 // One full solve: leaf rows (lower) -> top units (lower) -> top units
 // (upper) -> leaf rows (upper). `in` is read through perm by the lower leaf
 // kernel; `out` is written through perm by both upper kernels.
-int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in, void* out,
-               const int* skip, cudaStream_t s) {
+}  // namespace
+
+// One full solve with the permuted-space work array `work` (n x nrhs of T).
+int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in,
+                            void* out, const int* skip, void* work, cudaStream_t s) {
     const SolvePlan& P = h->plan;
     RowSys rs;
     rs.perm = h->perm.p;
-    rs.tmp = h->tmp.p;
+    rs.tmp = work;
     rs.flags = h->flags.p;
     rs.nrhs = nrhs;
     RowSweepArgs lo;
@@ -328,7 +331,7 @@ int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in,
     sn.sys0.panels = f32 ? (const void*)h->pan32.p : (const void*)h->pan64.p;
     sn.sys0.dinv = f32 ? (const void*)h->dinv32.p : (const void*)h->dinv64.p;
     sn.sys0.perm = h->perm.p;
-    sn.sys0.tmp = h->tmp.p;
+    sn.sys0.tmp = work;
     sn.sys0.uflags = h->uflags.p;
     sn.sys0.nrhs = nrhs;
     sn.sys0.nslices = sn_slices(nrhs, !f32);
@@ -362,6 +365,13 @@ int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in,
     up.counters = h->counters.p + 6;
     CUDA_TRY(launch_row_sweep(up, false, io, s));
     return GBCHOL_OK;
+}
+
+namespace {
+
+int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in, void* out,
+               const int* skip, cudaStream_t s) {
+    return run_sweeps_with(h, f32, io, nrhs, in, out, skip, h->tmp.p, s);
 }
 
 // Kernel launches of one run_sweeps call.
@@ -604,6 +614,17 @@ int gbchol_grad_values(int32_t precision, int64_t nnz, int32_t nrhs, const int32
     a.x = x;
     a.grad_vals = grad_vals;
     CUDA_TRY(launch_grad_values(a, precision == 0, out_precision == 0, static_cast<cudaStream_t>(stream)));
+    return GBCHOL_OK;
+}
+
+int gbchol_selftest_wait(int32_t wait_us, int32_t* status_out) {
+    if (wait_us < 1 || wait_us > 2000000 || !status_out) return fail(GBCHOL_EINVAL, "Invalid arguments.");
+    DevBuf<int32_t> buf;
+    CUDA_TRY(buf.alloc(2));
+    CUDA_TRY(cudaMemset(buf.p, 0, 2 * sizeof(int32_t)));
+    CUDA_TRY(launch_selftest_wait(buf.p, buf.p + 1, (unsigned long long)wait_us * 1000ull, nullptr));
+    CUDA_TRY(cudaDeviceSynchronize());
+    CUDA_TRY(cudaMemcpy(status_out, buf.p + 1, sizeof(int32_t), cudaMemcpyDeviceToHost));
     return GBCHOL_OK;
 }
 

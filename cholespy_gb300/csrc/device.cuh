@@ -35,7 +35,8 @@ __device__ __forceinline__ unsigned long long globaltimer() {
 
 // Waits until *flag >= target. Returns false (after recording a timeout in
 // *status if this wait expired) when the wait is abandoned.
-__device__ __forceinline__ bool wait_geq(const int* flag, int target, int* status) {
+__device__ __forceinline__ bool wait_geq(const int* flag, int target, int* status,
+                                         unsigned long long limit_ns = kWaitLimitNs) {
     if (ld_acquire(flag) >= target) return true;
     unsigned long long t0 = 0;
     for (unsigned it = 1;; ++it) {
@@ -45,7 +46,7 @@ __device__ __forceinline__ bool wait_geq(const int* flag, int target, int* statu
             if (ld_volatile(status) != 0) return false;
             unsigned long long now = globaltimer();
             if (t0 == 0) t0 = now;
-            else if (now - t0 > kWaitLimitNs) {
+            else if (now - t0 > limit_ns) {
                 atomicCAS(status, 0, kStatusTimeout);
                 return false;
             }

@@ -20,6 +20,10 @@ cudaError_t launch_level_analysis(bool lower, int n, const int* rowptr, const in
 cudaError_t launch_level_verify(bool lower, int n, const int* rowptr, const int* cols,
                                 const int* cand, int* mismatch, cudaStream_t stream);
 
+// Self-test of the bounded wait: one wait on a flag that nothing sets.
+cudaError_t launch_selftest_wait(const int* flag, int* status, unsigned long long limit_ns,
+                                 cudaStream_t stream);
+
 // ---- row-wise sync-free sweeps (solve_rows.cu) ----------------------------
 // Lower sweep (L y = b[perm]):    tmp[row] = (in[perm[row]] - sum L[row,c] tmp[c]) / L[row,row]
 // Upper sweep (L^T x = y):        tmp[row] = (tmp[row] - sum U[row,c] tmp[c]) / U[row,row]

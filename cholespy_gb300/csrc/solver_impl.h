@@ -25,6 +25,15 @@ int row_chunk();
 
 }  // namespace gbchol
 
+struct gbchol_solver;
+
+namespace gbchol {
+// One full solve (leaf lower, supernodal lower, supernodal upper, top-row
+// terms, leaf upper) with `work` as the permuted-space work array.
+int run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in, void* out,
+                    const int* skip, void* work, cudaStream_t s);
+}  // namespace gbchol
+
 namespace gbchol {
 
 struct DeviceGuard {

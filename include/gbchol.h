@@ -158,6 +158,15 @@ int gbchol_grad_values(int32_t precision, int64_t nnz, int32_t nrhs, const int32
                        const int32_t* cols, const void* grad_b, const void* x, void* grad_vals,
                        int32_t out_precision, int32_t symmetric, void* stream);
 
+/*
+ * Failure-detection self-test: one device-side wait, bounded by `wait_us`
+ * microseconds (1..2e6), on a flag that nothing sets. Stores the status word
+ * the wait left (GBCHOL_ETIMEOUT expected) in *status_out; the context stays
+ * usable. Every sync-free kernel uses the same bounded wait. No counterpart in
+ * the reference (its waits are unbounded, kernels/kernels.cu:20-21).
+ */
+int gbchol_selftest_wait(int32_t wait_us, int32_t* status_out);
+
 /* Solver facts. */
 typedef struct {
     int32_t n;
