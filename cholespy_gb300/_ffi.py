@@ -74,6 +74,7 @@ def _declare(lib):
         "gbchol_batch_destroy": (C.c_int, [P]),
         "gbchol_grad_values": (C.c_int, [I32, I64, I32, P, P, P, P, P, I32, I32, P]),
         "gbchol_selftest_wait": (C.c_int, [I32, C.POINTER(I32)]),
+        "gbchol_solve_noalloc": (C.c_int, [P, I32, I32, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -123,6 +123,23 @@ int gbchol_destroy(gbchol_handle h);
 int gbchol_solve(gbchol_handle h, int32_t precision, int32_t nrhs, const void* b, void* x,
                  void* stream);
 
+/*
+ * gbchol_solve for callers that cannot allocate GPU memory while solving:
+ * code inside a CUDA-graph capture that must not allocate, real-time loops
+ * whose memory is fixed up front, or hosts whose allocator owns all device
+ * memory. gbchol_solve may grow the solver's work array with cudaMalloc when
+ * a call brings more RHS than any before; this call allocates nothing. Its
+ * work array is a fixed 16 MiB file-scope device array that every GPU
+ * loading the library holds until exit, so it fails with GBCHOL_EINVAL when
+ * n * nrhs * element size (4 bytes FP32, 8 FP64) exceeds 16 MiB. The first
+ * call on a device looks up the array's device address; make it outside any
+ * stream capture. All calls share the array, so calls that overlap on the
+ * GPU race: serialise them. Same arguments and results as gbchol_solve.
+ * No counterpart in the reference.
+ */
+int gbchol_solve_noalloc(gbchol_handle h, int32_t precision, int32_t nrhs, const void* b, void* x,
+                         void* stream);
+
 /* Statistics of one refined solve. */
 typedef struct {
     int32_t iterations;       /* refinement steps taken (0 = FP32 solve was enough) */
