@@ -68,6 +68,87 @@ __device__ __forceinline__ void warp_wait(const int* flag, int epoch, int* statu
     __syncwarp();
 }
 
+// One warp's share of a lower-sweep block: inner columns [j0, j0 + J) of
+// L[unit rows, source chunk] times the matching rows of x_source, added into
+// acc (lane = unit row). J = 32: the whole block; J = 4: an eighth (the block
+// on the dependency chain is split across the 8 warps).
+template <typename T, int KW, int J>
+__device__ __forceinline__ void lower_block(const SnSys& d, const SnContrib& C, const SnUnit& U,
+                                            int j0, int slice, int k0, int kw, int epoch,
+                                            int* status, int lane, int* inv, T (*xs)[KW + 1],
+                                            T (&acc)[KW]) {
+    const T* __restrict__ panels = static_cast<const T*>(d.panels);
+    const T* tmp = static_cast<const T*>(d.tmp);
+    const int nrhs = d.nrhs;
+    if (lane < C.nr) inv[d.sn_rows[C.rows_off + lane] - U.c0] = lane;
+    __syncwarp();
+    const int src = inv[lane];
+    __syncwarp();
+    inv[lane] = -1;
+    // L is constant: its loads go out before the flag wait
+    T lv[J];
+    const T* Lp = panels + C.panel_off + src;
+#pragma unroll
+    for (int j = 0; j < J; ++j)
+        lv[j] = (src >= 0 && j0 + j < C.w) ? __ldg(Lp + (size_t)(j0 + j) * C.ld) : T(0);
+    warp_wait(d.uflags + (size_t)C.src_unit * d.nslices + slice, epoch, status, lane);
+    constexpr int PER = J * KW / 32;
+    T xv[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        const int idx = lane + 32 * u, j = j0 + idx / KW, k = idx % KW;
+        xv[u] = (j < C.w && k < kw) ? __ldcg(tmp + (size_t)(C.xcol + j) * nrhs + k0 + k) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        const int idx = lane + 32 * u;
+        xs[idx / KW][idx % KW] = xv[u];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < J; ++j)
+#pragma unroll
+        for (int k = 0; k < KW; ++k) acc[k] = fma(lv[j], xs[j][k], acc[k]);
+    __syncwarp();
+}
+
+// One warp's share of an upper-sweep block: rows [i0, i0 + J) of the 32-row
+// block starting at row position p0 of the supernode, L[rows, unit]^T times
+// x[rows], added into acc (lane = unit column).
+template <typename T, int KW, int J>
+__device__ __forceinline__ void upper_block(const SnSys& d, const SnUnit& U, int p0, int nr, int i0,
+                                            int dep, int slice, int k0, int kw, int epoch,
+                                            int* status, int lane, T (*xs)[KW + 1], T (&acc)[KW]) {
+    const T* __restrict__ panels = static_cast<const T*>(d.panels);
+    const T* tmp = static_cast<const T*>(d.tmp);
+    const int nrhs = d.nrhs;
+    T lv[J];
+    const T* Lp = panels + U.panel_col_off + p0 + i0 + (size_t)lane * U.ld;
+#pragma unroll
+    for (int i = 0; i < J; ++i) lv[i] = (lane < U.w && i0 + i < nr) ? __ldg(Lp + i) : T(0);
+    const int myrow = (lane < J && i0 + lane < nr) ? d.sn_rows[U.rows_off + p0 + i0 + lane] : 0;
+    if (dep >= 0) warp_wait(d.uflags + (size_t)dep * d.nslices + slice, epoch, status, lane);
+    constexpr int PER = J * KW / 32;
+    T xv[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        const int idx = lane + 32 * u, i = idx / KW, k = idx % KW;
+        const int row = __shfl_sync(0xffffffffu, myrow, i);
+        xv[u] = (i0 + i < nr && k < kw) ? __ldcg(tmp + (size_t)row * nrhs + k0 + k) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        const int idx = lane + 32 * u;
+        xs[idx / KW][idx % KW] = xv[u];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < J; ++i)
+#pragma unroll
+        for (int k = 0; k < KW; ++k) acc[k] = fma(lv[i], xs[i][k], acc[k]);
+    __syncwarp();
+}
+
 template <class io, bool LOWER, int KW>
 __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
     using T = typename io::t;
@@ -104,7 +185,6 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
         if (ticket >= nitems) break;
         const SnSys& d = dsm;
         const int uidx = s_uidx, slice = s_slice;
-        const T* __restrict__ panels = static_cast<const T*>(d.panels);
         T* tmp = static_cast<T*>(d.tmp);
         const int nrhs = d.nrhs;
         const int k0 = slice * KW;
@@ -125,38 +205,22 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
 #pragma unroll
         for (int k = 0; k < KW; ++k) acc[k] = T(0);
 
+        // The block on the dependency chain (lower: from the previous chunk of
+        // the same supernode, listed last; upper: from the next chunk, taken
+        // last) is split across all 8 warps; the others go one per warp.
+        constexpr int kSplit = kW / kWarps;
         if (LOWER) {
             const int nb = U.contrib_end - U.contrib_begin;
-            for (int b = warp; b < nb; b += kWarps) {
+            const bool split = nb > 0 && U.pos0 > 0 && d.contribs[U.contrib_end - 1].src_unit == uidx - 1;
+            const int nfree = split ? nb - 1 : nb;
+            for (int b = warp; b < nfree; b += kWarps) {
                 const SnContrib C = d.contribs[U.contrib_begin + b];
-                if (lane < C.nr) sm.inv[warp][d.sn_rows[C.rows_off + lane] - U.c0] = lane;
-                __syncwarp();
-                const int src = sm.inv[warp][lane];
-                sm.inv[warp][lane] = -1;
-                // L is constant: its loads go out before the flag wait
-                T lv[kW];
-                const T* Lp = panels + C.panel_off + src;
-#pragma unroll
-                for (int j = 0; j < kW; ++j)
-                    lv[j] = (src >= 0 && j < C.w) ? __ldg(Lp + (size_t)j * C.ld) : T(0);
-                warp_wait(d.uflags + (size_t)C.src_unit * d.nslices + slice, epoch, a.status, lane);
-                T xv[KW];
-#pragma unroll
-                for (int u = 0; u < KW; ++u) {
-                    const int idx = lane + 32 * u, j = idx / KW, k = idx % KW;
-                    xv[u] = (j < C.w && k < kw) ? __ldcg(tmp + (size_t)(C.xcol + j) * nrhs + k0 + k) : T(0);
-                }
-#pragma unroll
-                for (int u = 0; u < KW; ++u) {
-                    const int idx = lane + 32 * u;
-                    xs[idx / KW][idx % KW] = xv[u];
-                }
-                __syncwarp();
-#pragma unroll
-                for (int j = 0; j < kW; ++j)
-#pragma unroll
-                    for (int k = 0; k < KW; ++k) acc[k] = fma(lv[j], xs[j][k], acc[k]);
-                __syncwarp();
+                lower_block<T, KW, kW>(d, C, U, 0, slice, k0, kw, epoch, a.status, lane, sm.inv[warp], xs, acc);
+            }
+            if (split) {
+                const SnContrib C = d.contribs[U.contrib_end - 1];
+                lower_block<T, KW, kSplit>(d, C, U, warp * kSplit, slice, k0, kw, epoch, a.status, lane,
+                                           sm.inv[warp], xs, acc);
             }
         } else {
             // block list: off-diagonal rows of the supernode (32-row blocks),
@@ -165,8 +229,10 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
             const int sn_w = U.sn_w;                        // supernode width
             const int nrb = (U.ld - sn_w + kW - 1) / kW;    // off-diagonal row blocks
             const int nlater = (sn_w - wj + kW - 1) / kW;   // later chunks
+            const bool split = nlater > 0;
+            const int nfree = nrb + nlater - (split ? 1 : 0);
             bool parent_ready = false;
-            for (int b = warp; b < nrb + nlater; b += kWarps) {
+            for (int b = warp; b < nfree; b += kWarps) {
                 int p0, nr, dep;
                 if (b < nrb) {
                     p0 = sn_w + b * kW;
@@ -179,30 +245,12 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
                     nr = min(kW, sn_w - p0);
                     dep = uidx + 1 + c;
                 }
-                T lv[kW];
-                const T* Lp = panels + U.panel_col_off + p0 + (size_t)lane * U.ld;
-#pragma unroll
-                for (int i = 0; i < kW; ++i) lv[i] = (lane < w && i < nr) ? __ldg(Lp + i) : T(0);
-                const int myrow = lane < nr ? d.sn_rows[U.rows_off + p0 + lane] : 0;
-                if (dep >= 0) warp_wait(d.uflags + (size_t)dep * d.nslices + slice, epoch, a.status, lane);
-                T xv[KW];
-#pragma unroll
-                for (int u = 0; u < KW; ++u) {
-                    const int idx = lane + 32 * u, i = idx / KW, k = idx % KW;
-                    const int row = __shfl_sync(0xffffffffu, myrow, i);
-                    xv[u] = (i < nr && k < kw) ? __ldcg(tmp + (size_t)row * nrhs + k0 + k) : T(0);
-                }
-#pragma unroll
-                for (int u = 0; u < KW; ++u) {
-                    const int idx = lane + 32 * u;
-                    xs[idx / KW][idx % KW] = xv[u];
-                }
-                __syncwarp();
-#pragma unroll
-                for (int i = 0; i < kW; ++i)
-#pragma unroll
-                    for (int k = 0; k < KW; ++k) acc[k] = fma(lv[i], xs[i][k], acc[k]);
-                __syncwarp();
+                upper_block<T, KW, kW>(d, U, p0, nr, 0, dep, slice, k0, kw, epoch, a.status, lane, xs, acc);
+            }
+            if (split) {  // the next chunk of the supernode (c = 0)
+                const int nr = min(kW, sn_w - wj);
+                upper_block<T, KW, kSplit>(d, U, wj, nr, warp * kSplit, uidx + 1, slice, k0, kw, epoch,
+                                           a.status, lane, xs, acc);
             }
         }
 
