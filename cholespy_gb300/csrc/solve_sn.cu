@@ -52,13 +52,45 @@ struct SnIO {
     static constexpr bool accum = ACCUM;
 };
 
+// Row stride of the x staging area: a multiple of 16 bytes so that a row
+// can be read with 16-byte vector loads (all lanes read the same row:
+// broadcast), plus 16 bytes of skew against bank conflicts in the reduction.
+template <typename T, int KW>
+struct XsStride {
+    static constexpr int value = KW + 16 / (int)sizeof(T);
+};
+
 template <typename T, int KW>
 struct SnSmem {
-    T xs[kWarps][kW][KW + 1];  // per-warp staging of x blocks; reused for the reduction
+    static constexpr int XS = XsStride<T, KW>::value;
+    __align__(16) T xs[kWarps][kW][XS];  // per-warp staging of x blocks; reused for the reduction
     T t[kW][KW + 1];           // reduced right-hand side of the unit
     T d[kW][kW + 1];           // diagonal block
     int inv[kWarps][kW];       // unit row -> block row (lower sweep)
 };
+
+// acc[k] += a * row[k] for k < KW, reading `row` (16-byte aligned shared
+// memory, same address in every lane) with 16-byte vector loads.
+template <int KW>
+__device__ __forceinline__ void axpy_row(float (&acc)[KW], float a, const float* row) {
+#pragma unroll
+    for (int k = 0; k < KW; k += 4) {
+        const float4 v = *reinterpret_cast<const float4*>(row + k);
+        acc[k] = fmaf(a, v.x, acc[k]);
+        acc[k + 1] = fmaf(a, v.y, acc[k + 1]);
+        acc[k + 2] = fmaf(a, v.z, acc[k + 2]);
+        acc[k + 3] = fmaf(a, v.w, acc[k + 3]);
+    }
+}
+template <int KW>
+__device__ __forceinline__ void axpy_row(double (&acc)[KW], double a, const double* row) {
+#pragma unroll
+    for (int k = 0; k < KW; k += 2) {
+        const double2 v = *reinterpret_cast<const double2*>(row + k);
+        acc[k] = fma(a, v.x, acc[k]);
+        acc[k + 1] = fma(a, v.y, acc[k + 1]);
+    }
+}
 
 // Lane 0 waits for a flag; the warp proceeds together. Loads of data
 // published under the flag use ld.cg (L2), which holds the producer's
@@ -75,7 +107,7 @@ __device__ __forceinline__ void warp_wait(const int* flag, int epoch, int* statu
 template <typename T, int KW, int J>
 __device__ __forceinline__ void lower_block(const SnSys& d, const SnContrib& C, const SnUnit& U,
                                             int j0, int slice, int k0, int kw, int epoch,
-                                            int* status, int lane, int* inv, T (*xs)[KW + 1],
+                                            int* status, int lane, int* inv, T (*xs)[XsStride<T, KW>::value],
                                             T (&acc)[KW]) {
     const T* __restrict__ panels = static_cast<const T*>(d.panels);
     const T* tmp = static_cast<const T*>(d.tmp);
@@ -105,10 +137,12 @@ __device__ __forceinline__ void lower_block(const SnSys& d, const SnContrib& C, 
         xs[idx / KW][idx % KW] = xv[u];
     }
     __syncwarp();
+    const int jn = min(J, C.w - j0);  // warp-uniform
 #pragma unroll
-    for (int j = 0; j < J; ++j)
-#pragma unroll
-        for (int k = 0; k < KW; ++k) acc[k] = fma(lv[j], xs[j][k], acc[k]);
+    for (int j = 0; j < J; ++j) {
+        if (j >= jn) break;
+        axpy_row<KW>(acc, lv[j], xs[j]);
+    }
     __syncwarp();
 }
 
@@ -118,7 +152,7 @@ __device__ __forceinline__ void lower_block(const SnSys& d, const SnContrib& C, 
 template <typename T, int KW, int J>
 __device__ __forceinline__ void upper_block(const SnSys& d, const SnUnit& U, int p0, int nr, int i0,
                                             int dep, int slice, int k0, int kw, int epoch,
-                                            int* status, int lane, T (*xs)[KW + 1], T (&acc)[KW]) {
+                                            int* status, int lane, T (*xs)[XsStride<T, KW>::value], T (&acc)[KW]) {
     const T* __restrict__ panels = static_cast<const T*>(d.panels);
     const T* tmp = static_cast<const T*>(d.tmp);
     const int nrhs = d.nrhs;
@@ -142,10 +176,12 @@ __device__ __forceinline__ void upper_block(const SnSys& d, const SnUnit& U, int
         xs[idx / KW][idx % KW] = xv[u];
     }
     __syncwarp();
+    const int in = min(J, nr - i0);  // warp-uniform
 #pragma unroll
-    for (int i = 0; i < J; ++i)
-#pragma unroll
-        for (int k = 0; k < KW; ++k) acc[k] = fma(lv[i], xs[i][k], acc[k]);
+    for (int i = 0; i < J; ++i) {
+        if (i >= in) break;
+        axpy_row<KW>(acc, lv[i], xs[i]);
+    }
     __syncwarp();
 }
 
@@ -159,7 +195,7 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
     const int nitems = a.nitems;
     // every CTA reads the sweep's epoch before the last CTA out bumps it
     const int epoch = dev::ld_volatile(a.epoch);
-    T (*xs)[KW + 1] = sm.xs[warp];
+    T (*xs)[XsStride<T, KW>::value] = sm.xs[warp];
     if (LOWER) sm.inv[warp][lane] = -1;
     __shared__ int ticket, s_uidx, s_slice;
     __shared__ SnSys dsm;
