@@ -41,11 +41,14 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["poisson64", "batch", "autograd", "ico6", "grid64"],
+    p.add_argument("--workload", choices=["poisson64", "batch", "autograd", "ico6", "grid64", "solve"],
                    default="poisson64",
                    help="poisson64 (default, headline): 64^3 FP32+IR; batch: 256 grid systems "
                         "in one graph-captured persistent launch; autograd: icosphere-7 forward+"
-                        "backward; ico6: icosphere-6 FP32 n_rhs=3; grid64: 64x64 FP64 n_rhs=1")
+                        "backward; ico6: icosphere-6 FP32 n_rhs=3; grid64: 64x64 FP64 n_rhs=1; "
+                        "solve: plain solves of the k^3 Poisson system (--k, --nrhs, --fp64), "
+                        "the program profiled with ncu")
+    p.add_argument("--fp64", action="store_true", help="solve workload: FP64 instead of FP32")
     p.add_argument("--k", type=int, default=64, help="grid side (n = k^3)")
     p.add_argument("--nrhs", type=int, default=128)
     p.add_argument("--tol", type=float, default=1e-10)
@@ -619,6 +622,41 @@ def run_mesh(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_solve(args, world, rank, local):
+    """Plain solves of the k^3 7-point Poisson system (shift 1e-3, N(0,1) RHS,
+    seed 2): the program the ncu captures profile."""
+    import torch
+
+    from cholespy_gb300 import CholeskySolverD, CholeskySolverF, MatrixType, _build
+    _build.build()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    n, vals, idx, b = workload(args)
+    cls = CholeskySolverD if args.fp64 else CholeskySolverF
+    s = cls(n, torch.tensor(idx[0]).to(dev), torch.tensor(idx[1]).to(dev), torch.tensor(vals).to(dev),
+            MatrixType.COO)
+    dt = torch.float64 if args.fp64 else torch.float32
+    bd = torch.tensor(b, dtype=dt, device=dev)
+    xd = torch.zeros_like(bd)
+    t = _events_time(torch, dev, stream, lambda: s.solve(bd, xd), args.steps, args.warmup, world)
+    s.check()
+    info = s.info()
+    es = 8 if args.fp64 else 4
+    byts = algorithmic_bytes(n, info.nnz_l, args.nrhs, es)
+    peak, kind = hbm_peak()
+    line = _line(args, world, "RHS-solves/s", world * args.nrhs * args.steps / t, "RHS-solves/s", t,
+                 "f64" if args.fp64 else "f32",
+                 config_dict(args, n, len(vals), info.nnz_l),
+                 roofline={"kernel": "triangular sweeps (lower+upper)", "bound": "hbm",
+                           "achieved": byts / (t / args.steps) / 1e9, "peak": peak, "peak_kind": kind,
+                           "unit": "GB/s", "frac": byts / (t / args.steps) / 1e9 / peak, "traffic": None,
+                           "algorithmic_bytes": byts},
+                 gpu_launches=info.launches_per_solve * args.steps)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup(args)
@@ -631,6 +669,8 @@ def main():
             run_autograd(args, world, rank, local)
         elif args.workload in ("ico6", "grid64"):
             run_mesh(args, world, rank, local)
+        elif args.workload == "solve":
+            run_solve(args, world, rank, local)
         else:
             run_ours(args, world, rank, local)
     finally:
