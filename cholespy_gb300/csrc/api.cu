@@ -198,6 +198,7 @@ int setup_plan(gbchol_solver* h, const std::vector<int32_t>& rp, const std::vect
     if (f64) CUDA_TRY(h->pan64.upload(P.panels.data(), P.panels.size()));
     CUDA_TRY(h->units.upload(P.units.data(), P.units.size()));
     CUDA_TRY(h->order_lo.upload(P.unit_order_lo.data(), P.unit_order_lo.size()));
+    CUDA_TRY(h->unit_of_row.upload(P.unit_of_row.data(), P.unit_of_row.size()));
     CUDA_TRY(h->order_up.upload(P.unit_order_up.data(), P.unit_order_up.size()));
     if (f32) CUDA_TRY(upload_cast(h->dinv32, P.dinv));
     if (f64) CUDA_TRY(h->dinv64.upload(P.dinv.data(), P.dinv.size()));
@@ -333,6 +334,7 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
     sn.sys0.perm = h->perm.p;
     sn.sys0.tmp = work;
     sn.sys0.uflags = h->uflags.p;
+    sn.sys0.unit_of_row = h->unit_of_row.p;
     sn.sys0.nrhs = nrhs;
     sn.sys0.nslices = sn_slices(nrhs, !f32);
     sn.nitems = (int)P.units.size() * sn.sys0.nslices;

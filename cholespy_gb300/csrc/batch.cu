@@ -194,6 +194,7 @@ int gbchol_batch_create(int32_t count, const gbchol_handle* solvers, const int32
         sn.perm = h->perm.p;
         sn.tmp = base.tmp;
         sn.uflags = b->uflags.p + b->uflag_off[s];
+        sn.unit_of_row = h->unit_of_row.p;
         sn.nrhs = nrhs[s];
         sn.nslices = b->nslices[s];
         b->sn_lo_h.push_back(sn);

@@ -160,9 +160,15 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
         for (int32_t u = 0; u < nunits; ++u)
             for (int32_t e = P.units[u].contrib_begin; e < P.units[u].contrib_end; ++e)
                 lo[u] = std::max(lo[u], lo[P.contribs[e].src_unit] + 1);
+        // upper sweep: each 32-row block of the supernode's off-diagonal rows
+        // waits for the unit holding its first (lowest) row: those rows lie on
+        // the etree path above the supernode, and in the upper sweep a higher
+        // row is always solved before a lower one
         for (int32_t u = nunits - 1; u >= 0; --u) {
             const SnUnit& U = P.units[u];
-            if (U.parent_first_unit >= 0) up[u] = std::max(up[u], up[U.parent_first_unit] + 1);
+            const int32_t* rows = P.sn_rows.data() + U.rows_off;
+            for (int32_t p = U.sn_w; p < U.ld; p += kChunk)
+                up[u] = std::max(up[u], up[unit_of_col[rows[p]]] + 1);
             const int32_t nlater = (U.sn_w - (U.pos0 + U.w) + kChunk - 1) / kChunk;
             for (int32_t c = 0; c < nlater; ++c) up[u] = std::max(up[u], up[u + 1 + c] + 1);
         }
@@ -176,6 +182,8 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
         std::stable_sort(P.unit_order_up.begin(), P.unit_order_up.end(),
                          [&](int32_t a, int32_t b) { return up[a] < up[b]; });
     }
+
+    P.unit_of_row = unit_of_col;
 
     // ---- leaf region -------------------------------------------------------
     // CSR of L (columns ascending, diagonal last)

@@ -55,6 +55,7 @@ struct SolvePlan {
     std::vector<int32_t> unit_order_lo;   // units sorted by lower-sweep dependency level
     std::vector<int32_t> unit_order_up;   // units sorted by upper-sweep dependency level
     std::vector<int32_t> unit_level_lo, unit_level_up;  // those levels, per unit
+    std::vector<int32_t> unit_of_row;     // top rows: the unit holding the row (-1: leaf row)
     // leaf region, lower sweep: CSR over all rows. Leaf rows hold their full
     // row of L (diagonal last); top rows hold only their leaf-column entries.
     std::vector<int32_t> lo_rowptr, lo_cols;

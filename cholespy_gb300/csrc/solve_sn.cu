@@ -259,22 +259,23 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
                                            sm.inv[warp], xs, acc);
             }
         } else {
-            // block list: off-diagonal rows of the supernode (32-row blocks),
-            // then the later chunks of the supernode, last chunk first
+            // block list: off-diagonal rows of the supernode in 32-row blocks,
+            // highest rows first (they are solved first), each waiting for the
+            // unit of its lowest row; then the later chunks of the supernode,
+            // last chunk first; the next chunk's block (the dependency chain)
+            // is split across all warps
             const int wj = U.pos0 + w;                      // end of this unit's columns
             const int sn_w = U.sn_w;                        // supernode width
             const int nrb = (U.ld - sn_w + kW - 1) / kW;    // off-diagonal row blocks
             const int nlater = (sn_w - wj + kW - 1) / kW;   // later chunks
             const bool split = nlater > 0;
             const int nfree = nrb + nlater - (split ? 1 : 0);
-            bool parent_ready = false;
             for (int b = warp; b < nfree; b += kWarps) {
                 int p0, nr, dep;
                 if (b < nrb) {
-                    p0 = sn_w + b * kW;
+                    p0 = sn_w + (nrb - 1 - b) * kW;
                     nr = min(kW, U.ld - p0);
-                    dep = parent_ready ? -1 : U.parent_first_unit;
-                    parent_ready = true;
+                    dep = d.unit_of_row[d.sn_rows[U.rows_off + p0]];
                 } else {
                     const int c = nlater - 1 - (b - nrb);  // later chunk index, last first
                     p0 = wj + c * kW;

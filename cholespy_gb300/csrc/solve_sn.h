@@ -18,6 +18,7 @@ struct SnSys {
     void* tmp = nullptr;            // T, n x nrhs, permuted space
     void* out = nullptr;            // upper: solution through perm (TOut)
     int* uflags = nullptr;          // n_units * nslices completion flags
+    const int32_t* unit_of_row = nullptr;  // unit holding each top row (upper sweep waits)
     int nrhs = 0;
     int nslices = 1;                // RHS slices (see sn_slices)
 };

@@ -123,6 +123,7 @@ struct gbchol_solver {
     DevBuf<SnContrib> contribs;
     DevBuf<int32_t> uflags;   // units * RHS slices
     DevBuf<int32_t> order_lo, order_up;  // units in dependency-level order
+    DevBuf<int32_t> unit_of_row;         // unit holding each top row
     DevBuf<float> dinv32;
     DevBuf<double> dinv64;    // inverse diagonal blocks of the units
     DevBuf<int32_t> counters; // [ticket, exits] per sweep kernel (5 kernels)
