@@ -213,7 +213,9 @@ int setup_plan(gbchol_solver* h, const std::vector<int32_t>& rp, const std::vect
         CUDA_TRY(h->dev_epoch.upload(&one, 1));
     }
     CUDA_TRY(h->contribs.upload(P.contribs.data(), P.contribs.size()));
-    CUDA_TRY(h->uflags.alloc(std::max<size_t>(1, P.units.size() * 8)));  // <= 8 RHS slices
+    CUDA_TRY(h->parts.upload(P.parts.data(), P.parts.size()));
+    // unit flags, then partial-sum flags; <= 8 RHS slices
+    CUDA_TRY(h->uflags.alloc(std::max<size_t>(1, (P.units.size() + P.parts.size()) * 8)));
     CUDA_TRY(cudaMemset(h->uflags.p, 0, sizeof(int32_t) * h->uflags.count));
     // row flags: top rows are always "ready" for the row kernels (they are
     // solved by the supernodal kernel in an earlier launch)
@@ -301,7 +303,14 @@ namespace {
 // kernel; `out` is written through perm by both upper kernels.
 }  // namespace
 
-// One full solve with the permuted-space work array `work` (n x nrhs of T).
+size_t gbchol::work_bytes(const gbchol_solver* h, int nrhs, bool f32) {
+    const size_t es = f32 ? sizeof(float) : sizeof(double);
+    const size_t x = ((size_t)std::max(h->n, 1) * nrhs * es + 255) / 256 * 256;
+    return x + sn_pbuf_bytes((int)h->plan.parts.size(), nrhs, !f32, false);
+}
+
+// One full solve with the work array `work` (work_bytes: the permuted-space
+// n x nrhs array of T, then the partial-sum slots).
 int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in,
                             void* out, const int* skip, void* work, cudaStream_t s) {
     const SolvePlan& P = h->plan;
@@ -335,9 +344,13 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
     sn.sys0.tmp = work;
     sn.sys0.uflags = h->uflags.p;
     sn.sys0.unit_of_row = h->unit_of_row.p;
+    sn.sys0.parts = h->parts.p;
+    sn.sys0.pbuf = static_cast<unsigned char*>(work) +
+                   ((size_t)h->n * nrhs * (f32 ? sizeof(float) : sizeof(double)) + 255) / 256 * 256;
+    sn.sys0.n_units = (int)P.units.size();
     sn.sys0.nrhs = nrhs;
     sn.sys0.nslices = sn_slices(nrhs, !f32);
-    sn.nitems = (int)P.units.size() * sn.sys0.nslices;
+    sn.nitems = (int)P.unit_order_lo.size() * sn.sys0.nslices;
     sn.status = h->status.p;
     sn.skip = skip;
     sn.order = h->order_lo.p;
@@ -345,6 +358,7 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
     sn.epoch = h->dev_epoch.p;
     CUDA_TRY(launch_sn_sweep(sn, true, io, s));
     sn.sys0.out = out;
+    sn.nitems = (int)P.units.size() * sn.sys0.nslices;
     sn.order = h->order_up.p;
     sn.counters = h->counters.p + 4;
     CUDA_TRY(launch_sn_sweep(sn, false, io, s));
@@ -514,8 +528,7 @@ int gbchol_reserve(gbchol_handle h, int32_t nrhs) {
     if (!h) return fail(GBCHOL_EINVAL, "Null handle.");
     if (int rc = check_rhs(nrhs)) return rc;
     DeviceGuard g(h->device);
-    size_t es = (h->store & GBCHOL_STORE_F64) ? sizeof(double) : sizeof(float);
-    return ensure_tmp(h, (size_t)std::max(h->n, 1) * nrhs * es);
+    return ensure_tmp(h, std::max(work_bytes(h, nrhs, true), work_bytes(h, nrhs, false)));
 }
 
 int gbchol_solve(gbchol_handle h, int32_t precision, int32_t nrhs, const void* b, void* x,
@@ -532,7 +545,7 @@ int gbchol_solve(gbchol_handle h, int32_t precision, int32_t nrhs, const void* b
     if (!b || !x) return fail(GBCHOL_EINVAL, "Null b or x.");
     DeviceGuard g(h->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (int rc = ensure_tmp(h, (size_t)h->n * nrhs * (f32 ? sizeof(float) : sizeof(double)))) return rc;
+    if (int rc = ensure_tmp(h, work_bytes(h, nrhs, f32))) return rc;
     const SweepIO io = f32 ? SweepIO::F32 : SweepIO::F64;
     if (int rc = run_sweeps(h, f32, io, nrhs, b, x, nullptr, s)) return rc;
     h->last_stream = s;
@@ -556,7 +569,7 @@ int gbchol_solve_refined(gbchol_handle h, int32_t nrhs, const double* b, double*
     DeviceGuard g(h->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int n = h->n;
-    if (int rc = ensure_tmp(h, (size_t)n * nrhs * sizeof(float))) return rc;
+    if (int rc = ensure_tmp(h, work_bytes(h, nrhs, true))) return rc;
     if (h->r64.count < (size_t)n * nrhs) CUDA_TRY(h->r64.alloc((size_t)n * nrhs));
     const int grid = residual_grid(n);
     if (h->partials.count < (size_t)grid * 2 * nrhs) CUDA_TRY(h->partials.alloc((size_t)grid * 2 * GBCHOL_MAX_RHS));

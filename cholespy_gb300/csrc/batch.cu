@@ -28,7 +28,7 @@ struct gbchol_batch_s {
     bool f32 = true;
     std::vector<gbchol_handle> solvers;
     std::vector<int32_t> nrhs, nslices;
-    std::vector<size_t> tmp_off, row_off, uflag_off;
+    std::vector<size_t> tmp_off, pbuf_off, row_off, uflag_off;
     std::vector<RowSys> lo_h, pt_h, up_h;
     std::vector<SnSys> sn_lo_h, sn_up_h;
     DevBuf<RowSys> lo_d, pt_d, up_d;
@@ -102,11 +102,14 @@ int gbchol_batch_create(int32_t count, const gbchol_handle* solvers, const int32
         b->tmp_off.push_back(tmp_total);
         tmp_total += (size_t)h->n * nrhs[s] * es;
         tmp_total = (tmp_total + 255) / 256 * 256;
+        b->pbuf_off.push_back(tmp_total);
+        tmp_total += sn_pbuf_bytes((int)h->plan.parts.size(), nrhs[s], !f32, true);
+        tmp_total = (tmp_total + 255) / 256 * 256;
         b->row_off.push_back(rows_total);
         rows_total += (size_t)h->n;
         flags_init.insert(flags_init.end(), h->flags_init.begin(), h->flags_init.end());
         b->uflag_off.push_back(uflags_total);
-        uflags_total += h->plan.units.size() * (size_t)b->nslices.back();
+        uflags_total += (h->plan.units.size() + h->plan.parts.size()) * (size_t)b->nslices.back();
     }
     CUDA_TRY(b->tmp.alloc(std::max<size_t>(tmp_total, 1)));
     CUDA_TRY(b->flags.upload(flags_init.data(), flags_init.size()));
@@ -143,16 +146,25 @@ int gbchol_batch_create(int32_t count, const gbchol_handle* solvers, const int32
     for (int lower = 1; lower >= 0; --lower) {
         std::vector<std::tuple<int32_t, int32_t, int32_t, int32_t>> items;
         for (int32_t s = 0; s < count; ++s) {
+            // items in the system's own order (units, and in the lower sweep
+            // partial sums ~p), keyed by level then that position
             const SolvePlan& P = b->solvers[s]->plan;
-            const std::vector<int32_t>& lev = lower ? P.unit_level_lo : P.unit_level_up;
-            for (int32_t u = 0; u < (int32_t)P.units.size(); ++u)
-                for (int32_t sl = 0; sl < b->nslices[s]; ++sl) items.emplace_back(lev[u], s, u, sl);
+            const std::vector<int32_t>& order = lower ? P.unit_order_lo : P.unit_order_up;
+            for (int32_t k = 0; k < (int32_t)order.size(); ++k) {
+                const int32_t it = order[k];
+                const int32_t lev = it >= 0 ? (lower ? P.unit_level_lo[it] : P.unit_level_up[it])
+                                            : P.part_level_lo[~it];
+                for (int32_t sl = 0; sl < b->nslices[s]; ++sl) items.emplace_back(lev, s, k, sl);
+            }
         }
         std::sort(items.begin(), items.end());
         std::vector<int32_t> isys(items.size()), icode(items.size());
         for (size_t k = 0; k < items.size(); ++k) {
-            isys[k] = std::get<1>(items[k]);
-            icode[k] = (std::get<2>(items[k]) << 3) | std::get<3>(items[k]);
+            const int32_t s = std::get<1>(items[k]);
+            const SolvePlan& P = b->solvers[s]->plan;
+            const int32_t it = (lower ? P.unit_order_lo : P.unit_order_up)[std::get<2>(items[k])];
+            isys[k] = s;
+            icode[k] = sn_item_code(it, std::get<3>(items[k]));
         }
         if (lower) {
             b->n_snlo = (int32_t)items.size();
@@ -195,6 +207,9 @@ int gbchol_batch_create(int32_t count, const gbchol_handle* solvers, const int32
         sn.tmp = base.tmp;
         sn.uflags = b->uflags.p + b->uflag_off[s];
         sn.unit_of_row = h->unit_of_row.p;
+        sn.parts = h->parts.p;
+        sn.pbuf = b->tmp.p + b->pbuf_off[s];
+        sn.n_units = (int)h->plan.units.size();
         sn.nrhs = nrhs[s];
         sn.nslices = b->nslices[s];
         b->sn_lo_h.push_back(sn);

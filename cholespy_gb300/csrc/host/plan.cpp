@@ -18,6 +18,7 @@
 #include "plan.h"
 
 #include <algorithm>
+#include <climits>
 #include <stdexcept>
 
 namespace gbchol {
@@ -82,25 +83,16 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
             u.pos0 = c0 - f;
             u.panel_col_off = panel_off[s] + (int64_t)(c0 - f) * ld;
             u.rows_off = rows_off[s];
-            u.upper_dep = -1;
             for (int32_t c = c0; c < c0 + u.w; ++c) unit_of_col[c] = (int32_t)P.units.size();
             P.units.push_back(u);
             unit_count[s]++;
         }
     }
     const int32_t nunits = (int32_t)P.units.size();
-    // upper-sweep dependency: the next chunk of the same supernode, else the
-    // first chunk of the parent supernode (whose completion implies every row
-    // below this supernode's diagonal block is solved)
     for (int32_t s = 0; s < nsn; ++s) {
         if (!P.sn_top[s]) continue;
-        for (int32_t k = 0; k < unit_count[s]; ++k) {
-            SnUnit& u = P.units[first_unit[s] + k];
-            u.sn_w = P.sn_start[s + 1] - P.sn_start[s];
-            u.parent_first_unit = sn_parent[s] >= 0 ? first_unit[sn_parent[s]] : -1;
-            if (k + 1 < unit_count[s]) u.upper_dep = first_unit[s] + k + 1;
-            else if (sn_parent[s] >= 0) u.upper_dep = first_unit[sn_parent[s]];
-        }
+        for (int32_t k = 0; k < unit_count[s]; ++k)
+            P.units[first_unit[s] + k].sn_w = P.sn_start[s + 1] - P.sn_start[s];
     }
     // lower-sweep contributions, gathered per destination unit in source order
     std::vector<std::vector<SnContrib>> per_unit((size_t)nunits);
@@ -127,16 +119,40 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
                 c.nr = q - p;
                 c.w = V.w;
                 c.src_unit = vu;
+                c.rowmask = 0;
+                for (int32_t t = p; t < q; ++t) c.rowmask |= 1u << (rows[t] - P.units[dst].c0);
                 per_unit[dst].push_back(c);
                 p = q;
             }
         }
         (void)w;
     }
+    // The list is in source order: descendants first, the earlier chunks of
+    // the unit's own supernode last (the previous chunk, on the dependency
+    // chain, is the very last). A long list keeps its last part_keep blocks
+    // and cuts the rest into consecutive groups of about part_group blocks,
+    // each summed by a partial-sum item.
     for (int32_t u = 0; u < nunits; ++u) {
-        P.units[u].contrib_begin = (int32_t)P.contribs.size();
+        SnUnit& U = P.units[u];
+        const int32_t b0 = (int32_t)P.contribs.size();
         P.contribs.insert(P.contribs.end(), per_unit[u].begin(), per_unit[u].end());
-        P.units[u].contrib_end = (int32_t)P.contribs.size();
+        const int32_t nb = (int32_t)per_unit[u].size();
+        U.contrib_begin = b0;
+        U.contrib_end = b0 + nb;
+        U.part_begin = U.part_end = (int32_t)P.parts.size();
+        if (opt.part_group > 0 && nb > opt.part_keep + opt.part_group) {
+            const int32_t m = nb - opt.part_keep;
+            const int32_t ng = (m + opt.part_group - 1) / opt.part_group;
+            for (int32_t g = 0; g < ng; ++g) {
+                SnPartial q{};
+                q.unit = u;
+                q.contrib_begin = b0 + (int32_t)((int64_t)m * g / ng);
+                q.contrib_end = b0 + (int32_t)((int64_t)m * (g + 1) / ng);
+                P.parts.push_back(q);
+            }
+            U.contrib_begin = b0 + m;
+            U.part_end = (int32_t)P.parts.size();
+        }
     }
 
     // inverses of the diagonal blocks (FP64 forward substitution on the
@@ -154,31 +170,88 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
             }
         }
     }
-    // dependency levels of the units, for level-ordered dynamic scheduling
+    // Ticket order of the supernodal items. Each item's start is estimated
+    // with a small cost model (per item: flag latency kLat, fixed cost kBase,
+    // kBlk per round of 8 blocks, one block per warp) from the estimated
+    // finish of the items it waits on: an item should start when its work
+    // before its last wait is just done as that wait ends. The key is that
+    // start, and at least one more than the key of every item it waits on, so
+    // sorting by key is a topological order (a CTA only ever waits on items
+    // with smaller tickets: the persistent kernels cannot deadlock).
+    // Ordering by plain dependency level instead would hand tickets to items
+    // whose inputs come from long, slow chains, idling CTAs that items on the
+    // critical path need.
     {
-        std::vector<int32_t> lo((size_t)nunits, 0), up((size_t)nunits, 0);
-        for (int32_t u = 0; u < nunits; ++u)
-            for (int32_t e = P.units[u].contrib_begin; e < P.units[u].contrib_end; ++e)
-                lo[u] = std::max(lo[u], lo[P.contribs[e].src_unit] + 1);
+        constexpr int64_t kLat = 1000, kBase = 2000, kBlk = 1500;  // ns
+        const int32_t nparts = (int32_t)P.parts.size();
+        struct Est {
+            int64_t first = INT64_MAX, last = 0, key_dep = -1;
+            void dep(int64_t fin, int64_t key) {
+                first = std::min(first, fin + kLat);
+                last = std::max(last, fin + kLat);
+                key_dep = std::max(key_dep, key);
+            }
+            // returns the finish estimate, sets the key
+            int64_t done(int64_t nblocks, int64_t& key) const {
+                const int64_t rounds = std::max<int64_t>(1, (nblocks + 7) / 8);
+                const int64_t f = first == INT64_MAX ? 0 : first;
+                key = std::max({f, last - (rounds - 1) * kBlk, key_dep + 1});
+                return std::max(std::max(key, last) + kBase + kBlk, key + kBase + kBlk * rounds);
+            }
+        };
+        std::vector<int64_t> fin_u((size_t)nunits, 0), fin_p((size_t)nparts, 0);
+        std::vector<int64_t> key_u((size_t)nunits, 0), key_p((size_t)nparts, 0), key_up((size_t)nunits, 0);
+        for (int32_t u = 0; u < nunits; ++u) {  // sources precede their destinations
+            const SnUnit& U = P.units[u];
+            Est eu;
+            for (int32_t q = U.part_begin; q < U.part_end; ++q) {
+                Est eq;
+                for (int32_t e = P.parts[q].contrib_begin; e < P.parts[q].contrib_end; ++e)
+                    eq.dep(fin_u[P.contribs[e].src_unit], key_u[P.contribs[e].src_unit]);
+                fin_p[q] = eq.done(P.parts[q].contrib_end - P.parts[q].contrib_begin, key_p[q]);
+                eu.dep(fin_p[q], key_p[q]);
+            }
+            for (int32_t e = U.contrib_begin; e < U.contrib_end; ++e)
+                eu.dep(fin_u[P.contribs[e].src_unit], key_u[P.contribs[e].src_unit]);
+            fin_u[u] = eu.done((U.contrib_end - U.contrib_begin) + (U.part_end - U.part_begin), key_u[u]);
+        }
         // upper sweep: each 32-row block of the supernode's off-diagonal rows
         // waits for the unit holding its first (lowest) row: those rows lie on
         // the etree path above the supernode, and in the upper sweep a higher
         // row is always solved before a lower one
+        std::vector<int64_t> fin_up((size_t)nunits, 0);
         for (int32_t u = nunits - 1; u >= 0; --u) {
             const SnUnit& U = P.units[u];
             const int32_t* rows = P.sn_rows.data() + U.rows_off;
-            for (int32_t p = U.sn_w; p < U.ld; p += kChunk)
-                up[u] = std::max(up[u], up[unit_of_col[rows[p]]] + 1);
+            Est eu;
+            int64_t nb = 0;
+            for (int32_t p = U.sn_w; p < U.ld; p += kChunk, ++nb) {
+                const int32_t d = unit_of_col[rows[p]];
+                eu.dep(fin_up[d], key_up[d]);
+            }
             const int32_t nlater = (U.sn_w - (U.pos0 + U.w) + kChunk - 1) / kChunk;
-            for (int32_t c = 0; c < nlater; ++c) up[u] = std::max(up[u], up[u + 1 + c] + 1);
+            for (int32_t c = 0; c < nlater; ++c, ++nb) eu.dep(fin_up[u + 1 + c], key_up[u + 1 + c]);
+            fin_up[u] = eu.done(nb, key_up[u]);
         }
-        P.unit_level_lo = lo;
-        P.unit_level_up = up;
-        P.unit_order_lo.resize((size_t)nunits);
+        auto clamp32 = [](int64_t v) { return (int32_t)std::min<int64_t>(v, INT32_MAX); };
+        P.unit_level_lo.resize((size_t)nunits);
+        P.unit_level_up.resize((size_t)nunits);
+        P.part_level_lo.resize((size_t)nparts);
+        for (int32_t u = 0; u < nunits; ++u) {
+            P.unit_level_lo[u] = clamp32(key_u[u]);
+            P.unit_level_up[u] = clamp32(key_up[u]);
+        }
+        for (int32_t q = 0; q < nparts; ++q) P.part_level_lo[q] = clamp32(key_p[q]);
+        const auto& lo = P.unit_level_lo;
+        const auto& lp = P.part_level_lo;
+        const auto& up = P.unit_level_up;
+        P.unit_order_lo.resize((size_t)nunits + nparts);
         P.unit_order_up.resize((size_t)nunits);
         for (int32_t u = 0; u < nunits; ++u) P.unit_order_lo[u] = P.unit_order_up[u] = u;
+        for (int32_t q = 0; q < nparts; ++q) P.unit_order_lo[nunits + q] = ~q;
+        auto key_lo = [&](int32_t item) { return item >= 0 ? lo[item] : lp[~item]; };
         std::stable_sort(P.unit_order_lo.begin(), P.unit_order_lo.end(),
-                         [&](int32_t a, int32_t b) { return lo[a] < lo[b]; });
+                         [&](int32_t a, int32_t b) { return key_lo(a) < key_lo(b); });
         std::stable_sort(P.unit_order_up.begin(), P.unit_order_up.end(),
                          [&](int32_t a, int32_t b) { return up[a] < up[b]; });
     }

@@ -20,8 +20,9 @@ struct SnContrib {
     int32_t xcol;       // first column (permuted index) of the source chunk
     int32_t nr;         // rows of the block (<= kChunk)
     int32_t w;          // columns of the block (<= kChunk)
-    int32_t src_unit;   // unit producing x_src (-1: same unit)
-    int32_t pad;
+    int32_t src_unit;   // unit producing x_src
+    uint32_t rowmask;   // bit p: the block has a row at unit row c0 + p (its
+                        // i-th row is the i-th set bit: rows are sorted)
 };
 
 // A chunk of <= kChunk consecutive columns of one top-region supernode.
@@ -31,11 +32,22 @@ struct SnUnit {
     int32_t pos0;           // position of column c0 in the supernode's row list
     int64_t panel_col_off;  // element offset of column c0 (row position 0) in the panel array
     int64_t rows_off;       // offset of the supernode's row list in sn_rows
-    int32_t contrib_begin;  // lower-sweep contributions [begin, end)
+    int32_t contrib_begin;  // lower-sweep contributions the unit applies itself [begin, end)
     int32_t contrib_end;
-    int32_t upper_dep;      // unit whose completion makes every row below the unit final
+    int32_t part_begin;     // lower-sweep partial sums the unit adds [begin, end)
     int32_t sn_w;           // width of the unit's supernode
-    int32_t parent_first_unit;  // first chunk of the parent supernode (-1: root)
+    int32_t part_end;
+    int32_t pad;
+};
+
+// A lower-sweep partial sum: the contributions [contrib_begin, contrib_end)
+// of one unit's list, summed by a separate work item into a 32-row buffer
+// slot. A unit hit by hundreds of source chunks (the chunks of a large
+// separator) would otherwise apply them all in one CTA, serially with its
+// dependency chain; its partial sums are ready as soon as their sources are.
+struct SnPartial {
+    int32_t unit;
+    int32_t contrib_begin, contrib_end;
     int32_t pad;
 };
 
@@ -51,10 +63,15 @@ struct SolvePlan {
     std::vector<double> panels;           // column-major panels (FP64; cast for FP32)
     std::vector<SnUnit> units;            // in lower topological order
     std::vector<SnContrib> contribs;
+    std::vector<SnPartial> parts;         // lower-sweep partial sums (by unit)
     std::vector<double> dinv;             // per unit: inverse of the diagonal block, 32x32 column-major
-    std::vector<int32_t> unit_order_lo;   // units sorted by lower-sweep dependency level
-    std::vector<int32_t> unit_order_up;   // units sorted by upper-sweep dependency level
-    std::vector<int32_t> unit_level_lo, unit_level_up;  // those levels, per unit
+    std::vector<int32_t> unit_order_lo;   // lower-sweep items in ticket order (sorted by key):
+                                          // unit u (>= 0) or partial sum p (~p)
+    std::vector<int32_t> unit_order_up;   // units in upper-sweep ticket order
+    // ticket-order keys (estimated start, ns; larger than the key of every
+    // item waited on): per unit, and per partial sum of the lower sweep
+    std::vector<int32_t> unit_level_lo, unit_level_up;
+    std::vector<int32_t> part_level_lo;
     std::vector<int32_t> unit_of_row;     // top rows: the unit holding the row (-1: leaf row)
     // leaf region, lower sweep: CSR over all rows. Leaf rows hold their full
     // row of L (diagonal last); top rows hold only their leaf-column entries.
@@ -76,6 +93,11 @@ struct SolvePlan {
 
 struct PlanOptions {
     int32_t min_top_width = 8;  // supernodes at least this wide (and their ancestors) are top
+    // units with more than part_keep + part_group contribution blocks keep
+    // their last part_keep blocks and hand the others to partial sums of
+    // about part_group blocks each (0: no partial sums)
+    int32_t part_keep = 16;
+    int32_t part_group = 32;
 };
 
 // Builds the plan from a factor and the level orders of L and L^T (rows

@@ -31,7 +31,8 @@ using namespace gbchol;
 
 namespace {
 
-// Maximum work array: n * nrhs * sizeof(element) bytes.
+// Maximum work array (work_bytes): about n * nrhs * sizeof(element) bytes,
+// plus the partial-sum slots of the supernodal lower sweep.
 constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -69,9 +70,9 @@ int gbchol_solve_noalloc(gbchol_handle h, int32_t precision, int32_t nrhs, const
     const bool f32 = precision == 0;
     if (!(h->store & (f32 ? GBCHOL_STORE_F32 : GBCHOL_STORE_F64)))
         return fail(GBCHOL_ESTATE, f32 ? "This solver keeps no FP32 factor." : "This solver keeps no FP64 factor.");
-    const size_t bytes = (size_t)h->n * (size_t)nrhs * (f32 ? sizeof(float) : sizeof(double));
+    const size_t bytes = work_bytes(h, nrhs, f32);
     if (bytes > kNoAllocScratchBytes)
-        return fail(GBCHOL_EINVAL, "gbchol_solve_noalloc: n * nrhs * element size (" + std::to_string(bytes) +
+        return fail(GBCHOL_EINVAL, "gbchol_solve_noalloc: the solve's work array (" + std::to_string(bytes) +
                                        " bytes) exceeds the 16 MiB static work array; use gbchol_solve.");
     if (h->n == 0) return GBCHOL_OK;
     if (!b || !x) return fail(GBCHOL_EINVAL, "Null b or x.");

@@ -11,15 +11,19 @@
 //   (block b -> warp b % 8). The warp waits for the source unit's flag,
 //   stages x_source (<= 32 x 32) in its own shared-memory slice, and each
 //   lane accumulates its row of L_block x_source in registers. The rows of a
-//   block are a sorted subset of the unit's rows, so lane p reads block row
-//   inv[p] directly (no scatter). The warps' partial sums are reduced in a
-//   fixed order, subtracted from t (b minus leaf terms), and the 32x32
-//   diagonal block is solved with warp shuffles (one lane per row).
+//   block are a sorted subset of the unit's rows, given as a 32-bit mask, so
+//   lane p reads block row popc(mask below p) directly (no scatter). Long
+//   block lists are cut into partial-sum items (other CTAs, started as soon
+//   as their sources are done); the unit adds their sums. The warps' sums
+//   are reduced in a fixed order, subtracted from t (b minus leaf terms),
+//   and the 32x32 diagonal block is solved (one lane per row).
 // Upper sweep (L^T x = y): the rows below the unit's diagonal block are cut
-//   into 32-row blocks: the supernode's off-diagonal rows first (ready once
-//   the parent supernode's first chunk is done; one wait), then the later
-//   chunks of the same supernode from the last one down (one wait each), so
-//   only the newest 32-row block sits on the dependency chain. Lane j holds
+//   into 32-row blocks: the supernode's off-diagonal rows first, highest
+//   block first, then the later chunks of the same supernode from the last
+//   one down. Each block waits for one unit only: the off-diagonal rows of a
+//   supernode lie on one etree path, and the unit holding a block's lowest
+//   row finishes after every higher row of the path; so only the newest
+//   32-row block sits on the dependency chain. Lane j holds
 //   column j of the unit and accumulates L[block, j]^T x_block; then the same
 //   fixed-order reduction and a transposed shuffle solve.
 // The diagonal solve of a unit is one product with the precomputed inverse
@@ -66,7 +70,6 @@ struct SnSmem {
     __align__(16) T xs[kWarps][kW][XS];  // per-warp staging of x blocks; reused for the reduction
     T t[kW][KW + 1];           // reduced right-hand side of the unit
     T d[kW][kW + 1];           // diagonal block
-    int inv[kWarps][kW];       // unit row -> block row (lower sweep)
 };
 
 // acc[k] += a * row[k] for k < KW, reading `row` (16-byte aligned shared
@@ -103,33 +106,31 @@ __device__ __forceinline__ void warp_wait(const int* flag, int epoch, int* statu
 // One warp's share of a lower-sweep block: inner columns [j0, j0 + J) of
 // L[unit rows, source chunk] times the matching rows of x_source, added into
 // acc (lane = unit row). J = 32: the whole block; J = 4: an eighth (the block
-// on the dependency chain is split across the 8 warps).
+// on the dependency chain is split across the 8 warps). Lane p holds block
+// row popc(rowmask below p) when bit p of rowmask is set. `ready`: the
+// source's flag was already seen set (no wait).
 template <typename T, int KW, int J>
-__device__ __forceinline__ void lower_block(const SnSys& d, const SnContrib& C, const SnUnit& U,
-                                            int j0, int slice, int k0, int kw, int epoch,
-                                            int* status, int lane, int* inv, T (*xs)[XsStride<T, KW>::value],
-                                            T (&acc)[KW]) {
+__device__ __forceinline__ void lower_block(const SnSys& d, long long panel_off, int ld, int xcol, int w,
+                                            int src_unit, unsigned rowmask, bool ready, int j0, int slice,
+                                            int k0, int kw, int epoch, int* status, int lane,
+                                            T (*xs)[XsStride<T, KW>::value], T (&acc)[KW]) {
     const T* __restrict__ panels = static_cast<const T*>(d.panels);
     const T* tmp = static_cast<const T*>(d.tmp);
     const int nrhs = d.nrhs;
-    if (lane < C.nr) inv[d.sn_rows[C.rows_off + lane] - U.c0] = lane;
-    __syncwarp();
-    const int src = inv[lane];
-    __syncwarp();
-    inv[lane] = -1;
+    const bool hit = (rowmask >> lane) & 1u;
+    const int src = __popc(rowmask & ((1u << lane) - 1u));
     // L is constant: its loads go out before the flag wait
     T lv[J];
-    const T* Lp = panels + C.panel_off + src;
+    const T* Lp = panels + panel_off + src;
 #pragma unroll
-    for (int j = 0; j < J; ++j)
-        lv[j] = (src >= 0 && j0 + j < C.w) ? __ldg(Lp + (size_t)(j0 + j) * C.ld) : T(0);
-    warp_wait(d.uflags + (size_t)C.src_unit * d.nslices + slice, epoch, status, lane);
+    for (int j = 0; j < J; ++j) lv[j] = (hit && j0 + j < w) ? __ldg(Lp + (size_t)(j0 + j) * ld) : T(0);
+    if (!ready) warp_wait(d.uflags + (size_t)src_unit * d.nslices + slice, epoch, status, lane);
     constexpr int PER = J * KW / 32;
     T xv[PER];
 #pragma unroll
     for (int u = 0; u < PER; ++u) {
         const int idx = lane + 32 * u, j = j0 + idx / KW, k = idx % KW;
-        xv[u] = (j < C.w && k < kw) ? __ldcg(tmp + (size_t)(C.xcol + j) * nrhs + k0 + k) : T(0);
+        xv[u] = (j < w && k < kw) ? __ldcg(tmp + (size_t)(xcol + j) * nrhs + k0 + k) : T(0);
     }
 #pragma unroll
     for (int u = 0; u < PER; ++u) {
@@ -137,13 +138,66 @@ __device__ __forceinline__ void lower_block(const SnSys& d, const SnContrib& C, 
         xs[idx / KW][idx % KW] = xv[u];
     }
     __syncwarp();
-    const int jn = min(J, C.w - j0);  // warp-uniform
+    const int jn = min(J, w - j0);  // warp-uniform
 #pragma unroll
     for (int j = 0; j < J; ++j) {
         if (j >= jn) break;
         axpy_row<KW>(acc, lv[j], xs[j]);
     }
     __syncwarp();
+}
+
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// One warp's blocks first, first + 8, ... < end of a lower-sweep block list,
+// whole blocks. They go in groups of up to 32: lane k loads the descriptor
+// of the group's k-th block and checks its source's flag (one round trip for
+// the group), the descriptors are broadcast by shuffles, and the next
+// block's L columns are prefetched into L2 while the current one is applied.
+template <typename T, int KW>
+__device__ __forceinline__ void lower_list(const SnSys& d, int first, int end, int slice, int k0, int kw,
+                                           int epoch, int* status, int lane,
+                                           T (*xs)[XsStride<T, KW>::value], T (&acc)[KW]) {
+    const T* __restrict__ panels = static_cast<const T*>(d.panels);
+    for (int g = first; g < end; g += 32 * kWarps) {
+        const int mb = g + lane * kWarps;
+        long long poff = 0;
+        int ld = 0, xcol = 0, w = 0, nr = 0, srcu = 0;
+        unsigned mask = 0;
+        int ready = 1;
+        if (mb < end) {
+            const SnContrib& C = d.contribs[mb];
+            poff = C.panel_off;
+            ld = C.ld;
+            xcol = C.xcol;
+            w = C.w;
+            nr = C.nr;
+            srcu = C.src_unit;
+            mask = C.rowmask;
+            ready = dev::ld_acquire(d.uflags + (size_t)srcu * d.nslices + slice) >= epoch;
+        }
+        __syncwarp();  // orders the lanes' flag observations before every lane's loads
+        const int cnt = min(32, (end - g + kWarps - 1) / kWarps);
+        for (int k = 0; k < cnt; ++k) {
+            if (k + 1 < cnt) {
+                const long long np = __shfl_sync(0xffffffffu, poff, k + 1);
+                const int nld = __shfl_sync(0xffffffffu, ld, k + 1);
+                const int nw = __shfl_sync(0xffffffffu, w, k + 1);
+                const int nnr = __shfl_sync(0xffffffffu, nr, k + 1);
+                if (lane < nw) {
+                    prefetch_l2(panels + np + (size_t)lane * nld);
+                    prefetch_l2(panels + np + nnr - 1 + (size_t)lane * nld);
+                }
+            }
+            lower_block<T, KW, kW>(d, __shfl_sync(0xffffffffu, poff, k), __shfl_sync(0xffffffffu, ld, k),
+                                   __shfl_sync(0xffffffffu, xcol, k), __shfl_sync(0xffffffffu, w, k),
+                                   __shfl_sync(0xffffffffu, srcu, k), __shfl_sync(0xffffffffu, mask, k),
+                                   __shfl_sync(0xffffffffu, ready, k) != 0, 0, slice, k0, kw, epoch, status,
+                                   lane, xs, acc);
+        }
+    }
 }
 
 // One warp's share of an upper-sweep block: rows [i0, i0 + J) of the 32-row
@@ -196,7 +250,6 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
     // every CTA reads the sweep's epoch before the last CTA out bumps it
     const int epoch = dev::ld_volatile(a.epoch);
     T (*xs)[XsStride<T, KW>::value] = sm.xs[warp];
-    if (LOWER) sm.inv[warp][lane] = -1;
     __shared__ int ticket, s_uidx, s_slice;
     __shared__ SnSys dsm;
     for (;;) {
@@ -207,8 +260,13 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
                 if (a.item_sys) {
                     dsm = a.sys[a.item_sys[it]];
                     const int code = a.item_code[it];
-                    s_uidx = code >> 3;
-                    s_slice = code & 7;
+                    if (code >= 0) {
+                        s_uidx = code >> 3;
+                        s_slice = code & 7;
+                    } else {  // partial sum
+                        s_uidx = ~(((-code) >> 3) - 1);
+                        s_slice = (-code) & 7;
+                    }
                 } else {
                     dsm = a.sys0;
                     s_uidx = a.order[it / a.sys0.nslices];
@@ -225,11 +283,14 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
         const int nrhs = d.nrhs;
         const int k0 = slice * KW;
         const int kw = min(KW, nrhs - k0);
-        const SnUnit U = d.units[uidx];
+        // a lower-sweep partial sum: the item is ~p
+        const bool part = LOWER && uidx < 0;
+        const SnPartial PS = part ? d.parts[~uidx] : SnPartial{};
+        const SnUnit U = d.units[part ? PS.unit : uidx];
         const int w = U.w;
         // off the dependency chain: the unit's current right-hand side and
         // its inverse diagonal block go to shared memory first
-        {
+        if (!part) {
             const T* __restrict__ dinv = static_cast<const T*>(d.dinv) + (size_t)uidx * kW * kW;
             for (int idx = tid; idx < kW * kW; idx += kT) sm.d[idx & 31][idx >> 5] = dinv[idx];
             for (int idx = tid; idx < kW * KW; idx += kT) {
@@ -245,18 +306,26 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
         // the same supernode, listed last; upper: from the next chunk, taken
         // last) is split across all 8 warps; the others go one per warp.
         constexpr int kSplit = kW / kWarps;
-        if (LOWER) {
+        if (part) {
+            lower_list<T, KW>(d, PS.contrib_begin + warp, PS.contrib_end, slice, k0, kw, epoch, a.status, lane,
+                              xs, acc);
+        } else if (LOWER) {
+            // the unit's partial sums, one per warp in turn (slot row = lane)
+            for (int q = U.part_begin + warp; q < U.part_end; q += kWarps) {
+                warp_wait(d.uflags + (size_t)(d.n_units + q) * d.nslices + slice, epoch, a.status, lane);
+                const T* ps = static_cast<const T*>(d.pbuf) + ((size_t)q * d.nslices + slice) * (kW * KW) + lane * KW;
+#pragma unroll
+                for (int k = 0; k < KW; ++k) acc[k] += __ldcg(ps + k);
+            }
             const int nb = U.contrib_end - U.contrib_begin;
             const bool split = nb > 0 && U.pos0 > 0 && d.contribs[U.contrib_end - 1].src_unit == uidx - 1;
             const int nfree = split ? nb - 1 : nb;
-            for (int b = warp; b < nfree; b += kWarps) {
-                const SnContrib C = d.contribs[U.contrib_begin + b];
-                lower_block<T, KW, kW>(d, C, U, 0, slice, k0, kw, epoch, a.status, lane, sm.inv[warp], xs, acc);
-            }
+            lower_list<T, KW>(d, U.contrib_begin + warp, U.contrib_begin + nfree, slice, k0, kw, epoch, a.status,
+                              lane, xs, acc);
             if (split) {
                 const SnContrib C = d.contribs[U.contrib_end - 1];
-                lower_block<T, KW, kSplit>(d, C, U, warp * kSplit, slice, k0, kw, epoch, a.status, lane,
-                                           sm.inv[warp], xs, acc);
+                lower_block<T, KW, kSplit>(d, C.panel_off, C.ld, C.xcol, C.w, C.src_unit, C.rowmask, false,
+                                           warp * kSplit, slice, k0, kw, epoch, a.status, lane, xs, acc);
             }
         } else {
             // block list: off-diagonal rows of the supernode in 32-row blocks,
@@ -295,6 +364,22 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
 #pragma unroll
         for (int k = 0; k < KW; ++k) xs[lane][k] = acc[k];
         __syncthreads();
+        if (part) {  // the sum goes to the partial's slot, then its flag
+            T* ps = static_cast<T*>(d.pbuf) + ((size_t)(~uidx) * d.nslices + slice) * (kW * KW);
+            for (int idx = tid; idx < kW * KW; idx += kT) {
+                const int i = idx / KW, k = idx % KW;
+                T v = T(0);
+#pragma unroll
+                for (int ww = 0; ww < kWarps; ++ww) v += sm.xs[ww][i][k];
+                ps[idx] = v;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                __threadfence();
+                dev::st_release(d.uflags + (size_t)(d.n_units + ~uidx) * d.nslices + slice, epoch);
+            }
+            continue;
+        }
         for (int idx = tid; idx < kW * KW; idx += kT) {
             const int i = idx / KW, k = idx % KW;
             T s = T(0);
@@ -368,6 +453,16 @@ cudaError_t launch_sn_io(const SnSweepArgs& a, cudaStream_t stream) {
 int sn_slices(int nrhs, bool f64) {
     const int wide = f64 ? 16 : 32;
     return nrhs <= 8 ? 1 : (nrhs + wide - 1) / wide;
+}
+
+int sn_slice_width(int nrhs, bool f64, bool wide) {
+    return (!wide && nrhs <= 8) ? 8 : (f64 ? 16 : 32);
+}
+
+size_t sn_pbuf_bytes(int nparts, int nrhs, bool f64, bool wide) {
+    const int kw = sn_slice_width(nrhs, f64, wide);
+    const int ns = (nrhs + kw - 1) / kw;
+    return (size_t)nparts * ns * kChunk * kw * (f64 ? sizeof(double) : sizeof(float));
 }
 
 cudaError_t launch_sn_sweep(const SnSweepArgs& a, bool lower, SweepIO io, cudaStream_t stream) {

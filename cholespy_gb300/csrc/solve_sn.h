@@ -19,6 +19,9 @@ struct SnSys {
     void* out = nullptr;            // upper: solution through perm (TOut)
     int* uflags = nullptr;          // n_units * nslices completion flags
     const int32_t* unit_of_row = nullptr;  // unit holding each top row (upper sweep waits)
+    const SnPartial* parts = nullptr;      // lower-sweep partial sums
+    void* pbuf = nullptr;           // T, partial-sum slots: (part, slice) -> 32 x slice width
+    int n_units = 0;                // partial p's flags follow the units': (n_units + p, slice)
     int nrhs = 0;
     int nslices = 1;                // RHS slices (see sn_slices)
 };
@@ -28,7 +31,7 @@ struct SnSweepArgs {
     const SnSys* sys = nullptr;     // device table of systems (batched sweep)
     const int32_t* order = nullptr; // single system: units in dependency-level order
     const int32_t* item_sys = nullptr;   // batched: system of each item
-    const int32_t* item_code = nullptr;  // batched: (unit << 3) | RHS slice of each item
+    const int32_t* item_code = nullptr;  // batched: sn_item_code(item, slice) of each item
     int nitems = 0;
     int wide = 0;                   // 1: use the wide-RHS variant for every system (batched)
     int* epoch = nullptr;           // device sweep counter: read at start, +1 by the last CTA out
@@ -39,6 +42,15 @@ struct SnSweepArgs {
 
 // RHS slices of one sweep: 1 for <= 8 RHS, else 32-wide (FP32) or 16-wide (FP64).
 int sn_slices(int nrhs, bool f64);
+// Width of one RHS slice: 8 for a single narrow slice, else 32 (FP32) or 16 (FP64).
+int sn_slice_width(int nrhs, bool f64, bool wide);
+// Bytes of the partial-sum slots of `nparts` partial sums.
+size_t sn_pbuf_bytes(int nparts, int nrhs, bool f64, bool wide);
+
+// Batched item code: item is a unit (>= 0) or ~partial.
+inline int32_t sn_item_code(int32_t item, int32_t slice) {
+    return item >= 0 ? (item << 3) | slice : -((((~item) + 1) << 3) | slice);
+}
 cudaError_t launch_sn_sweep(const SnSweepArgs& a, bool lower, SweepIO io, cudaStream_t stream);
 
 }  // namespace gbchol

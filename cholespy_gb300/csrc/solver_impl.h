@@ -30,6 +30,9 @@ struct gbchol_solver;
 namespace gbchol {
 // One full solve (leaf lower, supernodal lower, supernodal upper, top-row
 // terms, leaf upper) with `work` as the permuted-space work array.
+// Bytes of the work array of one solve: the permuted-space copy of the RHS
+// (n x nrhs, 256-byte aligned) followed by the partial-sum slots.
+size_t work_bytes(const gbchol_solver* h, int nrhs, bool f32);
 int run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in, void* out,
                     const int* skip, void* work, cudaStream_t s);
 }  // namespace gbchol
@@ -121,6 +124,7 @@ struct gbchol_solver {
     DevBuf<double> lo_v64, up_v64, pan64, upt_v64;
     DevBuf<SnUnit> units;
     DevBuf<SnContrib> contribs;
+    DevBuf<SnPartial> parts;             // lower-sweep partial sums
     DevBuf<int32_t> uflags;   // units * RHS slices
     DevBuf<int32_t> order_lo, order_up;  // units in dependency-level order
     DevBuf<int32_t> unit_of_row;         // unit holding each top row

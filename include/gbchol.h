@@ -131,7 +131,9 @@ int gbchol_solve(gbchol_handle h, int32_t precision, int32_t nrhs, const void* b
  * a call brings more RHS than any before; this call allocates nothing. Its
  * work array is a fixed 16 MiB file-scope device array that every GPU
  * loading the library holds until exit, so it fails with GBCHOL_EINVAL when
- * n * nrhs * element size (4 bytes FP32, 8 FP64) exceeds 16 MiB. The first
+ * the solve's work array exceeds 16 MiB: n * nrhs * element size (4 bytes
+ * FP32, 8 FP64), plus 32 * nrhs * element size (rounded up to the RHS slice
+ * width) per partial sum of the supernodal lower sweep. The first
  * call on a device looks up the array's device address; make it outside any
  * stream capture. All calls share the array, so calls that overlap on the
  * GPU race: serialise them. Same arguments and results as gbchol_solve.

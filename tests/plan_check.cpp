@@ -1,0 +1,319 @@
+// Host-side check of the solve plan (cholespy_gb300/csrc/host/plan.cpp): runs
+// every sweep of a solve on the CPU in FP64, item by item in the order the
+// GPU kernels hand out their tickets, and checks
+//   - that every flag an item waits on belongs to an item with an earlier
+//     ticket (the persistent kernels are deadlock-free only then) that wrote
+//     the values the item reads,
+//   - the partial-sum items of the lower sweep and the per-block waits of the
+//     upper sweep,
+//   - the solution against a plain column-oriented solve with the factor.
+// Built and run by tests/test_plan.py. Exit status 0 = all cases pass.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "host.h"
+#include "plan.h"
+
+using namespace gbchol;
+
+namespace {
+
+int errors = 0;
+#define CHECK(c)                                                        \
+    do {                                                                \
+        if (!(c)) {                                                     \
+            if (errors < 10) std::printf("check failed: %s (line %d)\n", #c, __LINE__); \
+            ++errors;                                                   \
+        }                                                               \
+    } while (0)
+
+// Rows of L sorted by (level, row): the level orders the analysis produces.
+std::vector<int32_t> level_order(int32_t n, const std::vector<int32_t>& rp, const std::vector<int32_t>& ci,
+                                 bool lower) {
+    std::vector<int32_t> lev((size_t)n, 0);
+    int32_t mx = 0;
+    for (int32_t t = 0; t < n; ++t) {
+        const int32_t row = lower ? t : n - 1 - t;
+        const int32_t lo = lower ? rp[row] : rp[row] + 1, hi = lower ? rp[row + 1] - 1 : rp[row + 1];
+        int32_t l = 0;
+        for (int32_t k = lo; k < hi; ++k) l = std::max(l, lev[ci[k]] + 1);
+        lev[row] = l;
+        mx = std::max(mx, l);
+    }
+    std::vector<int32_t> ord((size_t)n);
+    for (int32_t i = 0; i < n; ++i) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return lev[a] < lev[b]; });
+    return ord;
+}
+
+// One solve through the plan; returns the relative error against the plain solve.
+double run_case(const Factor& F, const SolvePlan& P, int r) {
+    const int32_t n = F.n;
+    std::mt19937 g(7);
+    std::normal_distribution<double> N;
+    std::vector<double> b((size_t)n * r), tmp((size_t)n * r, 0.0), out((size_t)n * r, 0.0);
+    for (auto& v : b) v = N(g);
+    // reference: y = L^{-1} P b, x = P^T L^{-T} y
+    std::vector<double> y((size_t)n * r);
+    for (int32_t i = 0; i < n; ++i)
+        for (int k = 0; k < r; ++k) y[(size_t)i * r + k] = b[(size_t)F.perm[i] * r + k];
+    for (int32_t c = 0; c < n; ++c)
+        for (int k = 0; k < r; ++k) {
+            const double yc = y[(size_t)c * r + k] / F.vals[F.colptr[c]];
+            y[(size_t)c * r + k] = yc;
+            for (int32_t p = F.colptr[c] + 1; p < F.colptr[c + 1]; ++p) y[(size_t)F.rowidx[p] * r + k] -= F.vals[p] * yc;
+        }
+    std::vector<double> xr = y;
+    for (int32_t c = n - 1; c >= 0; --c)
+        for (int k = 0; k < r; ++k) {
+            double v = xr[(size_t)c * r + k];
+            for (int32_t p = F.colptr[c] + 1; p < F.colptr[c + 1]; ++p) v -= F.vals[p] * xr[(size_t)F.rowidx[p] * r + k];
+            xr[(size_t)c * r + k] = v / F.vals[F.colptr[c]];
+        }
+    std::vector<double> ref((size_t)n * r);
+    for (int32_t i = 0; i < n; ++i)
+        for (int k = 0; k < r; ++k) ref[(size_t)F.perm[i] * r + k] = xr[(size_t)i * r + k];
+
+    // ---- lower leaf rows (row kernel): leaf rows solve, top rows get partial terms
+    std::vector<char> row_done((size_t)n, 0);
+    for (int32_t task : P.lo_tasks) {
+        const bool partial = task < 0;
+        const int32_t row = partial ? ~task : task;
+        CHECK(partial == (bool)P.row_top[row]);
+        const int32_t s = P.lo_rowptr[row], e = P.lo_rowptr[row + 1];
+        const int32_t hi = partial ? e : e - 1;
+        for (int k = 0; k < r; ++k) {
+            double acc = 0.0;
+            for (int32_t p = s; p < hi; ++p) {
+                const int32_t c = P.lo_cols[p];
+                CHECK(!P.row_top[c] && row_done[c]);
+                acc += P.lo_vals[p] * tmp[(size_t)c * r + k];
+            }
+            double v = b[(size_t)F.perm[row] * r + k] - acc;
+            if (!partial) v /= P.lo_vals[e - 1];
+            tmp[(size_t)row * r + k] = v;
+        }
+        if (!partial) row_done[row] = 1;
+    }
+    // ---- lower supernodal sweep, items in ticket order
+    const int32_t nunits = (int32_t)P.units.size(), nparts = (int32_t)P.parts.size();
+    std::vector<char> unit_done((size_t)nunits, 0), part_done((size_t)nparts, 0);
+    std::vector<double> pbuf((size_t)nparts * kChunk * r, 0.0);
+    CHECK((int32_t)P.unit_order_lo.size() == nunits + nparts);
+    auto apply = [&](const SnUnit& U, const SnContrib& C, double* acc) {
+        CHECK(C.src_unit >= 0 && C.src_unit < nunits && unit_done[C.src_unit]);
+        CHECK(C.nr >= 1 && C.nr <= kChunk && C.w >= 1 && C.w <= kChunk);
+        uint32_t mask = 0;
+        for (int32_t i = 0; i < C.nr; ++i) {
+            const int32_t pos = P.sn_rows[C.rows_off + i] - U.c0;
+            CHECK(pos >= 0 && pos < U.w);
+            if (pos < 0 || pos >= U.w) continue;
+            mask |= 1u << pos;
+            // the kernel's lane pos reads block row popc(mask below pos)
+            CHECK(__builtin_popcount(C.rowmask & ((1u << pos) - 1u)) == i);
+            for (int k = 0; k < r; ++k) {
+                double s = 0.0;
+                for (int32_t j = 0; j < C.w; ++j)
+                    s += P.panels[C.panel_off + i + (size_t)j * C.ld] * tmp[(size_t)(C.xcol + j) * r + k];
+                acc[(size_t)pos * r + k] += s;
+            }
+        }
+        CHECK(mask == C.rowmask);
+    };
+    for (int32_t item : P.unit_order_lo) {
+        if (item < 0) {
+            const SnPartial& Q = P.parts[~item];
+            CHECK(!part_done[~item]);
+            const SnUnit& U = P.units[Q.unit];
+            CHECK(Q.contrib_begin >= 0 && Q.contrib_begin < Q.contrib_end);
+            for (int32_t e = Q.contrib_begin; e < Q.contrib_end; ++e) apply(U, P.contribs[e], &pbuf[(size_t)(~item) * kChunk * r]);
+            part_done[~item] = 1;
+            continue;
+        }
+        const SnUnit& U = P.units[item];
+        CHECK(!unit_done[item]);
+        std::vector<double> acc((size_t)kChunk * r, 0.0);
+        for (int32_t q = U.part_begin; q < U.part_end; ++q) {
+            CHECK(part_done[q] && P.parts[q].unit == item);
+            for (size_t t = 0; t < acc.size(); ++t) acc[t] += pbuf[(size_t)q * kChunk * r + t];
+        }
+        for (int32_t e = U.contrib_begin; e < U.contrib_end; ++e) apply(U, P.contribs[e], acc.data());
+        // the partial sums and the unit's own blocks cover its whole list
+        if (U.part_begin < U.part_end) {
+            CHECK(P.parts[U.part_end - 1].contrib_end == U.contrib_begin);
+            for (int32_t q = U.part_begin + 1; q < U.part_end; ++q)
+                CHECK(P.parts[q].contrib_begin == P.parts[q - 1].contrib_end);
+        }
+        for (int32_t i = 0; i < U.w; ++i) {
+            CHECK(P.row_top[U.c0 + i]);
+            for (int k = 0; k < r; ++k) tmp[(size_t)(U.c0 + i) * r + k] -= acc[(size_t)i * r + k];
+        }
+        for (int k = 0; k < r; ++k)
+            for (int32_t j = 0; j < U.w; ++j) {
+                const double xj = tmp[(size_t)(U.c0 + j) * r + k] / P.panels[U.panel_col_off + U.pos0 + j + (size_t)j * U.ld];
+                tmp[(size_t)(U.c0 + j) * r + k] = xj;
+                for (int32_t i = j + 1; i < U.w; ++i)
+                    tmp[(size_t)(U.c0 + i) * r + k] -= P.panels[U.panel_col_off + U.pos0 + i + (size_t)j * U.ld] * xj;
+            }
+        unit_done[item] = 1;
+    }
+    for (int32_t u = 0; u < nunits; ++u) CHECK(unit_done[u]);
+    {
+        double m = 0.0, mm = 0.0;
+        for (size_t q = 0; q < y.size(); ++q) {
+            m = std::max(m, std::fabs(y[q] - tmp[q]));
+            mm = std::max(mm, std::fabs(y[q]));
+        }
+        CHECK(m <= 1e-9 * mm);
+    }
+    // ---- upper supernodal sweep, items in ticket order; a block of rows may
+    // read only rows whose unit finished, and it waits on one unit only
+    std::vector<char> udone((size_t)nunits, 0), rdone((size_t)n, 0);
+    CHECK((int32_t)P.unit_order_up.size() == nunits);
+    for (int32_t u : P.unit_order_up) {
+        const SnUnit& U = P.units[u];
+        const int32_t* rows = P.sn_rows.data() + U.rows_off;
+        // blocks and the one unit each waits on (as the kernel lists them)
+        for (int32_t p0 = U.sn_w; p0 < U.ld; p0 += kChunk) {
+            const int32_t dep = P.unit_of_row[rows[p0]];
+            CHECK(dep > u && udone[dep]);
+            for (int32_t p = p0; p < std::min(U.ld, p0 + kChunk); ++p) CHECK(rdone[rows[p]]);
+        }
+        const int32_t wj = U.pos0 + U.w;
+        for (int32_t c = 0; wj + c * kChunk < U.sn_w; ++c) {
+            CHECK(u + 1 + c < nunits && udone[u + 1 + c]);
+            CHECK(P.units[u + 1 + c].c0 == U.c0 + U.w + c * kChunk);
+        }
+        std::vector<double> t((size_t)U.w * r);
+        for (int32_t j = 0; j < U.w; ++j)
+            for (int k = 0; k < r; ++k) t[(size_t)j * r + k] = tmp[(size_t)(U.c0 + j) * r + k];
+        for (int32_t p = wj; p < U.ld; ++p)
+            for (int32_t j = 0; j < U.w; ++j)
+                for (int k = 0; k < r; ++k)
+                    t[(size_t)j * r + k] -= P.panels[U.panel_col_off + p + (size_t)j * U.ld] * tmp[(size_t)rows[p] * r + k];
+        for (int k = 0; k < r; ++k)
+            for (int32_t j = U.w - 1; j >= 0; --j) {
+                const double xj = t[(size_t)j * r + k] / P.panels[U.panel_col_off + U.pos0 + j + (size_t)j * U.ld];
+                t[(size_t)j * r + k] = xj;
+                for (int32_t i = 0; i < j; ++i)
+                    t[(size_t)i * r + k] -= P.panels[U.panel_col_off + U.pos0 + j + (size_t)i * U.ld] * xj;
+            }
+        for (int32_t j = 0; j < U.w; ++j) {
+            for (int k = 0; k < r; ++k) {
+                tmp[(size_t)(U.c0 + j) * r + k] = t[(size_t)j * r + k];
+                out[(size_t)F.perm[U.c0 + j] * r + k] = t[(size_t)j * r + k];
+            }
+            rdone[U.c0 + j] = 1;
+        }
+        udone[u] = 1;
+    }
+    // ---- upper leaf rows: top-row terms (no waits), then the chained pass
+    for (int32_t task : P.upt_tasks) {
+        const int32_t row = ~task;
+        CHECK(row >= 0 && !P.row_top[row]);
+        for (int k = 0; k < r; ++k) {
+            double acc = 0.0;
+            for (int32_t p = P.upt_rowptr[row]; p < P.upt_rowptr[row + 1]; ++p) {
+                const int32_t c = P.upt_cols[p];
+                CHECK(P.row_top[c] && rdone[c]);
+                acc += P.upt_vals[p] * tmp[(size_t)c * r + k];
+            }
+            tmp[(size_t)row * r + k] -= acc;
+        }
+    }
+    for (int32_t row : P.up_tasks) {
+        const int32_t s = P.upl_rowptr[row], e = P.upl_rowptr[row + 1];
+        CHECK(P.upl_cols[s] == row);
+        for (int k = 0; k < r; ++k) {
+            double acc = 0.0;
+            for (int32_t p = s + 1; p < e; ++p) {
+                const int32_t c = P.upl_cols[p];
+                CHECK(rdone[c] && !P.row_top[c]);
+                acc += P.upl_vals[p] * tmp[(size_t)c * r + k];
+            }
+            const double v = (tmp[(size_t)row * r + k] - acc) / P.upl_vals[s];
+            tmp[(size_t)row * r + k] = v;
+            out[(size_t)F.perm[row] * r + k] = v;
+        }
+        rdone[row] = 1;
+    }
+    for (int32_t i = 0; i < n; ++i) CHECK(rdone[i]);
+    double m = 0.0, mm = 0.0;
+    for (size_t q = 0; q < out.size(); ++q) {
+        m = std::max(m, std::fabs(out[q] - ref[q]));
+        mm = std::max(mm, std::fabs(ref[q]));
+    }
+    return m / mm;
+}
+
+// 2-D 5-point or 3-D 7-point grid Laplacian plus a diagonal shift (COO).
+void grid(int dim, int k, std::vector<int32_t>& ii, std::vector<int32_t>& jj, std::vector<double>& xx) {
+    auto id = [&](int a, int b, int c) { return dim == 3 ? (a * k + b) * k + c : a * k + b; };
+    for (int a = 0; a < k; ++a)
+        for (int b = 0; b < k; ++b)
+            for (int c = 0; c < (dim == 3 ? k : 1); ++c) {
+                const int i = id(a, b, c);
+                ii.push_back(i); jj.push_back(i); xx.push_back(2.0 * dim + 0.1);
+                const int nb[6][3] = {{a + 1, b, c}, {a - 1, b, c}, {a, b + 1, c}, {a, b - 1, c}, {a, b, c + 1}, {a, b, c - 1}};
+                for (int t = 0; t < 2 * dim; ++t) {
+                    const int A = nb[t][0], B = nb[t][1], C = nb[t][2];
+                    if (A < 0 || A >= k || B < 0 || B >= k || C < 0 || C >= (dim == 3 ? k : 1)) continue;
+                    ii.push_back(i); jj.push_back(id(A, B, C)); xx.push_back(-1.0);
+                }
+            }
+}
+
+}  // namespace
+
+int main() {
+    struct Case { int dim, k, minw, keep, group; };
+    const Case cases[] = {
+        {2, 8, 1, 16, 32},  {2, 20, 4, 16, 32}, {2, 20, 8, 2, 3},   {2, 40, 1, 1, 2},
+        {3, 8, 1, 2, 3},    {3, 14, 4, 16, 32}, {3, 14, 8, 4, 5},   {3, 18, 8, 16, 32},
+        {3, 18, 8, 0, 0},   {3, 14, 100000, 16, 32},
+    };
+    int failed = 0;
+    for (const Case& cs : cases) {
+        std::vector<int32_t> ii, jj;
+        std::vector<double> xx;
+        grid(cs.dim, cs.k, ii, jj, xx);
+        const int32_t n = cs.dim == 3 ? cs.k * cs.k * cs.k : cs.k * cs.k;
+        Csc A;
+        std::string err;
+        if (build_csc(n, (int64_t)xx.size(), ii.data(), jj.data(), xx.data(), FMT_COO, A, err)) {
+            std::printf("build_csc: %s\n", err.c_str());
+            return 1;
+        }
+        Factor F;
+        FactorOptions fo;
+        if (factorize(A, fo, F, err)) {
+            std::printf("factorize: %s\n", err.c_str());
+            return 1;
+        }
+        std::vector<int32_t> rp, ci;
+        std::vector<double> rv;
+        transpose(n, F.colptr, F.rowidx, F.vals, rp, ci, rv);
+        const auto lo = level_order(n, rp, ci, true), up = level_order(n, F.colptr, F.rowidx, false);
+        SolvePlan P;
+        PlanOptions po;
+        po.min_top_width = cs.minw;
+        po.part_keep = cs.keep;
+        po.part_group = cs.group;
+        build_plan(F, lo, up, po, P);
+        for (int r : {1, 3}) {
+            errors = 0;
+            const double rel = run_case(F, P, r);
+            const bool ok = errors == 0 && rel < 1e-10;
+            std::printf("%dD k=%d minw=%d keep=%d group=%d r=%d: units %zu parts %zu rel err %.2e checks failed %d %s\n",
+                        cs.dim, cs.k, cs.minw, cs.keep, cs.group, r, P.units.size(), P.parts.size(), rel, errors,
+                        ok ? "ok" : "FAIL");
+            failed += !ok;
+        }
+    }
+    return failed ? 1 : 0;
+}
