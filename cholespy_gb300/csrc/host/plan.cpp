@@ -140,8 +140,9 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
         U.contrib_begin = b0;
         U.contrib_end = b0 + nb;
         U.part_begin = U.part_end = (int32_t)P.parts.size();
-        if (opt.part_group > 0 && nb > opt.part_keep + opt.part_group) {
-            const int32_t m = nb - opt.part_keep;
+        const int32_t keep = std::max(opt.part_keep, 1);  // the chain block stays with the unit
+        if (opt.part_group > 0 && nb > keep + opt.part_group) {
+            const int32_t m = nb - keep;
             const int32_t ng = (m + opt.part_group - 1) / opt.part_group;
             for (int32_t g = 0; g < ng; ++g) {
                 SnPartial q{};
@@ -155,19 +156,49 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
         }
     }
 
-    // inverses of the diagonal blocks (FP64 forward substitution on the
-    // identity), so that a unit's diagonal solve is one 32x32 product
-    P.dinv.assign((size_t)nunits * kChunk * kChunk, 0.0);
+    // Per unit, three 32x32 column-major FP64 matrices (FP64 products, cast
+    // once for the FP32 factor):
+    //   Dinv  = D^{-1}, D the unit's diagonal block (forward substitution on
+    //           the identity), so that its diagonal solve is one product;
+    //   M_lo  = D^{-1} L[unit, previous chunk] (a unit that is not its
+    //           supernode's first chunk) and
+    //   M_up  = D^{-T} L[next chunk, unit]^T (not the last chunk): the block
+    //           on the sweep's dependency chain folded into the diagonal
+    //           solve, x = D^{-1} t' - M x_chain, so that after the chain
+    //           wait a unit does one 32x32 product and no reduction.
+    constexpr size_t kMat = (size_t)kChunk * kChunk;
+    P.dinv.assign((size_t)nunits * 3 * kMat, 0.0);
     for (int32_t u = 0; u < nunits; ++u) {
         const SnUnit& U = P.units[u];
         const double* D = P.panels.data() + U.panel_col_off + U.pos0;  // D(i,j) = D[i + j*ld]
-        double* X = P.dinv.data() + (size_t)u * kChunk * kChunk;     // X(i,j) = X[i + j*32]
+        double* X = P.dinv.data() + (size_t)u * 3 * kMat;             // X(i,j) = X[i + j*32]
         for (int32_t j = 0; j < U.w; ++j) {
             for (int32_t i = j; i < U.w; ++i) {
                 double v = (i == j) ? 1.0 : 0.0;
                 for (int32_t k = j; k < i; ++k) v -= D[i + (size_t)k * U.ld] * X[k + j * kChunk];
                 X[i + j * kChunk] = v / D[i + (size_t)i * U.ld];
             }
+        }
+        if (U.pos0 > 0) {  // previous chunk: 32 columns, panel columns just before the unit's
+            const double* Lp = P.panels.data() + U.panel_col_off - (int64_t)kChunk * U.ld + U.pos0;
+            double* Mlo = X + kMat;
+            for (int32_t j = 0; j < kChunk; ++j)
+                for (int32_t i = 0; i < U.w; ++i) {
+                    double v = 0.0;
+                    for (int32_t m = 0; m <= i; ++m) v += X[i + m * kChunk] * Lp[m + (size_t)j * U.ld];
+                    Mlo[i + j * kChunk] = v;
+                }
+        }
+        const int32_t wn = std::min(kChunk, U.sn_w - (U.pos0 + U.w));  // next chunk's width
+        if (wn > 0) {
+            const double* Ln = P.panels.data() + U.panel_col_off + U.pos0 + U.w;  // Ln(j, m) = Ln[j + m*ld]
+            double* Mup = X + 2 * kMat;
+            for (int32_t j = 0; j < wn; ++j)
+                for (int32_t i = 0; i < U.w; ++i) {
+                    double v = 0.0;
+                    for (int32_t m = i; m < U.w; ++m) v += X[m + i * kChunk] * Ln[j + (size_t)m * U.ld];
+                    Mup[i + j * kChunk] = v;
+                }
         }
     }
     // Ticket order of the supernodal items. Each item's start is estimated

@@ -64,7 +64,7 @@ struct SolvePlan {
     std::vector<SnUnit> units;            // in lower topological order
     std::vector<SnContrib> contribs;
     std::vector<SnPartial> parts;         // lower-sweep partial sums (by unit)
-    std::vector<double> dinv;             // per unit: inverse of the diagonal block, 32x32 column-major
+    std::vector<double> dinv;             // per unit: Dinv, M_lo, M_up (32x32 column-major each, plan.cpp)
     std::vector<int32_t> unit_order_lo;   // lower-sweep items in ticket order (sorted by key):
                                           // unit u (>= 0) or partial sum p (~p)
     std::vector<int32_t> unit_order_up;   // units in upper-sweep ticket order

@@ -25,10 +25,14 @@
 //   row finishes after every higher row of the path; so only the newest
 //   32-row block sits on the dependency chain. Lane j holds
 //   column j of the unit and accumulates L[block, j]^T x_block; then the same
-//   fixed-order reduction and a transposed shuffle solve.
+//   fixed-order reduction and a transposed solve.
 // The diagonal solve of a unit is one product with the precomputed inverse
 // of its 32x32 diagonal block (no 32-step substitution on the dependency
-// chain). Items are handed out by an atomic ticket in dependency-level order
+// chain), and the block on the chain itself (from the neighbouring chunk of
+// the same supernode) is folded into it: x = D^{-1} t' - M x_chain with M
+// precomputed (host, FP64), so that after the chain wait a unit does one
+// 32x32 product per RHS column, a warp per column, with no reduction across
+// warps. Items are handed out by an atomic ticket in dependency-level order
 // to a persistent grid: a CTA only waits on items with smaller tickets, all
 // of which were taken by running CTAs, so there is no deadlock; the last CTA
 // to leave resets the counters for the next launch. Waits are bounded
@@ -69,7 +73,8 @@ struct SnSmem {
     static constexpr int XS = XsStride<T, KW>::value;
     __align__(16) T xs[kWarps][kW][XS];  // per-warp staging of x blocks; reused for the reduction
     T t[kW][KW + 1];           // reduced right-hand side of the unit
-    T d[kW][kW + 1];           // diagonal block
+    T d[kW][kW + 1];           // inverse diagonal block
+    T m[kW][kW + 1];           // chain block folded into the diagonal solve (M_lo / M_up)
 };
 
 // acc[k] += a * row[k] for k < KW, reading `row` (16-byte aligned shared
@@ -105,10 +110,9 @@ __device__ __forceinline__ void warp_wait(const int* flag, int epoch, int* statu
 
 // One warp's share of a lower-sweep block: inner columns [j0, j0 + J) of
 // L[unit rows, source chunk] times the matching rows of x_source, added into
-// acc (lane = unit row). J = 32: the whole block; J = 4: an eighth (the block
-// on the dependency chain is split across the 8 warps). Lane p holds block
-// row popc(rowmask below p) when bit p of rowmask is set. `ready`: the
-// source's flag was already seen set (no wait).
+// acc (lane = unit row); J = 32: the whole block. Lane p holds block row
+// popc(rowmask below p) when bit p of rowmask is set. `ready`: the source's
+// flag was already seen set (no wait).
 template <typename T, int KW, int J>
 __device__ __forceinline__ void lower_block(const SnSys& d, long long panel_off, int ld, int xcol, int w,
                                             int src_unit, unsigned rowmask, bool ready, int j0, int slice,
@@ -290,9 +294,16 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
         const int w = U.w;
         // off the dependency chain: the unit's current right-hand side and
         // its inverse diagonal block go to shared memory first
+        // the chain input: lower, the previous chunk of the supernode; upper,
+        // the next one (both the neighbouring unit)
+        const bool chain = !part && (LOWER ? U.pos0 > 0 : U.pos0 + w < U.sn_w);
         if (!part) {
-            const T* __restrict__ dinv = static_cast<const T*>(d.dinv) + (size_t)uidx * kW * kW;
+            const T* __restrict__ dinv = static_cast<const T*>(d.dinv) + (size_t)uidx * 3 * kW * kW;
             for (int idx = tid; idx < kW * kW; idx += kT) sm.d[idx & 31][idx >> 5] = dinv[idx];
+            if (chain) {
+                const T* __restrict__ mc = dinv + (LOWER ? 1 : 2) * kW * kW;
+                for (int idx = tid; idx < kW * kW; idx += kT) sm.m[idx & 31][idx >> 5] = mc[idx];
+            }
             for (int idx = tid; idx < kW * KW; idx += kT) {
                 const int i = idx / KW, k = idx % KW;
                 sm.t[i][k] = (i < w && k < kw) ? tmp[(size_t)(U.c0 + i) * nrhs + k0 + k] : T(0);
@@ -302,10 +313,10 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
 #pragma unroll
         for (int k = 0; k < KW; ++k) acc[k] = T(0);
 
-        // The block on the dependency chain (lower: from the previous chunk of
-        // the same supernode, listed last; upper: from the next chunk, taken
-        // last) is split across all 8 warps; the others go one per warp.
-        constexpr int kSplit = kW / kWarps;
+        // Every block but the one on the dependency chain (lower: from the
+        // previous chunk of the same supernode, listed last; upper: from the
+        // next chunk) goes to a warp in turn; the chain block is folded into
+        // the diagonal solve below.
         if (part) {
             lower_list<T, KW>(d, PS.contrib_begin + warp, PS.contrib_end, slice, k0, kw, epoch, a.status, lane,
                               xs, acc);
@@ -318,27 +329,19 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
                 for (int k = 0; k < KW; ++k) acc[k] += __ldcg(ps + k);
             }
             const int nb = U.contrib_end - U.contrib_begin;
-            const bool split = nb > 0 && U.pos0 > 0 && d.contribs[U.contrib_end - 1].src_unit == uidx - 1;
-            const int nfree = split ? nb - 1 : nb;
+            const int nfree = chain ? nb - 1 : nb;  // the chain block is the list's last
             lower_list<T, KW>(d, U.contrib_begin + warp, U.contrib_begin + nfree, slice, k0, kw, epoch, a.status,
                               lane, xs, acc);
-            if (split) {
-                const SnContrib C = d.contribs[U.contrib_end - 1];
-                lower_block<T, KW, kSplit>(d, C.panel_off, C.ld, C.xcol, C.w, C.src_unit, C.rowmask, false,
-                                           warp * kSplit, slice, k0, kw, epoch, a.status, lane, xs, acc);
-            }
         } else {
             // block list: off-diagonal rows of the supernode in 32-row blocks,
             // highest rows first (they are solved first), each waiting for the
             // unit of its lowest row; then the later chunks of the supernode,
-            // last chunk first; the next chunk's block (the dependency chain)
-            // is split across all warps
+            // last chunk first, but the next one (the chain)
             const int wj = U.pos0 + w;                      // end of this unit's columns
             const int sn_w = U.sn_w;                        // supernode width
             const int nrb = (U.ld - sn_w + kW - 1) / kW;    // off-diagonal row blocks
             const int nlater = (sn_w - wj + kW - 1) / kW;   // later chunks
-            const bool split = nlater > 0;
-            const int nfree = nrb + nlater - (split ? 1 : 0);
+            const int nfree = nrb + nlater - (chain ? 1 : 0);
             for (int b = warp; b < nfree; b += kWarps) {
                 int p0, nr, dep;
                 if (b < nrb) {
@@ -352,11 +355,6 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
                     dep = uidx + 1 + c;
                 }
                 upper_block<T, KW, kW>(d, U, p0, nr, 0, dep, slice, k0, kw, epoch, a.status, lane, xs, acc);
-            }
-            if (split) {  // the next chunk of the supernode (c = 0)
-                const int nr = min(kW, sn_w - wj);
-                upper_block<T, KW, kSplit>(d, U, wj, nr, warp * kSplit, uidx + 1, slice, k0, kw, epoch,
-                                           a.status, lane, xs, acc);
             }
         }
 
@@ -388,24 +386,56 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
             sm.t[i][k] -= s;
         }
         __syncthreads();
-        // diagonal block: x = D^{-1} t (lower) or D^{-T} t (upper); lane = row
-        for (int k = warp; k < kw; k += kWarps) {
+        // diagonal block: x = D^{-1} t (lower) or D^{-T} t (upper), lane =
+        // row, RHS columns warp, warp + 8, ...; then, once the chain unit's
+        // flag is seen, the chain term x -= M x_chain, x_chain (the
+        // neighbouring unit's solution) broadcast from lane j by shuffles
+        constexpr int KPW = (KW + kWarps - 1) / kWarps;  // RHS columns per warp
+        T xv[KPW];
+#pragma unroll
+        for (int q = 0; q < KPW; ++q) {
+            const int k = warp + q * kWarps;
             T v = T(0);
-            if (LOWER) {
+            if (k < kw) {
+                if (LOWER) {
 #pragma unroll 8
-                for (int j = 0; j < kW; ++j) v = fma(sm.d[lane][j], sm.t[j][k], v);
-            } else {
+                    for (int j = 0; j < kW; ++j) v = fma(sm.d[lane][j], sm.t[j][k], v);
+                } else {
 #pragma unroll 8
-                for (int j = 0; j < kW; ++j) v = fma(sm.d[j][lane], sm.t[j][k], v);
+                    for (int j = 0; j < kW; ++j) v = fma(sm.d[j][lane], sm.t[j][k], v);
+                }
             }
-            if (lane < w) {
-                tmp[(size_t)(U.c0 + lane) * nrhs + k0 + k] = v;
+            xv[q] = v;
+        }
+        if (chain && warp < kw) {
+            const int cu = LOWER ? uidx - 1 : uidx + 1;                 // chain unit
+            const int crow = LOWER ? U.c0 - kW : U.c0 + w;              // its first row
+            const int cw = LOWER ? kW : min(kW, U.sn_w - (U.pos0 + w)); // its width
+            warp_wait(d.uflags + (size_t)cu * d.nslices + slice, epoch, a.status, lane);
+            T xc[KPW];
+#pragma unroll
+            for (int q = 0; q < KPW; ++q) {
+                const int k = warp + q * kWarps;
+                xc[q] = (k < kw && lane < cw) ? __ldcg(tmp + (size_t)(crow + lane) * nrhs + k0 + k) : T(0);
+            }
+#pragma unroll
+            for (int q = 0; q < KPW; ++q) {
+                if (warp + q * kWarps >= kw) break;  // warp-uniform
+#pragma unroll 8
+                for (int j = 0; j < kW; ++j) xv[q] = fma(-sm.m[lane][j], __shfl_sync(0xffffffffu, xc[q], j), xv[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < KPW; ++q) {
+            const int k = warp + q * kWarps;
+            if (k < kw && lane < w) {
+                tmp[(size_t)(U.c0 + lane) * nrhs + k0 + k] = xv[q];
                 if (!LOWER) {
                     using TO = typename io::tout;
                     TO* out = static_cast<TO*>(d.out);
                     const size_t oo = (size_t)d.perm[U.c0 + lane] * nrhs + k0 + k;
-                    if (io::accum) out[oo] += (TO)v;
-                    else out[oo] = (TO)v;
+                    if (io::accum) out[oo] += (TO)xv[q];
+                    else out[oo] = (TO)xv[q];
                 }
             }
         }
