@@ -119,7 +119,6 @@ __device__ __forceinline__ void row_nnz(const RowSys& d, int task, int epoch, in
     // writes before lane 0's release
     __syncwarp();
     if (lane == 0 && !partial) {
-        __threadfence();
         dev::st_release(d.flags + row, epoch);
     }
 }
@@ -190,7 +189,6 @@ __device__ __forceinline__ void row_rhs(const RowSys& d, int task, int epoch, in
     }
     __syncwarp();
     if (lane == 0 && !partial) {
-        __threadfence();
         dev::st_release(d.flags + row, epoch);
     }
 }

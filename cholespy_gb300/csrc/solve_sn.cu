@@ -373,7 +373,6 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
             }
             __syncthreads();
             if (tid == 0) {
-                __threadfence();
                 dev::st_release(d.uflags + (size_t)(d.n_units + ~uidx) * d.nslices + slice, epoch);
             }
             continue;
@@ -442,7 +441,6 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
         // the barrier orders the CTA's writes before thread 0's release
         __syncthreads();
         if (tid == 0) {
-            __threadfence();
             dev::st_release(d.uflags + (size_t)uidx * d.nslices + slice, epoch);
         }
     }
