@@ -40,6 +40,8 @@
 // fixed reduction order.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "device.cuh"
 #include "host/plan.h"
 #include "launch.h"
@@ -243,17 +245,288 @@ __device__ __forceinline__ void upper_block(const SnSys& d, const SnUnit& U, int
     __syncwarp();
 }
 
+// ---- wide FP64 RHS slices: a CTA-wide block pipeline ----------------------
+//
+// The CTA streams its item's blocks through S shared-memory stages with
+// cp.async: while the 8 warps apply one block, the L and x blocks of the next
+// S - 1 are in flight. Lane = RHS column k of the slice (FP64: two 16-lane
+// groups, each taking half of the block's inner dimension); warp w owns 4
+// destination rows (lower sweep) or unit columns (upper sweep), so a lane
+// accumulates only rows present in the block and no reduction across warps
+// is needed. Staged L blocks hold zeros beyond the block's extent, x blocks
+// are stored transposed (x[k][j]) so that a lane reads its column with
+// 16-byte loads.
+template <typename T, int KW>
+struct Wide {
+    static constexpr int G = 32 / KW;                 // lane groups
+    static constexpr int JR = kW / G;                 // inner indices per group
+    static constexpr int V = 16 / (int)sizeof(T);     // elements per 16 bytes
+    static constexpr int LS = kW + V;                 // row stride of a staged L block
+    static constexpr int XS = kW + V;                 // row stride of a staged x block
+    static constexpr int S = sizeof(T) == 4 ? 4 : 3;  // pipeline stages
+};
+
+template <typename T, int KW>
+struct SnStage {
+    __align__(16) T l[kW][Wide<T, KW>::LS];  // lower: l[i][j] (block row, source column); upper: l[j][i]
+    __align__(16) T x[KW][Wide<T, KW>::XS];  // x[k][j], transposed
+    unsigned mask;                           // lower: the block's row mask
+    int ext;                                 // lower: source columns; upper: block rows
+};
+
+template <typename T, int KW>
+struct SnSmemWide {
+    SnStage<T, KW> st[Wide<T, KW>::S];
+    T t[kW][KW + 1];
+    T d[kW][kW + 1];
+    T m[kW][kW + 1];
+};
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// acc[r] += sum over the group's inner range of l_row[i] * xr[i] (16-byte loads of l_row).
+template <typename T, int JR>
+__device__ __forceinline__ T dot_row(const T* l_row, const T (&xr)[JR], T acc) {
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int i = 0; i < JR; i += 4) {
+            const float4 v = *reinterpret_cast<const float4*>(l_row + i);
+            acc = fmaf(v.x, xr[i], acc);
+            acc = fmaf(v.y, xr[i + 1], acc);
+            acc = fmaf(v.z, xr[i + 2], acc);
+            acc = fmaf(v.w, xr[i + 3], acc);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < JR; i += 2) {
+            const double2 v = *reinterpret_cast<const double2*>(l_row + i);
+            acc = fma(v.x, xr[i], acc);
+            acc = fma(v.y, xr[i + 1], acc);
+        }
+    }
+    return acc;
+}
+
+template <typename T, int JR>
+__device__ __forceinline__ void load_col(const T* src, T (&xr)[JR]) {
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int i = 0; i < JR; i += 4) {
+            const float4 v = *reinterpret_cast<const float4*>(src + i);
+            xr[i] = v.x; xr[i + 1] = v.y; xr[i + 2] = v.z; xr[i + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < JR; i += 2) {
+            const double2 v = *reinterpret_cast<const double2*>(src + i);
+            xr[i] = v.x; xr[i + 1] = v.y;
+        }
+    }
+}
+
+// The S-stage pipeline over blocks 0..nblk-1: issue(b, stage) starts block
+// b's copies into a stage (all threads), compute(b, stage) applies it.
+template <int S, class Issue, class Compute>
+__device__ __forceinline__ void pipeline(int nblk, Issue issue, Compute compute) {
+#pragma unroll 1
+    for (int b = 0; b < S - 1; ++b) {
+        if (b < nblk) issue(b, b % S);
+        cp_async_commit();
+    }
+#pragma unroll 1
+    for (int b = 0; b < nblk; ++b) {
+        cp_async_wait<S - 2>();  // this thread's copies of block b have landed
+        __syncthreads();         // everyone's have, and every warp is done with block b - 1
+        if (b + S - 1 < nblk) issue(b + S - 1, (b + S - 1) % S);
+        cp_async_commit();
+        compute(b, b % S);
+    }
+    cp_async_wait<0>();
+}
+
+// Lower sweep, wide slices: contribution blocks [b0, b1), whose sources
+// have taken earlier tickets (a block waits for its source's flag before its
+// x copy is issued). acc[r] += (L_block x_source)[row 4 * warp + r][k]. Lane
+// k of each warp keeps a window of 32 block descriptors (lane j: block
+// 32 * n + j) with their flags checked, broadcast by shuffles.
+template <typename T, int KW>
+__device__ __forceinline__ void lower_wide(const SnSys& d, SnSmemWide<T, KW>& sm, int b0, int b1, int slice, int k0,
+                                           int kw, int epoch, int* status, int tid, int lane, int warp,
+                                           T (&acc)[4]) {
+    using C = Wide<T, KW>;
+    const T* __restrict__ panels = static_cast<const T*>(d.panels);
+    const T* tmp = static_cast<const T*>(d.tmp);
+    const int nrhs = d.nrhs;
+    int wbase = -1;
+    long long poff = 0;
+    int ld = 0, xcol = 0, w = 0, nr = 0, srcu = 0, ready = 1;
+    unsigned mask = 0;
+    auto issue = [&](int b, int s) {
+        SnStage<T, KW>& st = sm.st[s];
+        if ((b & ~31) != wbase) {  // next window
+            wbase = b & ~31;
+            const int mb = b0 + wbase + lane;
+            if (mb < b1) {
+                const SnContrib& c = d.contribs[mb];
+                poff = c.panel_off; ld = c.ld; xcol = c.xcol; w = c.w; nr = c.nr; srcu = c.src_unit;
+                mask = c.rowmask;
+                ready = dev::ld_acquire(d.uflags + (size_t)srcu * d.nslices + slice) >= epoch;
+            }
+            __syncwarp();  // orders the lanes' flag observations before every lane's copies
+        }
+        const int q = b & 31;
+        const long long bp = __shfl_sync(0xffffffffu, poff, q);
+        const int bld = __shfl_sync(0xffffffffu, ld, q), bx = __shfl_sync(0xffffffffu, xcol, q);
+        const int bw = __shfl_sync(0xffffffffu, w, q), bnr = __shfl_sync(0xffffffffu, nr, q);
+        const int bs = __shfl_sync(0xffffffffu, srcu, q), br = __shfl_sync(0xffffffffu, ready, q);
+        const unsigned bm = __shfl_sync(0xffffffffu, mask, q);
+        if (tid == 0) {
+            st.mask = bm;
+            st.ext = bw;
+        }
+        for (int idx = tid; idx < kW * kW; idx += kT) {  // l[i][j], zero beyond the source columns
+            const int i = idx & 31, j = idx >> 5;
+            if (i < bnr) {
+                if (j < bw) cp_async_elem(&st.l[i][j], panels + bp + (size_t)j * bld + i);
+                else st.l[i][j] = T(0);
+            }
+        }
+        if (!br) warp_wait(d.uflags + (size_t)bs * d.nslices + slice, epoch, status, lane);
+        for (int idx = tid; idx < kW * KW; idx += kT) {  // x[k][j] = x_source[j][k], zero beyond
+            const int k = idx % KW, j = idx / KW;
+            if (j < bw) {
+                if (k < kw) cp_async_elem(&st.x[k][j], tmp + (size_t)(bx + j) * nrhs + k0 + k);
+            } else {
+                st.x[k][j] = T(0);
+            }
+        }
+    };
+    auto compute = [&](int, int s) {
+        const SnStage<T, KW>& st = sm.st[s];
+        const unsigned bm = st.mask;
+        const unsigned rows4 = (bm >> (4 * warp)) & 0xFu;
+        if (!rows4) return;                  // warp-uniform
+        const int k = lane % KW, h = lane / KW;
+        if (h * C::JR >= st.ext) return;     // this group's source columns are all beyond the block
+        T xr[C::JR];
+        load_col<T, C::JR>(&st.x[k][h * C::JR], xr);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            if (!((rows4 >> r) & 1u)) continue;
+            const int i = __popc(bm & ((1u << (4 * warp + r)) - 1u));
+            acc[r] = dot_row<T, C::JR>(&st.l[i][h * C::JR], xr, acc[r]);
+        }
+    };
+    pipeline<C::S>(b1 - b0, issue, compute);
+}
+
+// Upper sweep, wide slices: blocks 0..nblk-1 of the unit's list (off-
+// diagonal 32-row blocks, highest first, then the later chunks but the next,
+// last first), each waiting for its flag before its x copy is issued.
+// acc[r] += (L_block^T x_block)[unit column 4 * warp + r][k].
+template <typename T, int KW>
+__device__ __forceinline__ void upper_wide(const SnSys& d, SnSmemWide<T, KW>& sm, const SnUnit& U, int uidx,
+                                           int nblk, int slice, int k0, int kw, int epoch, int* status, int tid,
+                                           int lane, int warp, T (&acc)[4]) {
+    using C = Wide<T, KW>;
+    const T* __restrict__ panels = static_cast<const T*>(d.panels);
+    const T* tmp = static_cast<const T*>(d.tmp);
+    const int nrhs = d.nrhs;
+    const int w = U.w, wj = U.pos0 + w, sn_w = U.sn_w, sn_c0 = U.c0 - U.pos0;
+    const int nrb = (U.ld - sn_w + kW - 1) / kW;
+    const int nlater = (sn_w - wj + kW - 1) / kW;
+    int wbase = -1, p0 = 0, nr = 0, ready = 1, dep = 0;
+    auto issue = [&](int b, int s) {
+        SnStage<T, KW>& st = sm.st[s];
+        if ((b & ~31) != wbase) {  // next window
+            wbase = b & ~31;
+            const int mb = wbase + lane;
+            if (mb < nblk) {
+                if (mb < nrb) {
+                    p0 = sn_w + (nrb - 1 - mb) * kW;
+                    nr = min(kW, U.ld - p0);
+                    dep = d.unit_of_row[d.sn_rows[U.rows_off + p0]];
+                } else {
+                    const int c = nlater - 1 - (mb - nrb);
+                    p0 = wj + c * kW;
+                    nr = min(kW, sn_w - p0);
+                    dep = uidx + 1 + c;
+                }
+                ready = dev::ld_acquire(d.uflags + (size_t)dep * d.nslices + slice) >= epoch;
+            }
+            __syncwarp();
+        }
+        const int q = b & 31;
+        const int bp0 = __shfl_sync(0xffffffffu, p0, q), bnr = __shfl_sync(0xffffffffu, nr, q);
+        const int bdep = __shfl_sync(0xffffffffu, dep, q), br = __shfl_sync(0xffffffffu, ready, q);
+        if (tid == 0) st.ext = bnr;
+        for (int idx = tid; idx < kW * kW; idx += kT) {  // l[j][i] = L[block row i, unit column j]
+            const int i = idx & 31, j = idx >> 5;
+            if (j < w) {
+                if (i < bnr) cp_async_elem(&st.l[j][i], panels + U.panel_col_off + (size_t)j * U.ld + bp0 + i);
+                else st.l[j][i] = T(0);
+            }
+        }
+        if (!br) warp_wait(d.uflags + (size_t)bdep * d.nslices + slice, epoch, status, lane);
+        for (int idx = tid; idx < kW * KW; idx += kT) {  // x[k][i] = x[row of block row i][k]
+            const int k = idx % KW, i = idx / KW;
+            if (i < bnr) {
+                if (k < kw) {
+                    const int pos = bp0 + i;
+                    const int row = pos < sn_w ? sn_c0 + pos : d.sn_rows[U.rows_off + pos];
+                    cp_async_elem(&st.x[k][i], tmp + (size_t)row * nrhs + k0 + k);
+                }
+            } else {
+                st.x[k][i] = T(0);
+            }
+        }
+    };
+    auto compute = [&](int, int s) {
+        const SnStage<T, KW>& st = sm.st[s];
+        if (4 * warp >= w) return;           // warp-uniform
+        const int k = lane % KW, h = lane / KW;
+        if (h * C::JR >= st.ext) return;     // this group's rows are all beyond the block
+        T xr[C::JR];
+        load_col<T, C::JR>(&st.x[k][h * C::JR], xr);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            if (4 * warp + r >= w) break;
+            acc[r] = dot_row<T, C::JR>(&st.l[4 * warp + r][h * C::JR], xr, acc[r]);
+        }
+    };
+    pipeline<C::S>(nblk, issue, compute);
+}
+
+// FP64 wide slices (16 RHS columns) use the CTA-wide block pipeline and 3
+// CTAs per SM: FP64 arithmetic is slow enough on this GPU that skipping the
+// rows a block does not have pays for the pipeline. Otherwise each warp takes
+// its own blocks (lane = row).
+template <class io, int KW>
+constexpr bool kPipelined = sizeof(typename io::t) == 8 && KW >= 16;
+template <class io, int KW>
+using SnSmemOf = std::conditional_t<kPipelined<io, KW>, SnSmemWide<typename io::t, KW>, SnSmem<typename io::t, KW>>;
+
 template <class io, bool LOWER, int KW>
-__global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
+__global__ void __launch_bounds__(kT, (kPipelined<io, KW> ? 3 : 2)) sn_sweep_kernel(SnSweepArgs a) {
     using T = typename io::t;
+    constexpr bool WIDE = kPipelined<io, KW>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SnSmem<T, KW>& sm = *reinterpret_cast<SnSmem<T, KW>*>(smem_raw);
+    SnSmemOf<io, KW>& sm = *reinterpret_cast<SnSmemOf<io, KW>*>(smem_raw);
     if (a.skip && dev::ld_volatile(a.skip)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nitems = a.nitems;
     // every CTA reads the sweep's epoch before the last CTA out bumps it
     const int epoch = dev::ld_volatile(a.epoch);
-    T (*xs)[XsStride<T, KW>::value] = sm.xs[warp];
     __shared__ int ticket, s_uidx, s_slice;
     __shared__ SnSys dsm;
     for (;;) {
@@ -306,85 +579,131 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
             }
             for (int idx = tid; idx < kW * KW; idx += kT) {
                 const int i = idx / KW, k = idx % KW;
-                sm.t[i][k] = (i < w && k < kw) ? tmp[(size_t)(U.c0 + i) * nrhs + k0 + k] : T(0);
+                // L2 loads: no value of an unsolved row enters L1 (the wide
+                // path's cp.async x copies read through L1)
+                sm.t[i][k] = (i < w && k < kw) ? __ldcg(tmp + (size_t)(U.c0 + i) * nrhs + k0 + k) : T(0);
             }
         }
-        T acc[KW];
-#pragma unroll
-        for (int k = 0; k < KW; ++k) acc[k] = T(0);
-
         // Every block but the one on the dependency chain (lower: from the
         // previous chunk of the same supernode, listed last; upper: from the
-        // next chunk) goes to a warp in turn; the chain block is folded into
-        // the diagonal solve below.
-        if (part) {
-            lower_list<T, KW>(d, PS.contrib_begin + warp, PS.contrib_end, slice, k0, kw, epoch, a.status, lane,
-                              xs, acc);
-        } else if (LOWER) {
-            // the unit's partial sums, one per warp in turn (slot row = lane)
-            for (int q = U.part_begin + warp; q < U.part_end; q += kWarps) {
-                warp_wait(d.uflags + (size_t)(d.n_units + q) * d.nslices + slice, epoch, a.status, lane);
-                const T* ps = static_cast<const T*>(d.pbuf) + ((size_t)q * d.nslices + slice) * (kW * KW) + lane * KW;
-#pragma unroll
-                for (int k = 0; k < KW; ++k) acc[k] += __ldcg(ps + k);
+        // next chunk) is applied here; the chain block is folded into the
+        // diagonal solve below.
+        const int nfree = part ? PS.contrib_end - PS.contrib_begin
+                          : LOWER ? (U.contrib_end - U.contrib_begin) - (chain ? 1 : 0)  // chain block: the list's last
+                                  : (U.ld - U.sn_w + kW - 1) / kW + (U.sn_w - (U.pos0 + w) + kW - 1) / kW -
+                                        (chain ? 1 : 0);
+        if constexpr (WIDE) {
+            // warp w owns rows (lower) / unit columns (upper) 4w .. 4w + 3;
+            // lane k < KW ends with the sums of RHS column k
+            T acc[4] = {T(0), T(0), T(0), T(0)};
+            if (LOWER) {
+                const int b0 = part ? PS.contrib_begin : U.contrib_begin;
+                lower_wide<T, KW>(d, sm, b0, b0 + nfree, slice, k0, kw, epoch, a.status, tid, lane, warp, acc);
+            } else {
+                upper_wide<T, KW>(d, sm, U, uidx, nfree, slice, k0, kw, epoch, a.status, tid, lane, warp, acc);
             }
-            const int nb = U.contrib_end - U.contrib_begin;
-            const int nfree = chain ? nb - 1 : nb;  // the chain block is the list's last
-            lower_list<T, KW>(d, U.contrib_begin + warp, U.contrib_begin + nfree, slice, k0, kw, epoch, a.status,
-                              lane, xs, acc);
-        } else {
-            // block list: off-diagonal rows of the supernode in 32-row blocks,
-            // highest rows first (they are solved first), each waiting for the
-            // unit of its lowest row; then the later chunks of the supernode,
-            // last chunk first, but the next one (the chain)
-            const int wj = U.pos0 + w;                      // end of this unit's columns
-            const int sn_w = U.sn_w;                        // supernode width
-            const int nrb = (U.ld - sn_w + kW - 1) / kW;    // off-diagonal row blocks
-            const int nlater = (sn_w - wj + kW - 1) / kW;   // later chunks
-            const int nfree = nrb + nlater - (chain ? 1 : 0);
-            for (int b = warp; b < nfree; b += kWarps) {
-                int p0, nr, dep;
-                if (b < nrb) {
-                    p0 = sn_w + (nrb - 1 - b) * kW;
-                    nr = min(kW, U.ld - p0);
-                    dep = d.unit_of_row[d.sn_rows[U.rows_off + p0]];
-                } else {
-                    const int c = nlater - 1 - (b - nrb);  // later chunk index, last first
-                    p0 = wj + c * kW;
-                    nr = min(kW, sn_w - p0);
-                    dep = uidx + 1 + c;
+            if constexpr (Wide<T, KW>::G == 2) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], 16);
+            }
+            const int k = lane % KW;
+            const bool lead = lane < KW;
+            if (LOWER && !part) {  // the unit's partial sums
+                for (int q = U.part_begin; q < U.part_end; ++q) {
+                    warp_wait(d.uflags + (size_t)(d.n_units + q) * d.nslices + slice, epoch, a.status, lane);
+                    const T* ps = static_cast<const T*>(d.pbuf) + ((size_t)q * d.nslices + slice) * (kW * KW);
+                    if (lead) {
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) acc[r] += __ldcg(ps + (4 * warp + r) * KW + k);
+                    }
                 }
-                upper_block<T, KW, kW>(d, U, p0, nr, 0, dep, slice, k0, kw, epoch, a.status, lane, xs, acc);
             }
-        }
-
-        // fixed-order reduction of the warps' partial sums
+            if (part) {  // the sum goes to the partial's slot, then its flag
+                T* ps = static_cast<T*>(d.pbuf) + ((size_t)(~uidx) * d.nslices + slice) * (kW * KW);
+                if (lead) {
 #pragma unroll
-        for (int k = 0; k < KW; ++k) xs[lane][k] = acc[k];
-        __syncthreads();
-        if (part) {  // the sum goes to the partial's slot, then its flag
-            T* ps = static_cast<T*>(d.pbuf) + ((size_t)(~uidx) * d.nslices + slice) * (kW * KW);
+                    for (int r = 0; r < 4; ++r) ps[(4 * warp + r) * KW + k] = acc[r];
+                }
+                __syncthreads();
+                if (tid == 0) dev::st_release(d.uflags + (size_t)(d.n_units + ~uidx) * d.nslices + slice, epoch);
+                continue;
+            }
+            __syncthreads();  // the staged t is complete
+            if (lead) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) sm.t[4 * warp + r][k] -= acc[r];
+            }
+            __syncthreads();
+        } else {
+            T (*xs)[XsStride<T, KW>::value] = sm.xs[warp];
+            T acc[KW];
+#pragma unroll
+            for (int k = 0; k < KW; ++k) acc[k] = T(0);
+            if (part) {
+                lower_list<T, KW>(d, PS.contrib_begin + warp, PS.contrib_end, slice, k0, kw, epoch, a.status, lane,
+                                  xs, acc);
+            } else if (LOWER) {
+                // the unit's partial sums, one per warp in turn (slot row = lane)
+                for (int q = U.part_begin + warp; q < U.part_end; q += kWarps) {
+                    warp_wait(d.uflags + (size_t)(d.n_units + q) * d.nslices + slice, epoch, a.status, lane);
+                    const T* ps =
+                        static_cast<const T*>(d.pbuf) + ((size_t)q * d.nslices + slice) * (kW * KW) + lane * KW;
+#pragma unroll
+                    for (int k = 0; k < KW; ++k) acc[k] += __ldcg(ps + k);
+                }
+                lower_list<T, KW>(d, U.contrib_begin + warp, U.contrib_begin + nfree, slice, k0, kw, epoch,
+                                  a.status, lane, xs, acc);
+            } else {
+                // block list: off-diagonal rows of the supernode in 32-row
+                // blocks, highest rows first (they are solved first), each
+                // waiting for the unit of its lowest row; then the later chunks
+                // of the supernode, last chunk first, but the next one (the chain)
+                const int wj = U.pos0 + w;                      // end of this unit's columns
+                const int sn_w = U.sn_w;                        // supernode width
+                const int nrb = (U.ld - sn_w + kW - 1) / kW;    // off-diagonal row blocks
+                const int nlater = (sn_w - wj + kW - 1) / kW;   // later chunks
+                for (int b = warp; b < nfree; b += kWarps) {
+                    int p0, nr, dep;
+                    if (b < nrb) {
+                        p0 = sn_w + (nrb - 1 - b) * kW;
+                        nr = min(kW, U.ld - p0);
+                        dep = d.unit_of_row[d.sn_rows[U.rows_off + p0]];
+                    } else {
+                        const int c = nlater - 1 - (b - nrb);  // later chunk index, last first
+                        p0 = wj + c * kW;
+                        nr = min(kW, sn_w - p0);
+                        dep = uidx + 1 + c;
+                    }
+                    upper_block<T, KW, kW>(d, U, p0, nr, 0, dep, slice, k0, kw, epoch, a.status, lane, xs, acc);
+                }
+            }
+
+            // fixed-order reduction of the warps' partial sums
+#pragma unroll
+            for (int k = 0; k < KW; ++k) xs[lane][k] = acc[k];
+            __syncthreads();
+            if (part) {  // the sum goes to the partial's slot, then its flag
+                T* ps = static_cast<T*>(d.pbuf) + ((size_t)(~uidx) * d.nslices + slice) * (kW * KW);
+                for (int idx = tid; idx < kW * KW; idx += kT) {
+                    const int i = idx / KW, k = idx % KW;
+                    T v = T(0);
+#pragma unroll
+                    for (int ww = 0; ww < kWarps; ++ww) v += sm.xs[ww][i][k];
+                    ps[idx] = v;
+                }
+                __syncthreads();
+                if (tid == 0) dev::st_release(d.uflags + (size_t)(d.n_units + ~uidx) * d.nslices + slice, epoch);
+                continue;
+            }
             for (int idx = tid; idx < kW * KW; idx += kT) {
                 const int i = idx / KW, k = idx % KW;
                 T v = T(0);
 #pragma unroll
                 for (int ww = 0; ww < kWarps; ++ww) v += sm.xs[ww][i][k];
-                ps[idx] = v;
+                sm.t[i][k] -= v;
             }
             __syncthreads();
-            if (tid == 0) {
-                dev::st_release(d.uflags + (size_t)(d.n_units + ~uidx) * d.nslices + slice, epoch);
-            }
-            continue;
         }
-        for (int idx = tid; idx < kW * KW; idx += kT) {
-            const int i = idx / KW, k = idx % KW;
-            T s = T(0);
-#pragma unroll
-            for (int ww = 0; ww < kWarps; ++ww) s += sm.xs[ww][i][k];
-            sm.t[i][k] -= s;
-        }
-        __syncthreads();
         // diagonal block: x = D^{-1} t (lower) or D^{-T} t (upper), lane =
         // row, RHS columns warp, warp + 8, ...; then, once the chain unit's
         // flag is seen, the chain term x -= M x_chain, x_chain (the
@@ -458,9 +777,8 @@ __global__ void __launch_bounds__(kT, 2) sn_sweep_kernel(SnSweepArgs a) {
 
 template <class io, bool LOWER, int KW>
 cudaError_t launch_sn_kw(const SnSweepArgs& a, cudaStream_t stream) {
-    using T = typename io::t;
     const void* fn = (const void*)sn_sweep_kernel<io, LOWER, KW>;
-    const size_t smem = sizeof(SnSmem<T, KW>);
+    const size_t smem = sizeof(SnSmemOf<io, KW>);
     int grid = 0;
     cudaError_t e = coop_grid(fn, kT, smem, &grid);  // resident CTAs: a persistent grid
     if (e != cudaSuccess) return e;
