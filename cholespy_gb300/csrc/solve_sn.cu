@@ -206,6 +206,40 @@ __device__ __forceinline__ void lower_list(const SnSys& d, int first, int end, i
     }
 }
 
+// Column quarters (lower sweep) or row quarters (upper sweep) of a block
+// list, dealt to the 8 warps in equal contiguous shares (warp w: quarters
+// [w Q / 8, (w + 1) Q / 8) of the list's Q = 4 * nblk), so that the warps of
+// a CTA finish an item together whatever its number of blocks. A warp waits
+// for a block's input once, at its first quarter of the block.
+constexpr int kQ = 4, kJQ = kW / kQ;
+
+template <typename T, int KW>
+__device__ __forceinline__ void lower_quarters(const SnSys& d, int b0, int nblk, int warp, int slice, int k0,
+                                               int kw, int epoch, int* status, int lane,
+                                               T (*xs)[XsStride<T, KW>::value], T (&acc)[KW]) {
+    const int total = nblk * kQ;
+    const int u0 = warp * total / kWarps, u1 = (warp + 1) * total / kWarps;
+    if (u0 >= u1) return;
+    int cur = u0 / kQ;
+    const int last = (u1 - 1) / kQ;
+    SnContrib C = d.contribs[b0 + cur];
+    SnContrib Cn = cur < last ? d.contribs[b0 + cur + 1] : C;  // the next block's descriptor, ahead
+    bool waited = false;
+    for (int u = u0; u < u1; ++u) {
+        const int b = u / kQ, q = u % kQ;
+        if (b != cur) {
+            cur = b;
+            C = Cn;
+            waited = false;
+            if (cur < last) Cn = d.contribs[b0 + cur + 1];
+        }
+        if (q * kJQ >= C.w) continue;  // warp-uniform
+        lower_block<T, KW, kJQ>(d, C.panel_off, C.ld, C.xcol, C.w, C.src_unit, C.rowmask, waited, q * kJQ, slice,
+                                k0, kw, epoch, status, lane, xs, acc);
+        waited = true;
+    }
+}
+
 // One warp's share of an upper-sweep block: rows [i0, i0 + J) of the 32-row
 // block starting at row position p0 of the supernode, L[rows, unit]^T times
 // x[rows], added into acc (lane = unit column).
@@ -243,6 +277,44 @@ __device__ __forceinline__ void upper_block(const SnSys& d, const SnUnit& U, int
         axpy_row<KW>(acc, lv[i], xs[i]);
     }
     __syncwarp();
+}
+
+// Upper-sweep block list of unit `uidx` (off-diagonal 32-row blocks of the
+// supernode, highest first, each final once the unit holding its first row
+// is; then the later chunks of the supernode but the next, last first),
+// dealt in row quarters as lower_quarters deals columns.
+template <typename T, int KW>
+__device__ __forceinline__ void upper_quarters(const SnSys& d, const SnUnit& U, int uidx, int nblk, int warp,
+                                               int slice, int k0, int kw, int epoch, int* status, int lane,
+                                               T (*xs)[XsStride<T, KW>::value], T (&acc)[KW]) {
+    const int wj = U.pos0 + U.w, sn_w = U.sn_w;
+    const int nrb = (U.ld - sn_w + kW - 1) / kW;   // off-diagonal row blocks
+    const int nlater = (sn_w - wj + kW - 1) / kW;  // later chunks
+    const int total = nblk * kQ;
+    const int u0 = warp * total / kWarps, u1 = (warp + 1) * total / kWarps;
+    int cur = -1, p0 = 0, nr = 0, dep = -1;
+    bool waited = false;
+    for (int u = u0; u < u1; ++u) {
+        const int b = u / kQ, q = u % kQ;
+        if (b != cur) {
+            cur = b;
+            waited = false;
+            if (b < nrb) {
+                p0 = sn_w + (nrb - 1 - b) * kW;
+                nr = min(kW, U.ld - p0);
+                dep = d.unit_of_row[d.sn_rows[U.rows_off + p0]];
+            } else {
+                const int c = nlater - 1 - (b - nrb);  // later chunk index, last first
+                p0 = wj + c * kW;
+                nr = min(kW, sn_w - p0);
+                dep = uidx + 1 + c;
+            }
+        }
+        if (q * kJQ >= nr) continue;  // warp-uniform
+        upper_block<T, KW, kJQ>(d, U, p0, nr, q * kJQ, waited ? -1 : dep, slice, k0, kw, epoch, status, lane, xs,
+                                acc);
+        waited = true;
+    }
 }
 
 // ---- wide FP64 RHS slices: a CTA-wide block pipeline ----------------------
@@ -639,9 +711,17 @@ __global__ void __launch_bounds__(kT, (kPipelined<io, KW> ? 3 : 2)) sn_sweep_ker
             T acc[KW];
 #pragma unroll
             for (int k = 0; k < KW; ++k) acc[k] = T(0);
+            // several 32-wide slices (throughput bound): blocks dealt in
+            // balanced quarters; otherwise (latency bound): whole blocks,
+            // round robin
+            const bool kQuarters = KW >= 32 && d.nslices > 1;
             if (part) {
-                lower_list<T, KW>(d, PS.contrib_begin + warp, PS.contrib_end, slice, k0, kw, epoch, a.status, lane,
-                                  xs, acc);
+                if (kQuarters)
+                    lower_quarters<T, KW>(d, PS.contrib_begin, nfree, warp, slice, k0, kw, epoch, a.status, lane,
+                                          xs, acc);
+                else
+                    lower_list<T, KW>(d, PS.contrib_begin + warp, PS.contrib_end, slice, k0, kw, epoch, a.status,
+                                      lane, xs, acc);
             } else if (LOWER) {
                 // the unit's partial sums, one per warp in turn (slot row = lane)
                 for (int q = U.part_begin + warp; q < U.part_end; q += kWarps) {
@@ -651,13 +731,19 @@ __global__ void __launch_bounds__(kT, (kPipelined<io, KW> ? 3 : 2)) sn_sweep_ker
 #pragma unroll
                     for (int k = 0; k < KW; ++k) acc[k] += __ldcg(ps + k);
                 }
-                lower_list<T, KW>(d, U.contrib_begin + warp, U.contrib_begin + nfree, slice, k0, kw, epoch,
-                                  a.status, lane, xs, acc);
+                if (kQuarters)
+                    lower_quarters<T, KW>(d, U.contrib_begin, nfree, warp, slice, k0, kw, epoch, a.status, lane, xs,
+                                          acc);
+                else
+                    lower_list<T, KW>(d, U.contrib_begin + warp, U.contrib_begin + nfree, slice, k0, kw, epoch,
+                                      a.status, lane, xs, acc);
+            } else if (kQuarters) {
+                upper_quarters<T, KW>(d, U, uidx, nfree, warp, slice, k0, kw, epoch, a.status, lane, xs, acc);
             } else {
-                // block list: off-diagonal rows of the supernode in 32-row
-                // blocks, highest rows first (they are solved first), each
-                // waiting for the unit of its lowest row; then the later chunks
-                // of the supernode, last chunk first, but the next one (the chain)
+                // off-diagonal rows of the supernode in 32-row blocks, highest
+                // rows first (they are solved first), each waiting for the unit
+                // of its lowest row; then the later chunks of the supernode, last
+                // chunk first, but the next one (the chain); round robin
                 const int wj = U.pos0 + w;                      // end of this unit's columns
                 const int sn_w = U.sn_w;                        // supernode width
                 const int nrb = (U.ld - sn_w + kW - 1) / kW;    // off-diagonal row blocks
