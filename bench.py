@@ -61,6 +61,19 @@ def parse_args():
 
 # ------------------------------------------------------------- helpers ----
 
+# DRAM bytes (read + write) of one FP32 solve, summed over its 5 sweep
+# launches, from one ncu capture of `bench.py --workload solve` at the same
+# size (dram__bytes_read.sum + dram__bytes_write.sum; the table and command
+# are in profiles/sweeps_poisson64_nrhs128_dram.md). Keyed by (k, nrhs).
+MEASURED_SOLVE_TRAFFIC_F32 = {(64, 128): 2128167168}
+
+
+def measured_traffic(args, f32=True):
+    if not f32:
+        return None
+    return MEASURED_SOLVE_TRAFFIC_F32.get((args.k, args.nrhs))
+
+
 def hbm_peak():
     try:
         d = json.loads(PEAKS_FILE.read_text())
@@ -363,7 +376,7 @@ def run_ours(args, world, rank, local):
                        "max_rel_residual": res_64, "ir_over_fp64": value / value_64},
         "roofline": {"kernel": "triangular sweeps (FP32 solve, lower+upper)", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": measured_traffic(args),
                      "algorithmic_bytes": bytes32, "ms_per_solve": 1e3 * t_32},
         "e2e": {"value": e2e_value, "unit": "RHS-solves/s",
                 "h2d_bytes_per_step": int(b.nbytes), "d2h_bytes_per_step": int(b.nbytes)},
@@ -650,7 +663,8 @@ def run_solve(args, world, rank, local):
                  config_dict(args, n, len(vals), info.nnz_l),
                  roofline={"kernel": "triangular sweeps (lower+upper)", "bound": "hbm",
                            "achieved": byts / (t / args.steps) / 1e9, "peak": peak, "peak_kind": kind,
-                           "unit": "GB/s", "frac": byts / (t / args.steps) / 1e9 / peak, "traffic": None,
+                           "unit": "GB/s", "frac": byts / (t / args.steps) / 1e9 / peak,
+                           "traffic": measured_traffic(args, not args.fp64),
                            "algorithmic_bytes": byts},
                  gpu_launches=info.launches_per_solve * args.steps)
     if rank == 0:
