@@ -588,7 +588,10 @@ constexpr bool kPipelined = sizeof(typename io::t) == 8 && KW >= 16;
 template <class io, int KW>
 using SnSmemOf = std::conditional_t<kPipelined<io, KW>, SnSmemWide<typename io::t, KW>, SnSmem<typename io::t, KW>>;
 
-template <class io, bool LOWER, int KW>
+// QUART: every block list dealt in balanced quarters (FP32, several 32-wide
+// slices of one system), known at compile time. (3 CTAs per SM was measured
+// slower for it: more tickets held by waiting CTAs.)
+template <class io, bool LOWER, int KW, bool QUART>
 __global__ void __launch_bounds__(kT, (kPipelined<io, KW> ? 3 : 2)) sn_sweep_kernel(SnSweepArgs a) {
     using T = typename io::t;
     constexpr bool WIDE = kPipelined<io, KW>;
@@ -714,7 +717,7 @@ __global__ void __launch_bounds__(kT, (kPipelined<io, KW> ? 3 : 2)) sn_sweep_ker
             // several 32-wide slices (throughput bound): blocks dealt in
             // balanced quarters; otherwise (latency bound): whole blocks,
             // round robin
-            const bool kQuarters = KW >= 32 && d.nslices > 1;
+            const bool kQuarters = QUART || (KW >= 32 && d.nslices > 1);
             if (part) {
                 if (kQuarters)
                     lower_quarters<T, KW>(d, PS.contrib_begin, nfree, warp, slice, k0, kw, epoch, a.status, lane,
@@ -861,15 +864,15 @@ __global__ void __launch_bounds__(kT, (kPipelined<io, KW> ? 3 : 2)) sn_sweep_ker
     }
 }
 
-template <class io, bool LOWER, int KW>
+template <class io, bool LOWER, int KW, bool QUART = false>
 cudaError_t launch_sn_kw(const SnSweepArgs& a, cudaStream_t stream) {
-    const void* fn = (const void*)sn_sweep_kernel<io, LOWER, KW>;
+    const void* fn = (const void*)sn_sweep_kernel<io, LOWER, KW, QUART>;
     const size_t smem = sizeof(SnSmemOf<io, KW>);
     int grid = 0;
     cudaError_t e = coop_grid(fn, kT, smem, &grid);  // resident CTAs: a persistent grid
     if (e != cudaSuccess) return e;
     if (grid > a.nitems) grid = a.nitems;
-    sn_sweep_kernel<io, LOWER, KW><<<grid, kT, smem, stream>>>(a);
+    sn_sweep_kernel<io, LOWER, KW, QUART><<<grid, kT, smem, stream>>>(a);
     return cudaGetLastError();
 }
 
@@ -877,6 +880,8 @@ template <class io, bool LOWER>
 cudaError_t launch_sn_io(const SnSweepArgs& a, cudaStream_t stream) {
     constexpr int wide = sizeof(typename io::t) == 8 ? 16 : 32;
     if (!a.wide && a.sys0.nrhs <= 8) return launch_sn_kw<io, LOWER, 8>(a, stream);
+    if constexpr (sizeof(typename io::t) == 4)
+        if (!a.sys && a.sys0.nslices > 1) return launch_sn_kw<io, LOWER, wide, true>(a, stream);
     return launch_sn_kw<io, LOWER, wide>(a, stream);
 }
 
