@@ -166,7 +166,7 @@ int setup_plan(gbchol_solver* h, const std::vector<int32_t>& rp, const std::vect
     const int32_t n = F.n;
     SolvePlan& P = h->plan;
     try {
-        build_plan(F, h->lower.order_h, h->upper.order_h, PlanOptions(), P);
+        build_plan(F, h->lower.order_h, h->upper.order_h, h->plan_opt, P);
     } catch (const std::exception& ex) {
         return fail(GBCHOL_EINTERNAL, std::string("solve plan: ") + ex.what());
     }
@@ -522,6 +522,89 @@ int gbchol_destroy(gbchol_handle h) {
         delete h;
     }
     return GBCHOL_OK;
+}
+
+int gbchol_replan(gbchol_handle h, int32_t min_top_width, int32_t part_keep, int32_t part_group) {
+    if (!h) return fail(GBCHOL_EINVAL, "Null handle.");
+    if (min_top_width < 1 || part_keep < 0 || part_group < 0)
+        return fail(GBCHOL_EINVAL, "min_top_width must be >= 1, part_keep and part_group >= 0.");
+    DeviceGuard g(h->device);
+    CUDA_TRY(cudaDeviceSynchronize());  // no solve may still use the old plan's buffers
+    h->plan_opt.min_top_width = min_top_width;
+    h->plan_opt.part_keep = part_keep;
+    h->plan_opt.part_group = part_group;
+    ++h->plan_gen;
+    if (h->n == 0) return GBCHOL_OK;
+    const std::vector<int32_t> none;
+    const std::vector<double> nonev;
+    if (int rc = setup_plan(h, none, none, nonev)) return rc;
+    CUDA_TRY(cudaDeviceSynchronize());
+    return GBCHOL_OK;
+}
+
+int gbchol_autotune(gbchol_handle h, int32_t precision, int32_t nrhs, const int32_t* candidates, int32_t count,
+                    int32_t reps, int32_t* chosen) {
+    if (!h) return fail(GBCHOL_EINVAL, "Null handle.");
+    if (int rc = check_rhs(nrhs)) return rc;
+    if (precision != 0 && precision != 1) return fail(GBCHOL_EINVAL, "precision must be 0 or 1.");
+    const bool f32 = precision == 0;
+    if (!(h->store & (f32 ? GBCHOL_STORE_F32 : GBCHOL_STORE_F64)))
+        return fail(GBCHOL_ESTATE, f32 ? "This solver keeps no FP32 factor." : "This solver keeps no FP64 factor.");
+    if (!candidates || count < 1 || count > 64) return fail(GBCHOL_EINVAL, "1 to 64 candidate widths are needed.");
+    if (reps < 1 || reps > 100) return fail(GBCHOL_EINVAL, "reps must be in [1, 100].");
+    for (int32_t c = 0; c < count; ++c)
+        if (candidates[c] < 1) return fail(GBCHOL_EINVAL, "Candidate widths must be >= 1.");
+    if (h->n == 0) {
+        if (chosen) *chosen = h->plan_opt.min_top_width;
+        return GBCHOL_OK;
+    }
+    DeviceGuard g(h->device);
+    const size_t bytes = (size_t)h->n * nrhs * (f32 ? sizeof(float) : sizeof(double));
+    DevBuf<unsigned char> b, x;
+    CUDA_TRY(b.alloc(bytes));
+    CUDA_TRY(x.alloc(bytes));
+    CUDA_TRY(cudaMemset(b.p, 0, bytes));
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    int rc = GBCHOL_OK;
+    int32_t best = -1;
+    float best_ms = 0.f;
+    const PlanOptions keep = h->plan_opt;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        rc = fail(GBCHOL_ECUDA, "cudaEventCreate failed.");
+    const SweepIO io = f32 ? SweepIO::F32 : SweepIO::F64;
+    for (int32_t c = 0; c < count && rc == GBCHOL_OK; ++c) {
+        if ((rc = gbchol_replan(h, candidates[c], keep.part_keep, keep.part_group))) break;
+        if ((rc = ensure_tmp(h, work_bytes(h, nrhs, f32)))) break;
+        for (int w = 0; w < 2 && rc == GBCHOL_OK; ++w) rc = run_sweeps(h, f32, io, nrhs, b.p, x.p, nullptr, s);
+        if (rc) break;
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < reps && rc == GBCHOL_OK; ++r) rc = run_sweeps(h, f32, io, nrhs, b.p, x.p, nullptr, s);
+        cudaEventRecord(e1, s);
+        if (rc) break;
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            rc = fail(GBCHOL_ECUDA, "autotune: timing failed.");
+            break;
+        }
+        h->last_stream = s;
+        if ((rc = gbchol_check(h))) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (best < 0 || ms < best_ms) {
+            best = candidates[c];
+            best_ms = ms;
+        }
+    }
+    h->last_stream = nullptr;
+    if (rc == GBCHOL_OK && best != h->plan_opt.min_top_width)
+        rc = gbchol_replan(h, best, keep.part_keep, keep.part_group);
+    if (rc == GBCHOL_OK && chosen) *chosen = best;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    return rc;
 }
 
 int gbchol_reserve(gbchol_handle h, int32_t nrhs) {

@@ -27,6 +27,7 @@ struct gbchol_batch_s {
     int32_t count = 0;
     bool f32 = true;
     std::vector<gbchol_handle> solvers;
+    std::vector<int32_t> plan_gen;   // each solver's plan counter when the batch was built
     std::vector<int32_t> nrhs, nslices;
     std::vector<size_t> tmp_off, pbuf_off, row_off, uflag_off;
     std::vector<RowSys> lo_h, pt_h, up_h;
@@ -89,6 +90,7 @@ int gbchol_batch_create(int32_t count, const gbchol_handle* solvers, const int32
     b->count = count;
     b->f32 = f32;
     b->solvers.assign(solvers, solvers + count);
+    for (int32_t s = 0; s < count; ++s) b->plan_gen.push_back(solvers[s]->plan_gen);
     b->nrhs.assign(nrhs, nrhs + count);
     const size_t es = f32 ? sizeof(float) : sizeof(double);
     size_t tmp_total = 0, rows_total = 0, uflags_total = 0;
@@ -240,6 +242,9 @@ int gbchol_batch_set_io(gbchol_batch b, const void* const* bs, void* const* xs) 
 
 int gbchol_batch_solve(gbchol_batch b, void* stream) {
     if (!b) return fail(GBCHOL_EINVAL, "Null batch.");
+    for (int32_t s = 0; s < b->count; ++s)
+        if (b->solvers[s]->plan_gen != b->plan_gen[s])
+            return fail(GBCHOL_ESTATE, "A solver of the batch was replanned after the batch was built; build it again.");
     if (!b->bound) return fail(GBCHOL_ESTATE, "Bind the batch's b and x arrays first (gbchol_batch_set_io).");
     DeviceGuard g(b->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -116,8 +116,11 @@ struct gbchol_solver {
     double t_factor = 0.0, t_analysis = 0.0;
     DevBuf<int32_t> perm;
     Triangle lower, upper;    // level analysis of L (CSR, diagonal last) and L^T
-    // solve plan (see host/plan.cpp)
+    // solve plan (see host/plan.cpp), its options and a counter of rebuilds
+    // (batches record it and refuse a solver whose plan changed)
     SolvePlan plan;
+    PlanOptions plan_opt;
+    int32_t plan_gen = 0;
     DevBuf<int32_t> lo_rowptr, lo_cols, lo_tasks, up_rowptr, up_cols, up_tasks, sn_rows;
     DevBuf<int32_t> upt_rowptr, upt_cols, upt_tasks;
     DevBuf<float> lo_v32, up_v32, pan32, upt_v32;

@@ -252,6 +252,31 @@ class _CholeskySolver:
         """Preallocate scratch for up to n_rhs RHS (before CUDA-graph capture)."""
         _ffi.check(_ffi.lib().gbchol_reserve(self._h, int(n_rhs)))
 
+    def replan(self, min_top_width=8, part_keep=16, part_group=32):
+        """Rebuild the solve plan with other tuning parameters (gbchol_replan):
+        supernodes at least `min_top_width` columns wide and their ancestors
+        are solved as dense blocks; long block lists keep `part_keep` blocks
+        and hand the rest to partial sums of about `part_group` blocks.
+        Results change only by rounding. Batches built from this solver must
+        be built again. No counterpart in the reference."""
+        _ffi.check(_ffi.lib().gbchol_replan(self._h, int(min_top_width), int(part_keep), int(part_group)))
+
+    def autotune(self, n_rhs, precision=None, candidates=(4, 8, 16, 32), reps=3):
+        """Time `reps` solves of `n_rhs` RHS for each candidate top-region
+        width and keep the fastest plan (gbchol_autotune); returns the chosen
+        width. `precision`: "float" / "double" (default: the precision the
+        solver's solves run in; FP32 for a refining CholeskySolverD). No
+        counterpart in the reference."""
+        if precision is None:
+            prec = 0 if (self._precision == 0 or self._refine) else 1
+        else:
+            prec = 0 if precision == "float" else 1
+        cand = (C.c_int32 * len(candidates))(*[int(c) for c in candidates])
+        chosen = C.c_int32(0)
+        _ffi.check(_ffi.lib().gbchol_autotune(self._h, prec, int(n_rhs), cand, len(candidates), int(reps),
+                                              C.byref(chosen)))
+        return int(chosen.value)
+
     def info(self) -> SolverInfo:
         inf = _ffi.Info()
         _ffi.check(_ffi.lib().gbchol_get_info(self._h, C.byref(inf)))

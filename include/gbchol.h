@@ -238,6 +238,29 @@ int gbchol_check(gbchol_handle h);
 int gbchol_reserve(gbchol_handle h, int32_t nrhs);
 
 /*
+ * Rebuild the solve plan with other tuning parameters: supernodes at least
+ * min_top_width columns wide (and their ancestors) form the supernodal top
+ * region (default 8); lower-sweep contribution lists longer than
+ * part_keep + part_group keep their last part_keep blocks and hand the rest
+ * to partial sums of about part_group blocks (defaults 16 and 32; 0: none).
+ * Results change only by rounding. Synchronises the device. A batch built
+ * from this solver before the call refuses to solve (GBCHOL_ESTATE): build it
+ * again. No counterpart in the reference.
+ */
+int gbchol_replan(gbchol_handle h, int32_t min_top_width, int32_t part_keep, int32_t part_group);
+
+/*
+ * Autotuner: for each of the `count` candidate widths, rebuild the plan with
+ * that min_top_width (gbchol_replan, keeping the partial-sum settings), time
+ * `reps` solves of nrhs right-hand sides in the given precision (0 FP32,
+ * 1 FP64) after two warm-up solves, and keep the fastest plan; the chosen
+ * width is written to *chosen (may be NULL). Allocates and frees its own
+ * buffers and stream. No counterpart in the reference.
+ */
+int gbchol_autotune(gbchol_handle h, int32_t precision, int32_t nrhs, const int32_t* candidates, int32_t count,
+                    int32_t reps, int32_t* chosen);
+
+/*
  * Batched solves: `count` solvers (same device) solved together, system s
  * with nrhs[s] right-hand sides, by one persistent launch per sweep phase.
  * precision 0 = FP32, 1 = FP64 (every solver must keep that factor). The

@@ -346,3 +346,40 @@ def test_repeated_solves_bit_identical(cuda, variant):
         A = sym_matrix(n, vals, idx)
         res = np.abs(A @ x0.cpu().numpy().astype(np.float64) - b).max() / np.abs(b).max()
         assert res <= (2e-3 if variant == "float" else 1e-10), res
+
+
+def test_replan_and_autotune(cuda):
+    """gbchol_replan / gbchol_autotune (no reference counterpart): any top-region
+    width and partial-sum setting gives the same solution up to rounding; the
+    autotuner keeps one of its candidates; a batch built before a replan
+    refuses to solve."""
+    import cholespy_gb300 as cg
+    from cholespy_gb300 import MatrixType, workloads
+    torch = cuda
+    k = 24
+    vals, idx = workloads.grid3d_coo(k, 1e-3)
+    n = k ** 3
+    s = cg.CholeskySolverF(n, torch.tensor(idx[0], device="cuda"), torch.tensor(idx[1], device="cuda"),
+                           torch.tensor(vals, device="cuda"), MatrixType.COO)
+    rng = np.random.default_rng(5)
+    b = rng.standard_normal((n, 20))
+    b_t = torch.tensor(b, dtype=torch.float32, device="cuda")
+    x_ref = spsolve_ref(n, vals, idx, b)
+    scale = np.abs(x_ref).max()
+    for width, keep, group in ((8, 16, 32), (1, 16, 32), (4, 2, 3), (16, 0, 0), (10 ** 6, 16, 32)):
+        s.replan(width, keep, group)
+        x_t = torch.zeros_like(b_t)
+        s.solve(b_t, x_t)
+        s.check()
+        assert np.abs(x_t.cpu().numpy() - x_ref).max() <= 1e-3 * scale, (width, keep, group)
+    batch = cg.BatchSolver([s], [20])
+    batch.bind([b_t], [torch.zeros_like(b_t)])
+    s.replan(8)
+    with pytest.raises(RuntimeError):
+        batch.solve()
+    chosen = s.autotune(20, candidates=(4, 8, 32), reps=2)
+    assert chosen in (4, 8, 32)
+    x_t = torch.zeros_like(b_t)
+    s.solve(b_t, x_t)
+    s.check()
+    assert np.abs(x_t.cpu().numpy() - x_ref).max() <= 1e-3 * scale
