@@ -56,6 +56,8 @@ def parse_args():
     p.add_argument("--cpu-sample-rhs", type=int, default=32,
                    help="RHS columns of the bounded CPU sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="ico6/grid64: keep the default top-region width instead of autotuning it")
     return p.parse_args()
 
 
@@ -72,6 +74,47 @@ def measured_traffic(args, f32=True):
     if not f32:
         return None
     return MEASURED_SOLVE_TRAFFIC_F32.get((args.k, args.nrhs))
+
+
+_FMA_PEAKS = {}
+
+
+def fma_peak(torch, f64):
+    """FP32 / FP64 CUDA-core peak of this GPU in TFLOP/s, measured by probe:
+    cuBLAS SGEMM with TF32 off (8192^3) / DGEMM (4096^3), best of 3 after a
+    warm-up. The 128-RHS sweeps are bounded by these as much as by HBM."""
+    key = "f64" if f64 else "f32"
+    if key in _FMA_PEAKS:
+        return _FMA_PEAKS[key]
+    torch.backends.cuda.matmul.allow_tf32 = False
+    m = 4096 if f64 else 8192
+    dt = torch.float64 if f64 else torch.float32
+    a = torch.randn(m, m, dtype=dt, device="cuda")
+    bm = torch.randn(m, m, dtype=dt, device="cuda")
+    c = a @ bm
+    best = None
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        c = a @ bm
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        best = t if best is None else min(best, t)
+    del a, bm, c
+    _FMA_PEAKS[key] = 2.0 * m ** 3 / best / 1e12
+    return _FMA_PEAKS[key]
+
+
+def compute_roofline(torch, n, nnz_l, nrhs, t_solve, f64):
+    """FMA roofline of one solve: 4 nnz(L) r + 2 n r flops (both sweeps)."""
+    flops = 4.0 * nnz_l * nrhs + 2.0 * n * nrhs
+    peak = fma_peak(torch, f64)
+    achieved = flops / t_solve / 1e12
+    return {"bound": "fp64 fma" if f64 else "fp32 fma", "achieved": achieved, "peak": peak,
+            "peak_kind": "measured (cuBLAS DGEMM)" if f64 else "measured (cuBLAS SGEMM, TF32 off)",
+            "unit": "TFLOP/s", "frac": achieved / peak, "flops": flops}
 
 
 def hbm_peak():
@@ -373,11 +416,13 @@ def run_ours(args, world, rank, local):
                    "max_rel_residual_device": stats.max_rel_residual,
                    "max_rel_residual_host": res_ir, "max_rel_err_vs_fp64_solve": err_ir_vs_64},
         "fp64_plain": {"value": value_64, "unit": "RHS-solves/s", "ms_per_step": 1e3 * t_64 / args.steps,
-                       "max_rel_residual": res_64, "ir_over_fp64": value / value_64},
+                       "max_rel_residual": res_64, "ir_over_fp64": value / value_64,
+                       "compute": compute_roofline(torch, n, info.nnz_l, args.nrhs, t_64 / args.steps, True)},
         "roofline": {"kernel": "triangular sweeps (FP32 solve, lower+upper)", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": measured_traffic(args),
-                     "algorithmic_bytes": bytes32, "ms_per_solve": 1e3 * t_32},
+                     "algorithmic_bytes": bytes32, "ms_per_solve": 1e3 * t_32,
+                     "compute": compute_roofline(torch, n, info.nnz_l, args.nrhs, t_32, False)},
         "e2e": {"value": e2e_value, "unit": "RHS-solves/s",
                 "h2d_bytes_per_step": int(b.nbytes), "d2h_bytes_per_step": int(b.nbytes)},
         "clocks": clocks,
@@ -601,6 +646,8 @@ def run_mesh(args, world, rank, local):
     bd = torch.tensor(b, dtype=dt, device=dev)
     xd = torch.zeros_like(bd)
     r = bd.shape[1]
+    # the library's autotuner picks the top-region width (untimed set-up)
+    width = 8 if args.no_autotune else s.autotune(r, candidates=(2, 4, 8, 16), reps=5)
     t = _events_time(torch, dev, stream, lambda: s.solve(bd, xd), args.steps, args.warmup, world)
     info = s.info()
     byts = algorithmic_bytes(n, info.nnz_l, r, es)
@@ -624,6 +671,7 @@ def run_mesh(args, world, rank, local):
     line = _line(args, world, "RHS-solves/s", world * r * args.steps / t, "RHS-solves/s", t,
                  "f32" if es == 4 else "f64", {"workload": name, "n": n, "nnz_l": info.nnz_l,
                                               "n_rhs": r, "levels": info.levels_lower,
+                                              "top_width": width, "autotuned": not args.no_autotune,
                                               "l2": "factor fits L2; no flush between steps"},
                  roofline={"kernel": "triangular sweeps (lower+upper)", "bound": "hbm",
                            "achieved": achieved, "peak": peak, "peak_kind": kind, "unit": "GB/s",
@@ -665,6 +713,8 @@ def run_solve(args, world, rank, local):
                            "achieved": byts / (t / args.steps) / 1e9, "peak": peak, "peak_kind": kind,
                            "unit": "GB/s", "frac": byts / (t / args.steps) / 1e9 / peak,
                            "traffic": measured_traffic(args, not args.fp64),
+                           "compute": compute_roofline(torch, n, info.nnz_l, args.nrhs, t / args.steps,
+                                                       args.fp64),
                            "algorithmic_bytes": byts},
                  gpu_launches=info.launches_per_solve * args.steps)
     if rank == 0:
