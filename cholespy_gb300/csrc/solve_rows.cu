@@ -61,18 +61,23 @@ __device__ __forceinline__ typename io::t load_rhs(const RowSys& d, int row, int
     return static_cast<const T*>(d.tmp)[(size_t)row * d.nrhs + j];
 }
 
-// Lanes split the nonzeros of the row; R >= nrhs accumulators per lane.
+// Lanes split the nonzeros of the row (entries [s, e) of its CSR row); R >=
+// nrhs accumulators per lane. The row's own loads (perm, diagonal, right-hand
+// side) go out before the waits on its dependencies.
 template <class io, bool LOWER, int R>
-__device__ __forceinline__ void row_nnz(const RowSys& d, int task, int epoch, int* status, int lane) {
+__device__ __forceinline__ void row_nnz(const RowSys& d, int task, int s, int e, int epoch, int* status,
+                                        int lane) {
     using T = typename io::t;
     const T* __restrict__ vals = static_cast<const T*>(d.vals);
     const T* tmp = static_cast<const T*>(d.tmp);
     const int nrhs = d.nrhs;
     const bool partial = task < 0;
     const int row = partial ? ~task : task;
-    const int s = d.rowptr[row], e = d.rowptr[row + 1];
     const int lo = (LOWER || partial) ? s : s + 1;
     const int hi = (LOWER && !partial) ? e - 1 : e;
+    const T diag = partial ? T(1) : vals[LOWER ? e - 1 : s];
+    const int prow = d.perm[row];
+    const T rhs = lane < nrhs ? load_rhs<io, LOWER>(d, row, prow, lane) : T(0);
     T acc[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) acc[j] = T(0);
@@ -108,10 +113,8 @@ __device__ __forceinline__ void row_nnz(const RowSys& d, int task, int epoch, in
         T sj = dev::warp_sum(acc[j]);
         if (j == lane) mine = sj;
     }
-    const T diag = partial ? T(1) : vals[LOWER ? e - 1 : s];
-    const int prow = d.perm[row];
     if (lane < nrhs) {
-        T v = load_rhs<io, LOWER>(d, row, prow, lane) - mine;
+        T v = rhs - mine;
         if (!partial) v = v / diag;
         emit<io, LOWER>(d, row, prow, lane, v, partial);
     }
@@ -126,7 +129,8 @@ __device__ __forceinline__ void row_nnz(const RowSys& d, int task, int epoch, in
 // Lanes split the RHS columns: G lanes per group (32/G groups take
 // alternating nonzeros), Q RHS columns per lane (nrhs <= G*Q).
 template <class io, bool LOWER, int G, int Q>
-__device__ __forceinline__ void row_rhs(const RowSys& d, int task, int epoch, int* status, int lane) {
+__device__ __forceinline__ void row_rhs(const RowSys& d, int task, int s, int e, int epoch, int* status,
+                                        int lane) {
     using T = typename io::t;
     constexpr int NG = 32 / G;
     const int grp = lane / G, sub = lane % G;
@@ -135,9 +139,16 @@ __device__ __forceinline__ void row_rhs(const RowSys& d, int task, int epoch, in
     const int nrhs = d.nrhs;
     const bool partial = task < 0;
     const int row = partial ? ~task : task;
-    const int s = d.rowptr[row], e = d.rowptr[row + 1];
     const int lo = (LOWER || partial) ? s : s + 1;
     const int hi = (LOWER && !partial) ? e - 1 : e;
+    const T diag = partial ? T(1) : vals[LOWER ? e - 1 : s];
+    const int prow = d.perm[row];
+    T rhs[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int j = sub + q * G;
+        rhs[q] = (grp == 0 && j < nrhs) ? load_rhs<io, LOWER>(d, row, prow, j) : T(0);
+    }
     T acc[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) acc[q] = T(0);
@@ -174,14 +185,12 @@ __device__ __forceinline__ void row_rhs(const RowSys& d, int task, int epoch, in
 #pragma unroll
             for (int o = G; o < 32; o <<= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
     }
-    const T diag = partial ? T(1) : vals[LOWER ? e - 1 : s];
-    const int prow = d.perm[row];
     if (grp == 0) {
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             const int j = sub + q * G;
             if (j < nrhs) {
-                T v = load_rhs<io, LOWER>(d, row, prow, j) - acc[q];
+                T v = rhs[q] - acc[q];
                 if (!partial) v = v / diag;
                 emit<io, LOWER>(d, row, prow, j, v, partial);
             }
@@ -203,26 +212,66 @@ __global__ void __launch_bounds__(256) row_sweep_kernel(RowSweepArgs a) {
     if (a.skip && dev::ld_volatile(a.skip)) return;
     // every warp reads the sweep's epoch before the last warp out bumps it
     const int epoch = dev::ld_volatile(a.epoch);
-    for (;;) {
-        int t0 = 0;
-        if (lane == 0) t0 = atomicAdd(a.counters, 1) * a.chunk;
-        t0 = __shfl_sync(0xffffffffu, t0, 0);
-        if (t0 >= a.ntasks) break;
-        const int tend = min(a.ntasks, t0 + a.chunk);
-        for (int t = t0; t < tend; ++t) {
-            const int task = a.tasks[t];
-            const RowSys d = a.task_sys ? a.sys[a.task_sys[t]] : a.sys0;
-            if (MODE == 1) row_nnz<io, LOWER, 1>(d, task, epoch, a.status, lane);
-            else if (MODE == 2) row_nnz<io, LOWER, 2>(d, task, epoch, a.status, lane);
-            else if (MODE == 4) row_nnz<io, LOWER, 4>(d, task, epoch, a.status, lane);
-            else if (MODE == 8) row_nnz<io, LOWER, 8>(d, task, epoch, a.status, lane);
-            else if (MODE == 16) row_rhs<io, LOWER, 16, 1>(d, task, epoch, a.status, lane);
-            else if (MODE == 32) row_rhs<io, LOWER, 32, 1>(d, task, epoch, a.status, lane);
-            else if (MODE == 64) row_rhs<io, LOWER, 32, 2>(d, task, epoch, a.status, lane);
-            else if (MODE == 128) row_rhs<io, LOWER, 32, 4>(d, task, epoch, a.status, lane);
-            else {
-                if (d.nrhs <= 8) row_nnz<io, LOWER, 8>(d, task, epoch, a.status, lane);
-                else row_rhs<io, LOWER, 32, 4>(d, task, epoch, a.status, lane);
+    auto run = [&](const RowSys& d, int task, int s, int e) {
+        if (MODE == 1) row_nnz<io, LOWER, 1>(d, task, s, e, epoch, a.status, lane);
+        else if (MODE == 2) row_nnz<io, LOWER, 2>(d, task, s, e, epoch, a.status, lane);
+        else if (MODE == 4) row_nnz<io, LOWER, 4>(d, task, s, e, epoch, a.status, lane);
+        else if (MODE == 8) row_nnz<io, LOWER, 8>(d, task, s, e, epoch, a.status, lane);
+        else if (MODE == 16) row_rhs<io, LOWER, 16, 1>(d, task, s, e, epoch, a.status, lane);
+        else if (MODE == 32) row_rhs<io, LOWER, 32, 1>(d, task, s, e, epoch, a.status, lane);
+        else if (MODE == 64) row_rhs<io, LOWER, 32, 2>(d, task, s, e, epoch, a.status, lane);
+        else if (MODE == 128) row_rhs<io, LOWER, 32, 4>(d, task, s, e, epoch, a.status, lane);
+        else {
+            if (d.nrhs <= 8) row_nnz<io, LOWER, 8>(d, task, s, e, epoch, a.status, lane);
+            else row_rhs<io, LOWER, 32, 4>(d, task, s, e, epoch, a.status, lane);
+        }
+    };
+    auto row_range = [&](const RowSys& d, int task, int& s, int& e) {
+        const int row = task < 0 ? ~task : task;
+        s = d.rowptr[row];
+        e = d.rowptr[row + 1];
+    };
+    if (a.chunk == 1 && !a.task_sys) {
+        // One task per ticket, the next ticket, task and row range fetched
+        // while the current row is solved (a warp holds at most two tickets
+        // and solves them in ticket order, so waits still point only to
+        // smaller tickets).
+        int t = 0;
+        if (lane == 0) t = atomicAdd(a.counters, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        int task = 0, s = 0, e = 0;
+        if (t < a.ntasks) {
+            task = a.tasks[t];
+            row_range(a.sys0, task, s, e);
+        }
+        while (t < a.ntasks) {
+            int tn = 0;
+            if (lane == 0) tn = atomicAdd(a.counters, 1);
+            tn = __shfl_sync(0xffffffffu, tn, 0);
+            int taskn = 0, sn = 0, en = 0;
+            if (tn < a.ntasks) {
+                taskn = a.tasks[tn];
+                row_range(a.sys0, taskn, sn, en);
+            }
+            run(a.sys0, task, s, e);
+            t = tn;
+            task = taskn;
+            s = sn;
+            e = en;
+        }
+    } else {
+        for (;;) {
+            int t0 = 0;
+            if (lane == 0) t0 = atomicAdd(a.counters, 1) * a.chunk;
+            t0 = __shfl_sync(0xffffffffu, t0, 0);
+            if (t0 >= a.ntasks) break;
+            const int tend = min(a.ntasks, t0 + a.chunk);
+            for (int t = t0; t < tend; ++t) {
+                const int task = a.tasks[t];
+                const RowSys d = a.task_sys ? a.sys[a.task_sys[t]] : a.sys0;
+                int s, e;
+                row_range(d, task, s, e);
+                run(d, task, s, e);
             }
         }
     }
