@@ -9,8 +9,8 @@
 //     nonzeros (coalesced index/value loads, warp-shuffle reduction); for more
 //     RHS the lanes split the RHS columns, so x loads are coalesced, and the
 //     row's (col, val) pairs are loaded 32 at a time and broadcast by shuffle;
-//   * flags of a batch of entries are read together with relaxed loads and
-//     one acquire fence (no dependent acquire per nonzero);
+//   * flags of a batch of entries are read together, one acquire load per
+//     lane (no dependent acquire per nonzero, no separate fence);
 //   * persistent grid; warps take tasks (in level order) by an atomic ticket,
 //     so a warp only waits on tasks with smaller tickets, all taken by running
 //     warps (no deadlock); the last warp out resets the ticket;
@@ -91,13 +91,14 @@ __device__ __forceinline__ void row_nnz(const RowSys& d, int task, int s, int e,
             c[u] = k < hi ? d.cols[k] : -1;
             v[u] = k < hi ? vals[k] : T(0);
         }
+        // acquire loads of the flags (no separate fence); a flag not yet set
+        // is waited for with acquire loads too
         int f[2];
 #pragma unroll
-        for (int u = 0; u < 2; ++u) f[u] = c[u] >= 0 ? dev::ld_volatile(d.flags + c[u]) : epoch;
+        for (int u = 0; u < 2; ++u) f[u] = c[u] >= 0 ? dev::ld_acquire(d.flags + c[u]) : epoch;
 #pragma unroll
         for (int u = 0; u < 2; ++u)
             if (f[u] < epoch) dev::wait_geq(d.flags + c[u], epoch, status);
-        dev::fence_acquire();
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
             if (c[u] < 0) continue;
@@ -158,10 +159,9 @@ __device__ __forceinline__ void row_rhs(const RowSys& d, int task, int s, int e,
         const T myv = k < hi ? vals[k] : T(0);
         // every lane waits for its own entry, then the warp consumes the 32
         // entries without further waits (independent loads in flight)
-        if (k < hi && dev::ld_volatile(d.flags + mycol) < epoch)
+        if (k < hi && dev::ld_acquire(d.flags + mycol) < epoch)
             dev::wait_geq(d.flags + mycol, epoch, status);
-        dev::fence_acquire();
-        __syncwarp();
+        __syncwarp();  // orders every lane's observation before the warp's x loads
         const int cnt = min(32, hi - base);
         const int steps = (cnt + NG - 1) / NG;
 #pragma unroll 8
