@@ -95,9 +95,11 @@ struct PlanOptions {
     int32_t min_top_width = 8;  // supernodes at least this wide (and their ancestors) are top
     // units with more than part_keep + part_group contribution blocks keep
     // their last part_keep blocks and hand the others to partial sums of
-    // about part_group blocks each (0: no partial sums)
+    // about part_group blocks each (0: no partial sums, the default: with
+    // the estimated-start ticket order and the folded chain step, partial
+    // sums measured slower on every RHS count)
     int32_t part_keep = 16;
-    int32_t part_group = 32;
+    int32_t part_group = 0;
 };
 
 // Builds the plan from a factor and the level orders of L and L^T (rows

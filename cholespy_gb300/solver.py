@@ -252,7 +252,7 @@ class _CholeskySolver:
         """Preallocate scratch for up to n_rhs RHS (before CUDA-graph capture)."""
         _ffi.check(_ffi.lib().gbchol_reserve(self._h, int(n_rhs)))
 
-    def replan(self, min_top_width=8, part_keep=16, part_group=32):
+    def replan(self, min_top_width=8, part_keep=16, part_group=0):
         """Rebuild the solve plan with other tuning parameters (gbchol_replan):
         supernodes at least `min_top_width` columns wide and their ancestors
         are solved as dense blocks; long block lists keep `part_keep` blocks

@@ -242,7 +242,8 @@ int gbchol_reserve(gbchol_handle h, int32_t nrhs);
  * min_top_width columns wide (and their ancestors) form the supernodal top
  * region (default 8); lower-sweep contribution lists longer than
  * part_keep + part_group keep their last part_keep blocks and hand the rest
- * to partial sums of about part_group blocks (defaults 16 and 32; 0: none).
+ * to partial sums of about part_group blocks (defaults 16 and 0; 0: no
+ * partial sums).
  * Results change only by rounding. Synchronises the device. A batch built
  * from this solver before the call refuses to solve (GBCHOL_ESTATE): build it
  * again. No counterpart in the reference.
