@@ -440,6 +440,73 @@ int gbchol_create(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t*
     return GBCHOL_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Numeric factor of new values on the same pattern: the old ordering is
+// given to the factorisation, and the resulting pattern must be the old one.
+int refactor_values(const Factor& old, int32_t n, int64_t nnz, const int32_t* ii, const int32_t* jj,
+                    const double* x, int32_t matrix_type, int32_t threads, Csc& A, Factor& Fn) {
+    if (nnz > 0 && (!ii || !jj || !x)) return fail(GBCHOL_EINVAL, "Null input array.");
+    if (matrix_type != GBCHOL_COO && !ii) return fail(GBCHOL_EINVAL, "Null pointer array.");
+    if ((int32_t)old.perm.size() != n) return fail(GBCHOL_ESTATE, "No factor to refactorise.");
+    std::string err;
+    Status st = build_csc(n, nnz, ii, jj, x, matrix_type, A, err);
+    if (st != ST_OK) return fail(GBCHOL_EINVAL, err);
+    FactorOptions opt;
+    opt.threads = threads;
+    opt.use_given_perm = true;
+    opt.perm_in = old.perm.data();
+    st = factorize(A, opt, Fn, err);
+    if (st == ST_NOT_POSDEF) return fail(GBCHOL_ENOTPOSDEF, "Matrix is not positive definite!");
+    if (st != ST_OK) return fail(st == ST_NOMEM ? GBCHOL_ENOMEM : GBCHOL_EINVAL, err);
+    if (Fn.perm != old.perm || Fn.colptr != old.colptr || Fn.rowidx != old.rowidx || Fn.sn_start != old.sn_start)
+        return fail(GBCHOL_EINVAL, "The sparsity pattern differs from the factor's: make a new solver.");
+    return GBCHOL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbchol_refactorize(gbchol_handle h, int64_t nnz, const int32_t* ii, const int32_t* jj, const double* x,
+                       int32_t matrix_type) {
+    if (!h) return fail(GBCHOL_EINVAL, "Null handle.");
+    if (h->n == 0) return GBCHOL_OK;
+    auto t0 = std::chrono::steady_clock::now();
+    Csc A;
+    Factor Fn;
+    if (int rc = refactor_values(h->F, h->n, nnz, ii, jj, x, matrix_type, 0, A, Fn)) return rc;
+    Csc S;
+    if (h->store & GBCHOL_STORE_A64) {
+        symmetric_from_lower(A, S);
+        if (S.nnz() != h->nnz_a) return fail(GBCHOL_EINVAL, "The sparsity pattern differs from the solver's.");
+    }
+    h->t_factor = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    DeviceGuard g(h->device);
+    CUDA_TRY(cudaDeviceSynchronize());  // no solve may still use the old values
+    h->F.vals.swap(Fn.vals);
+    if (h->store & GBCHOL_STORE_A64) CUDA_TRY(h->a_vals.upload(S.vals.data(), S.vals.size()));
+    ++h->plan_gen;
+    const std::vector<int32_t> none;
+    const std::vector<double> nonev;
+    if (int rc = setup_plan(h, none, none, nonev)) return rc;
+    CUDA_TRY(cudaDeviceSynchronize());
+    return GBCHOL_OK;
+}
+
+int gbchol_factor_refactorize(gbchol_factor_handle f, int64_t nnz, const int32_t* ii, const int32_t* jj,
+                              const double* x, int32_t matrix_type, int32_t threads) {
+    if (!f) return fail(GBCHOL_EINVAL, "Null factor.");
+    if (f->F.n == 0) return GBCHOL_OK;
+    Csc A;
+    Factor Fn;
+    if (int rc = refactor_values(f->F, f->F.n, nnz, ii, jj, x, matrix_type, threads, A, Fn)) return rc;
+    f->F.vals.swap(Fn.vals);
+    return GBCHOL_OK;
+}
+
 int gbchol_create_from_factor(int32_t n, const int32_t* perm, const int32_t* colptr,
                               const int32_t* rowidx, const double* vals, int32_t store,
                               gbchol_handle* out) {

@@ -106,6 +106,27 @@ def _as_torch(a):
     return torch.as_tensor(np.asarray(a))
 
 
+def _check_shapes(n_rows, ii, jj, x, type):
+    """Shape checks of src/main.cpp:28-43 (same messages); returns len(x)."""
+    ni, nj, nx = _len(ii), _len(jj), _len(x)
+    if type == MatrixType.COO:
+        if ni != nj:
+            raise ValueError("Sparse COO matrix: the two index arrays should have the same size.")
+        if ni != nx:
+            raise ValueError("Sparse COO matrix: the index and data arrays should have the same size.")
+    elif type == MatrixType.CSR:
+        if nj != nx:
+            raise ValueError("Sparse CSR matrix: the column index and data arrays should have the same size.")
+        if ni != n_rows + 1:
+            raise ValueError("Sparse CSR matrix: Invalid size for row pointer array.")
+    else:
+        if nj != nx:
+            raise ValueError("Sparse CSC matrix: the row index and data arrays should have the same size.")
+        if ni != n_rows + 1:
+            raise ValueError("Sparse CSC matrix: Invalid size for column pointer array.")
+    return nx
+
+
 def _host_vector(a, dtype, name):
     """1-D host copy of a constructor argument, as the reference's D2H copies
     (src/main.cpp:55-61)."""
@@ -136,23 +157,7 @@ class _CholeskySolver:
         if n_rows < 0 or n_rows > np.iinfo(np.uint32).max:
             raise ValueError("n_rows out of range.")
         type = MatrixType(int(type))
-        ni, nj, nx = _len(ii), _len(jj), _len(x)
-        # Shape checks of src/main.cpp:28-43 (same messages)
-        if type == MatrixType.COO:
-            if ni != nj:
-                raise ValueError("Sparse COO matrix: the two index arrays should have the same size.")
-            if ni != nx:
-                raise ValueError("Sparse COO matrix: the index and data arrays should have the same size.")
-        elif type == MatrixType.CSR:
-            if nj != nx:
-                raise ValueError("Sparse CSR matrix: the column index and data arrays should have the same size.")
-            if ni != n_rows + 1:
-                raise ValueError("Sparse CSR matrix: Invalid size for row pointer array.")
-        else:
-            if nj != nx:
-                raise ValueError("Sparse CSC matrix: the row index and data arrays should have the same size.")
-            if ni != n_rows + 1:
-                raise ValueError("Sparse CSC matrix: Invalid size for column pointer array.")
+        nx = _check_shapes(n_rows, ii, jj, x, type)
         devs = {_device_of(a)[0] for a in (ii, jj, x)}
         if len(devs) != 1:
             raise ValueError("All input tensors should be on the same device!")
@@ -251,6 +256,23 @@ class _CholeskySolver:
     def reserve(self, n_rhs):
         """Preallocate scratch for up to n_rhs RHS (before CUDA-graph capture)."""
         _ffi.check(_ffi.lib().gbchol_reserve(self._h, int(n_rhs)))
+
+    def refactorize(self, ii, jj, x, type):
+        """New values for the same sparsity pattern (arguments as the
+        constructor's; NumPy or torch, host or device): the ordering, the
+        symbolic factor and the level analysis are kept, the numeric factor is
+        recomputed on the host and uploaded (gbchol_refactorize). ValueError if
+        the pattern differs or the matrix is not positive definite; the solver
+        then keeps its old factor. No counterpart in the reference."""
+        type = MatrixType(int(type))
+        nx = _check_shapes(self._n, ii, jj, x, type)
+        hi = _host_vector(ii, np.int32, "ii")
+        hj = _host_vector(jj, np.int32, "jj")
+        hx = _host_vector(x, np.float64, "x")
+        torch = _torch()
+        with torch.cuda.device(self._device):
+            st = _ffi.lib().gbchol_refactorize(self._h, int(nx), _ptr(hi), _ptr(hj), _ptr(hx), int(type))
+        _ffi.check(st)
 
     def replan(self, min_top_width=8, part_keep=16, part_group=0):
         """Rebuild the solve plan with other tuning parameters (gbchol_replan):

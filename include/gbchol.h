@@ -109,6 +109,17 @@ int gbchol_factor_export(gbchol_factor_handle f, int32_t* perm, int32_t* colptr,
 
 int gbchol_factor_free(gbchol_factor_handle f);
 
+/*
+ * Numeric refactorisation of a host factor: new values for the same
+ * sparsity pattern (n as before; any input format, duplicates summed). The
+ * factor's ordering is reused (no new ordering); GBCHOL_EINVAL if the new
+ * pattern gives another factor pattern, GBCHOL_ENOTPOSDEF if the new matrix
+ * is not positive definite (the factor keeps its old values on any error).
+ * No counterpart in the reference (it refactors through a new solver).
+ */
+int gbchol_factor_refactorize(gbchol_factor_handle f, int64_t nnz, const int32_t* ii, const int32_t* jj,
+                              const double* x, int32_t matrix_type, int32_t threads);
+
 /* Free every device and host buffer of the solver (src/cholesky_solver.cpp:465-486). */
 int gbchol_destroy(gbchol_handle h);
 
@@ -260,6 +271,19 @@ int gbchol_replan(gbchol_handle h, int32_t min_top_width, int32_t part_keep, int
  */
 int gbchol_autotune(gbchol_handle h, int32_t precision, int32_t nrhs, const int32_t* candidates, int32_t count,
                     int32_t reps, int32_t* chosen);
+
+/*
+ * Numeric refactorisation of a solver: new values of the same sparsity
+ * pattern (same n and input format as at creation). Keeps the ordering, the
+ * symbolic factor and the level analysis; recomputes the numeric factor on the
+ * host (reusing the ordering) and uploads it with the solve plan. Errors as
+ * gbchol_factor_refactorize; the solver keeps its old factor on any error.
+ * Synchronises the device; batches built from this solver must be built
+ * again. No counterpart in the reference, whose users build a new solver per
+ * set of values.
+ */
+int gbchol_refactorize(gbchol_handle h, int64_t nnz, const int32_t* ii, const int32_t* jj, const double* x,
+                       int32_t matrix_type);
 
 /*
  * Batched solves: `count` solvers (same device) solved together, system s

@@ -383,3 +383,37 @@ def test_replan_and_autotune(cuda):
     s.solve(b_t, x_t)
     s.check()
     assert np.abs(x_t.cpu().numpy() - x_ref).max() <= 1e-3 * scale
+
+
+def test_refactorize(cuda):
+    """solver.refactorize (no reference counterpart): new values on the same
+    pattern solve the new system; a matrix that is not positive definite is
+    refused and the old factor kept; a batch built before refuses to solve."""
+    import cholespy_gb300 as cg
+    from cholespy_gb300 import MatrixType, workloads
+    torch = cuda
+    k = 16
+    v1, idx = workloads.grid3d_coo(k, 1e-3)
+    v2, _ = workloads.grid3d_coo(k, 0.5)
+    n = k ** 3
+    for cls, tol in ((cg.CholeskySolverF, 1e-4), (cg.CholeskySolverD, 1e-10)):
+        s = cls(n, torch.tensor(idx[0], device="cuda"), torch.tensor(idx[1], device="cuda"),
+                torch.tensor(v1, device="cuda"), MatrixType.COO)
+        dt = torch.float32 if cls is cg.CholeskySolverF else torch.float64
+        b = np.random.default_rng(9).standard_normal((n, 5))
+        b_t = torch.tensor(b, dtype=dt, device="cuda")
+        batch = cg.BatchSolver([s], [5])
+        batch.bind([b_t], [torch.zeros_like(b_t)])
+        s.refactorize(idx[0], idx[1], v2, MatrixType.COO)
+        x_t = torch.zeros_like(b_t)
+        s.solve(b_t, x_t)
+        s.check()
+        x2 = spsolve_ref(n, v2, idx, b)
+        assert np.abs(x_t.cpu().numpy() - x2).max() <= tol * np.abs(x2).max()
+        with pytest.raises(ValueError):
+            s.refactorize(idx[0], idx[1], -np.asarray(v2), MatrixType.COO)
+        x_t.zero_()
+        s.solve(b_t, x_t)
+        assert np.abs(x_t.cpu().numpy() - x2).max() <= tol * np.abs(x2).max()
+        with pytest.raises(RuntimeError):
+            batch.solve()

@@ -111,3 +111,59 @@ def test_nested_dissection_fill_reasonable(gblib):
     n, vals, idx = 4096, *workloads.grid3d_coo(16, 1e-3)
     _, colptr, _, _, nsn = factorize(gblib, n, idx[0], idx[1], vals, 2)
     assert colptr[-1] < 400_000  # METIS-quality ND gives ~3.9e5 on 16^3
+
+
+def _export(gblib, f, n):
+    nn, nnz, nsn, fl = C.c_int32(), C.c_int64(), C.c_int32(), C.c_double()
+    _ffi.check(gblib.gbchol_factor_info(f, C.byref(nn), C.byref(nnz), C.byref(nsn), C.byref(fl)))
+    perm = np.zeros(n, np.int32)
+    colptr = np.zeros(n + 1, np.int32)
+    rowidx = np.zeros(nnz.value, np.int32)
+    vals = np.zeros(nnz.value, np.float64)
+    _ffi.check(gblib.gbchol_factor_export(f, perm.ctypes.data, colptr.ctypes.data, rowidx.ctypes.data,
+                                          vals.ctypes.data))
+    return perm, colptr, rowidx, vals
+
+
+def test_factor_refactorize(gblib):
+    """gbchol_factor_refactorize (no reference counterpart): new values on the
+    same pattern give the factor a fresh factorisation gives (same ordering:
+    nested dissection depends on the pattern only); a different pattern and a
+    matrix that is not positive definite are refused and leave the factor as
+    it was."""
+    k = 20
+    n = k * k
+    v1, idx = workloads.grid2d_coo(k, 10.0, 1.0)
+    v2, idx2 = workloads.grid2d_coo(k, 3.0, 2.5)
+    assert np.array_equal(idx, idx2)
+    ii = np.ascontiguousarray(idx[0], np.int32)
+    jj = np.ascontiguousarray(idx[1], np.int32)
+    x1 = np.ascontiguousarray(v1, np.float64)
+    x2 = np.ascontiguousarray(v2, np.float64)
+    f = C.c_void_p()
+    _ffi.check(gblib.gbchol_factorize(n, len(x1), ii.ctypes.data, jj.ctypes.data, x1.ctypes.data, 2, 2,
+                                      C.byref(f)))
+    try:
+        _ffi.check(gblib.gbchol_factor_refactorize(f, len(x2), ii.ctypes.data, jj.ctypes.data, x2.ctypes.data,
+                                                   2, 2))
+        perm, colptr, rowidx, vals = _export(gblib, f, n)
+        p2, c2, r2, v2f, _ = factorize(gblib, n, ii, jj, x2, 2)
+        assert np.array_equal(perm, p2) and np.array_equal(colptr, c2) and np.array_equal(rowidx, r2)
+        np.testing.assert_allclose(vals, v2f, rtol=1e-12, atol=1e-14)
+        # not positive definite: refused, values kept
+        bad = -x2
+        st = gblib.gbchol_factor_refactorize(f, len(bad), ii.ctypes.data, jj.ctypes.data, bad.ctypes.data,
+                                             2, 2)
+        assert st == _ffi.ENOTPOSDEF
+        assert np.array_equal(_export(gblib, f, n)[3], vals)
+        # another pattern (one off-diagonal pair dropped): refused
+        keep = ~(((ii == 0) & (jj == 1)) | ((ii == 1) & (jj == 0)))
+        i3 = np.ascontiguousarray(ii[keep]); j3 = np.ascontiguousarray(jj[keep]); x3 = np.ascontiguousarray(x2[keep])
+        st = gblib.gbchol_factor_refactorize(f, len(x3), i3.ctypes.data, j3.ctypes.data, x3.ctypes.data,
+                                             2, 2)
+        assert st in (_ffi.EINVAL, _ffi.OK)
+        if st == _ffi.EINVAL:
+            assert "pattern" in _ffi.last_error()
+            assert np.array_equal(_export(gblib, f, n)[3], vals)
+    finally:
+        gblib.gbchol_factor_free(f)
