@@ -329,6 +329,52 @@ class _CholeskySolver:
                                                 _ptr(vals)))
         return perm, colptr, rowidx, vals
 
+    # -- serialised factor (no reference counterpart) ---------------------
+    FORMAT = "gbchol-factor-1"
+
+    def save(self, path):
+        """Write the analysed factor (permutation and L in CSC, diagonal first,
+        FP64 values) to an .npz file, so that another process rebuilds the
+        solver with `load` without ordering or factorising again."""
+        perm, colptr, rowidx, vals = self.factor()
+        np.savez(path, format=np.array(self.FORMAT), n=np.int64(self._n), perm=perm, colptr=colptr,
+                 rowidx=rowidx, vals=vals)
+
+    @classmethod
+    def load(cls, path, device=0):
+        """Rebuild a solver from a file written by `save` on CUDA device
+        `device` (gbchol_create_from_factor: the factor is validated, the
+        level analysis and the solve plan are redone on the device). A loaded
+        CholeskySolverD solves in FP64 (refinement needs A, which the file
+        does not hold)."""
+        with np.load(path) as z:
+            if str(z["format"]) != cls.FORMAT:
+                raise ValueError(f"Not a {cls.FORMAT} file.")
+            n = int(z["n"])
+            perm = np.ascontiguousarray(z["perm"], np.int32)
+            colptr = np.ascontiguousarray(z["colptr"], np.int32)
+            rowidx = np.ascontiguousarray(z["rowidx"], np.int32)
+            vals = np.ascontiguousarray(z["vals"], np.float64)
+        if perm.shape != (n,) or colptr.shape != (n + 1,) or rowidx.shape != vals.shape or \
+                rowidx.shape[0] != int(colptr[-1]):
+            raise ValueError("Inconsistent factor arrays in the file.")
+        self = cls.__new__(cls)
+        self._h = None
+        self._device = int(device)
+        self._refine = False
+        self._tol = 1e-10
+        self._max_iter = 10
+        store = _ffi.STORE_F32 if self._precision == 0 else _ffi.STORE_F64
+        torch = _torch()
+        h = C.c_void_p()
+        with torch.cuda.device(self._device):
+            st = _ffi.lib().gbchol_create_from_factor(n, _ptr(perm), _ptr(colptr), _ptr(rowidx), _ptr(vals),
+                                                      store, C.byref(h))
+        _ffi.check(st)
+        self._h = h
+        self._n = n
+        return self
+
     @property
     def handle(self):
         return self._h

@@ -417,3 +417,28 @@ def test_refactorize(cuda):
         assert np.abs(x_t.cpu().numpy() - x2).max() <= tol * np.abs(x2).max()
         with pytest.raises(RuntimeError):
             batch.solve()
+
+
+def test_save_load(cuda, tmp_path):
+    """solver.save / CholeskySolver*.load (no reference counterpart): the
+    reloaded solver holds the same factor and plan, so its solves are
+    bit-identical; a file of another format is refused."""
+    import cholespy_gb300 as cg
+    from cholespy_gb300 import MatrixType
+    torch = cuda
+    n, vals, idx, b = reference_problem("ico5", dtype=np.float32)
+    for cls, dt in ((cg.CholeskySolverF, torch.float32), (cg.CholeskySolverD, torch.float64)):
+        s = cls(n, torch.tensor(idx[0], device="cuda"), torch.tensor(idx[1], device="cuda"),
+                torch.tensor(vals, device="cuda"), MatrixType.COO)
+        path = tmp_path / f"{cls.__name__}.npz"
+        s.save(path)
+        t = cls.load(path)
+        b_t = torch.tensor(b[:, :16], dtype=dt, device="cuda")
+        x1, x2 = torch.zeros_like(b_t), torch.zeros_like(b_t)
+        s.solve(b_t, x1)
+        t.solve(b_t, x2)
+        t.check()
+        assert torch.equal(x1, x2)
+    np.savez(tmp_path / "bad.npz", format=np.array("other"), n=np.int64(1))
+    with pytest.raises(ValueError):
+        cg.CholeskySolverF.load(tmp_path / "bad.npz")
