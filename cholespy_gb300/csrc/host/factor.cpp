@@ -254,13 +254,59 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
         int32_t last = F.sn_start[s + 1] - 1;
         if (parent[last] >= 0) sn_nchild[sn_of[parent[last]]]++;
     }
+    // A finished front is handed to its parent whole: its trailing m x m
+    // block (leading dimension Fsz) is the update matrix, so nothing is
+    // copied. Large extend-adds and column copies run in parallel over
+    // columns (each writes its own destination column); the arithmetic and
+    // its order are those of a serial run, so results do not depend on the
+    // thread count.
     struct Update {
         int32_t sn;
-        std::vector<double> u;  // m x m, column-major, lower part valid
+        int64_t fsz, w;          // the front's size and the supernode's width
+        std::vector<double> u;   // the whole front, column-major; the update is u[w.., w..]
     };
     std::vector<Update> stack;
     std::vector<int32_t> relpos((size_t)n, -1);
     std::vector<double> front;
+    constexpr int64_t kParCols = 256;  // columns from which copies go parallel
+    // Consumed fronts are kept for reuse (best fit by capacity, at most 8):
+    // a fresh multi-megabyte buffer per front costs its page faults.
+    std::vector<std::vector<double>> pool;
+    auto recycle = [&](std::vector<double>& v) {
+        if (v.capacity() == 0) return;
+        pool.push_back(std::move(v));
+        v = std::vector<double>();
+        if (pool.size() > 8) {  // drop the smallest
+            size_t k = 0;
+            for (size_t i = 1; i < pool.size(); ++i)
+                if (pool[i].capacity() < pool[k].capacity()) k = i;
+            pool.erase(pool.begin() + (std::ptrdiff_t)k);
+        }
+    };
+    auto take = [&](size_t need) {
+        std::vector<double> v;
+        size_t best = pool.size();
+        for (size_t i = 0; i < pool.size(); ++i)
+            if (pool[i].capacity() >= need && (best == pool.size() || pool[i].capacity() < pool[best].capacity()))
+                best = i;
+        if (best == pool.size() && !pool.empty()) {  // none fits: grow the largest
+            best = 0;
+            for (size_t i = 1; i < pool.size(); ++i)
+                if (pool[i].capacity() > pool[best].capacity()) best = i;
+        }
+        if (best < pool.size()) {
+            v = std::move(pool[best]);
+            pool.erase(pool.begin() + (std::ptrdiff_t)best);
+        }
+        if (v.size() < need) v.resize(need);
+        return v;
+    };
+    // Only the lower triangle of a front is ever read (assembly, the dense
+    // kernels and the update all stay on or below the diagonal): zero that.
+    auto zero_lower = [&](double* a, int64_t fsz) {
+#pragma omp parallel for num_threads(threads) schedule(static) if (threads > 1 && fsz >= kParCols)
+        for (int64_t j = 0; j < fsz; ++j) std::fill(a + j * fsz + j, a + (j + 1) * fsz, 0.0);
+    };
     double flops = 0.0;
     for (int32_t s = 0; s < nsn; ++s) {
         const int32_t f = F.sn_start[s], l1 = F.sn_start[s + 1];
@@ -269,7 +315,9 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
         const int64_t Fsz = F.colptr[f + 1] - F.colptr[f];
         const int64_t m = Fsz - w;
         for (int64_t i = 0; i < Fsz; ++i) relpos[rows[i]] = (int32_t)i;
-        front.assign((size_t)(Fsz * Fsz), 0.0);
+        recycle(front);
+        front = take((size_t)(Fsz * Fsz));
+        zero_lower(front.data(), Fsz);
         // assemble original entries of columns f..l1-1 (lower part)
         for (int32_t j = f; j < l1; ++j) {
             double* col = front.data() + (int64_t)(j - f) * Fsz;
@@ -279,14 +327,19 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
         for (int32_t c = 0; c < sn_nchild[s]; ++c) {
             Update& up = stack.back();
             const int32_t cf = F.sn_start[up.sn];
-            const int32_t cw = F.sn_start[up.sn + 1] - cf;
+            const int32_t cw = (int32_t)up.w;
             const int32_t* crows = F.rowidx.data() + F.colptr[cf] + cw;
-            const int64_t cm = (F.colptr[cf + 1] - F.colptr[cf]) - cw;
+            const int64_t cm = up.fsz - cw, ld = up.fsz;
+            const double* ub = up.u.data() + cw + cw * ld;  // update block (lower part)
+            double* fr = front.data();
+            const int32_t* rp = relpos.data();
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 16) if (threads > 1 && cm >= kParCols)
             for (int64_t jj = 0; jj < cm; ++jj) {
-                double* dst = front.data() + (int64_t)relpos[crows[jj]] * Fsz;
-                const double* src = up.u.data() + jj * cm;
-                for (int64_t ii = jj; ii < cm; ++ii) dst[relpos[crows[ii]]] += src[ii];
+                double* dst = fr + (int64_t)rp[crows[jj]] * Fsz;
+                const double* src = ub + jj * ld;
+                for (int64_t ii = jj; ii < cm; ++ii) dst[rp[crows[ii]]] += src[ii];
             }
+            recycle(up.u);
             stack.pop_back();
         }
         // partial dense factorisation of the front
@@ -302,19 +355,23 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
         }
         flops += (double)w * w * w / 3.0 + (double)m * w * w + (double)m * m * w;
         // store the columns of L
-        for (int64_t j = 0; j < w; ++j) {
-            double* dst = F.vals.data() + F.colptr[f + j];
-            const double* src = front.data() + j + j * Fsz;
-            for (int64_t i = 0; i < Fsz - j; ++i) dst[i] = src[i];
+        {
+            double* vals = F.vals.data();
+            const int32_t* cp = F.colptr.data();
+            const double* fr = front.data();
+#pragma omp parallel for num_threads(threads) schedule(static) if (threads > 1 && w * Fsz >= kParCols * kParCols)
+            for (int64_t j = 0; j < w; ++j) {
+                double* dst = vals + cp[f + j];
+                const double* src = fr + j + j * Fsz;
+                for (int64_t i = 0; i < Fsz - j; ++i) dst[i] = src[i];
+            }
         }
         if (m > 0 && parent[l1 - 1] >= 0) {
             Update up;
             up.sn = s;
-            up.u.resize((size_t)(m * m));
-            for (int64_t jj = 0; jj < m; ++jj) {
-                const double* src = front.data() + w + (w + jj) * Fsz;
-                std::copy(src + jj, src + m, up.u.data() + jj * m + jj);
-            }
+            up.fsz = Fsz;
+            up.w = w;
+            up.u.swap(front);  // the front itself carries the update
             stack.push_back(std::move(up));
         }
         for (int64_t i = 0; i < Fsz; ++i) relpos[rows[i]] = -1;
