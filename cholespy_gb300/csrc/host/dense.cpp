@@ -179,22 +179,18 @@ void trsm_rec(int64_t m, int64_t n, const double* L, int64_t ldl, double* B, int
 void trsm_right_lower_t(int64_t m, int64_t n, const double* L, int64_t ldl, double* B, int64_t ldb,
                         int threads) {
     if (m <= 0 || n <= 0) return;
-    // Rows of B are independent: split them across threads when large.
+    // Rows of B are independent: solve them in fixed blocks of kRows rows
+    // (a multiple of the micro-kernel's MR), spread over threads when large.
+    // The blocks do not depend on the thread count, and neither do the results.
+    constexpr int64_t kRows = 256;
+    const int64_t chunks = (m + kRows - 1) / kRows;
     const double work = (double)m * (double)n * (double)n;
-    if (threads > 1 && work > 8.0e6 && m >= 256) {
-        int64_t chunks = std::min<int64_t>(threads * 2, (m + 127) / 128);
-        int64_t rows = (m + chunks - 1) / chunks;
-        rows = (rows + 7) / 8 * 8;
-#pragma omp parallel for num_threads(threads) schedule(dynamic, 1)
-        for (int64_t c = 0; c < chunks; ++c) {
-            int64_t r0 = c * rows;
-            if (r0 >= m) continue;
-            int64_t mr = std::min(rows, m - r0);
-            trsm_rec(mr, n, L, ldl, B + r0, ldb, 1);
-        }
-        return;
+    const int nt = (threads > 1 && work > 8.0e6) ? (int)std::min<int64_t>(threads, chunks) : 1;
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 1) if (nt > 1)
+    for (int64_t c = 0; c < chunks; ++c) {
+        const int64_t r0 = c * kRows;
+        trsm_rec(std::min(kRows, m - r0), n, L, ldl, B + r0, ldb, 1);
     }
-    trsm_rec(m, n, L, ldl, B, ldb, 1);
 }
 
 int64_t potrf_lower(int64_t n, double* A, int64_t lda, int threads) {

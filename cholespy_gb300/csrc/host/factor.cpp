@@ -245,137 +245,204 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     const int32_t nsn = (int32_t)F.sn_start.size() - 1;
 
     // ---- multifrontal numeric factorisation -----------------------------
+    // Supernodes whose subtree holds more than 1/(4 threads) of the flops (a
+    // set closed towards the roots) are factorised last, one after the other,
+    // with multi-threaded dense kernels; every subtree hanging below that set
+    // is an independent task, factorised by one thread. A finished front is
+    // kept whole and handed to its parent: its trailing m x m block (leading
+    // dimension Fsz) is the update. A parent adds its children's updates in
+    // reverse child order, the order of a serial postorder stack, so results
+    // do not depend on the thread count.
     F.vals.assign((size_t)total, 0.0);
     std::vector<int32_t> sn_of((size_t)n);
     for (int32_t s = 0; s < nsn; ++s)
         for (int32_t j = F.sn_start[s]; j < F.sn_start[s + 1]; ++j) sn_of[j] = s;
-    std::vector<int32_t> sn_nchild((size_t)nsn, 0);
+    std::vector<int32_t> sn_parent((size_t)nsn, -1), child_ptr((size_t)nsn + 1, 0);
     for (int32_t s = 0; s < nsn; ++s) {
-        int32_t last = F.sn_start[s + 1] - 1;
-        if (parent[last] >= 0) sn_nchild[sn_of[parent[last]]]++;
+        const int32_t last = F.sn_start[s + 1] - 1;
+        if (parent[last] >= 0) {
+            sn_parent[s] = sn_of[parent[last]];
+            child_ptr[sn_parent[s] + 1]++;
+        }
     }
-    // A finished front is handed to its parent whole: its trailing m x m
-    // block (leading dimension Fsz) is the update matrix, so nothing is
-    // copied. Large extend-adds and column copies run in parallel over
-    // columns (each writes its own destination column); the arithmetic and
-    // its order are those of a serial run, so results do not depend on the
-    // thread count.
-    struct Update {
-        int32_t sn;
-        int64_t fsz, w;          // the front's size and the supernode's width
-        std::vector<double> u;   // the whole front, column-major; the update is u[w.., w..]
-    };
-    std::vector<Update> stack;
-    std::vector<int32_t> relpos((size_t)n, -1);
-    std::vector<double> front;
-    constexpr int64_t kParCols = 256;  // columns from which copies go parallel
-    // Consumed fronts are kept for reuse (best fit by capacity, at most 8):
-    // a fresh multi-megabyte buffer per front costs its page faults.
-    std::vector<std::vector<double>> pool;
-    auto recycle = [&](std::vector<double>& v) {
-        if (v.capacity() == 0) return;
-        pool.push_back(std::move(v));
-        v = std::vector<double>();
-        if (pool.size() > 8) {  // drop the smallest
-            size_t k = 0;
-            for (size_t i = 1; i < pool.size(); ++i)
-                if (pool[i].capacity() < pool[k].capacity()) k = i;
-            pool.erase(pool.begin() + (std::ptrdiff_t)k);
-        }
-    };
-    auto take = [&](size_t need) {
-        std::vector<double> v;
-        size_t best = pool.size();
-        for (size_t i = 0; i < pool.size(); ++i)
-            if (pool[i].capacity() >= need && (best == pool.size() || pool[i].capacity() < pool[best].capacity()))
-                best = i;
-        if (best == pool.size() && !pool.empty()) {  // none fits: grow the largest
-            best = 0;
-            for (size_t i = 1; i < pool.size(); ++i)
-                if (pool[i].capacity() > pool[best].capacity()) best = i;
-        }
-        if (best < pool.size()) {
-            v = std::move(pool[best]);
-            pool.erase(pool.begin() + (std::ptrdiff_t)best);
-        }
-        if (v.size() < need) v.resize(need);
-        return v;
-    };
-    // Only the lower triangle of a front is ever read (assembly, the dense
-    // kernels and the update all stay on or below the diagonal): zero that.
-    auto zero_lower = [&](double* a, int64_t fsz) {
-#pragma omp parallel for num_threads(threads) schedule(static) if (threads > 1 && fsz >= kParCols)
-        for (int64_t j = 0; j < fsz; ++j) std::fill(a + j * fsz + j, a + (j + 1) * fsz, 0.0);
-    };
-    double flops = 0.0;
+    for (int32_t s = 0; s < nsn; ++s) child_ptr[s + 1] += child_ptr[s];
+    std::vector<int32_t> children((size_t)child_ptr[nsn]);
+    {
+        std::vector<int32_t> nx(child_ptr.begin(), child_ptr.end() - 1);
+        for (int32_t s = 0; s < nsn; ++s)  // children in increasing order
+            if (sn_parent[s] >= 0) children[nx[sn_parent[s]]++] = s;
+    }
+    std::vector<double> sn_flops((size_t)nsn), sub_flops((size_t)nsn);
+    std::vector<int32_t> first((size_t)nsn);  // first supernode of each subtree (postorder: contiguous)
+    double total_flops = 0.0;
     for (int32_t s = 0; s < nsn; ++s) {
+        const double w = F.sn_start[s + 1] - F.sn_start[s];
+        const double m = (double)(F.colptr[F.sn_start[s] + 1] - F.colptr[F.sn_start[s]]) - w;
+        sn_flops[s] = w * w * w / 3.0 + m * w * w + m * m * w;
+        total_flops += sn_flops[s];
+        sub_flops[s] = sn_flops[s];
+        first[s] = s;
+    }
+    for (int32_t s = 0; s < nsn; ++s)
+        if (sn_parent[s] >= 0) {
+            sub_flops[sn_parent[s]] += sub_flops[s];
+            first[sn_parent[s]] = std::min(first[sn_parent[s]], first[s]);
+        }
+    const double cut = threads > 1 ? total_flops / (4.0 * threads) : -1.0;
+    std::vector<char> top((size_t)nsn, 0);
+    for (int32_t s = 0; s < nsn; ++s) top[s] = sub_flops[s] > cut;
+
+    struct Front {
+        int64_t fsz = 0, w = 0;
+        std::vector<double> u;  // the whole front, column-major; the update is u[w.., w..]
+    };
+    std::vector<Front> upd((size_t)nsn);  // finished fronts waiting for their parent
+    constexpr int64_t kParCols = 256;     // columns from which copies go parallel
+    // per-thread scratch: row positions, and consumed fronts kept for reuse
+    // (best fit by capacity, at most 8): a fresh multi-megabyte buffer per
+    // front costs its page faults
+    struct Work {
+        std::vector<int32_t> relpos;
+        std::vector<std::vector<double>> pool;
+        void recycle(std::vector<double>& v) {
+            if (v.capacity() == 0) return;
+            pool.push_back(std::move(v));
+            v = std::vector<double>();
+            if (pool.size() > 8) {  // drop the smallest
+                size_t k = 0;
+                for (size_t i = 1; i < pool.size(); ++i)
+                    if (pool[i].capacity() < pool[k].capacity()) k = i;
+                pool.erase(pool.begin() + (std::ptrdiff_t)k);
+            }
+        }
+        std::vector<double> take(size_t need) {
+            std::vector<double> v;
+            size_t best = pool.size();
+            for (size_t i = 0; i < pool.size(); ++i)
+                if (pool[i].capacity() >= need && (best == pool.size() || pool[i].capacity() < pool[best].capacity()))
+                    best = i;
+            if (best == pool.size() && !pool.empty()) {  // none fits: grow the largest
+                best = 0;
+                for (size_t i = 1; i < pool.size(); ++i)
+                    if (pool[i].capacity() > pool[best].capacity()) best = i;
+            }
+            if (best < pool.size()) {
+                v = std::move(pool[best]);
+                pool.erase(pool.begin() + (std::ptrdiff_t)best);
+            }
+            if (v.size() < need) v.resize(need);
+            return v;
+        }
+    };
+    std::vector<Work> work((size_t)threads);
+
+    // Factorises supernode s with `dt` threads for its dense kernels and copies;
+    // false if a pivot is not positive.
+    auto factor_sn = [&](int32_t s, Work& wk, int dt) -> bool {
+        if (wk.relpos.empty()) wk.relpos.assign((size_t)n, -1);
+        int32_t* relpos = wk.relpos.data();
         const int32_t f = F.sn_start[s], l1 = F.sn_start[s + 1];
         const int64_t w = l1 - f;
         const int32_t* rows = F.rowidx.data() + F.colptr[f];
         const int64_t Fsz = F.colptr[f + 1] - F.colptr[f];
         const int64_t m = Fsz - w;
         for (int64_t i = 0; i < Fsz; ++i) relpos[rows[i]] = (int32_t)i;
-        recycle(front);
-        front = take((size_t)(Fsz * Fsz));
-        zero_lower(front.data(), Fsz);
-        // assemble original entries of columns f..l1-1 (lower part)
+        std::vector<double> front = wk.take((size_t)(Fsz * Fsz));
+        double* fr = front.data();
+        // only the lower triangle of a front is ever read (assembly, the dense
+        // kernels and the update all stay on or below the diagonal): zero that
+#pragma omp parallel for num_threads(dt) schedule(static) if (dt > 1 && Fsz >= kParCols)
+        for (int64_t j = 0; j < Fsz; ++j) std::fill(fr + j * Fsz + j, fr + (j + 1) * Fsz, 0.0);
+        // original entries of columns f..l1-1 (lower part)
         for (int32_t j = f; j < l1; ++j) {
-            double* col = front.data() + (int64_t)(j - f) * Fsz;
+            double* col = fr + (int64_t)(j - f) * Fsz;
             for (int32_t k = cptr[j]; k < cptr[j + 1]; ++k) col[relpos[crow[k]]] += cval[k];
         }
-        // extend-add the children's update matrices (top of the stack)
-        for (int32_t c = 0; c < sn_nchild[s]; ++c) {
-            Update& up = stack.back();
-            const int32_t cf = F.sn_start[up.sn];
+        // extend-add the children's updates, last child first
+        for (int32_t q = child_ptr[s + 1] - 1; q >= child_ptr[s]; --q) {
+            const int32_t c = children[q];
+            Front& up = upd[c];
+            const int32_t cf = F.sn_start[c];
             const int32_t cw = (int32_t)up.w;
             const int32_t* crows = F.rowidx.data() + F.colptr[cf] + cw;
             const int64_t cm = up.fsz - cw, ld = up.fsz;
             const double* ub = up.u.data() + cw + cw * ld;  // update block (lower part)
-            double* fr = front.data();
-            const int32_t* rp = relpos.data();
-#pragma omp parallel for num_threads(threads) schedule(dynamic, 16) if (threads > 1 && cm >= kParCols)
+#pragma omp parallel for num_threads(dt) schedule(dynamic, 16) if (dt > 1 && cm >= kParCols)
             for (int64_t jj = 0; jj < cm; ++jj) {
-                double* dst = fr + (int64_t)rp[crows[jj]] * Fsz;
+                double* dst = fr + (int64_t)relpos[crows[jj]] * Fsz;
                 const double* src = ub + jj * ld;
-                for (int64_t ii = jj; ii < cm; ++ii) dst[rp[crows[ii]]] += src[ii];
+                for (int64_t ii = jj; ii < cm; ++ii) dst[relpos[crows[ii]]] += src[ii];
             }
-            recycle(up.u);
-            stack.pop_back();
+            wk.recycle(up.u);
+            up = Front();
         }
         // partial dense factorisation of the front
-        int64_t bad = dense::potrf_lower(w, front.data(), Fsz, threads);
-        if (bad >= 0) {
-            err = "Matrix is not positive definite!";
-            return ST_NOT_POSDEF;
+        const int64_t bad = dense::potrf_lower(w, fr, Fsz, dt);
+        bool ok = bad < 0;
+        if (ok && m > 0) {
+            dense::trsm_right_lower_t(m, w, fr, Fsz, fr + w, Fsz, dt);
+            dense::gemm_nt_sub(m, m, w, fr + w, Fsz, fr + w, Fsz, fr + w + w * Fsz, Fsz, true, dt);
         }
-        if (m > 0) {
-            dense::trsm_right_lower_t(m, w, front.data(), Fsz, front.data() + w, Fsz, threads);
-            dense::gemm_nt_sub(m, m, w, front.data() + w, Fsz, front.data() + w, Fsz,
-                               front.data() + w + w * Fsz, Fsz, true, threads);
-        }
-        flops += (double)w * w * w / 3.0 + (double)m * w * w + (double)m * m * w;
-        // store the columns of L
-        {
+        if (ok) {  // store the columns of L
             double* vals = F.vals.data();
             const int32_t* cp = F.colptr.data();
-            const double* fr = front.data();
-#pragma omp parallel for num_threads(threads) schedule(static) if (threads > 1 && w * Fsz >= kParCols * kParCols)
+#pragma omp parallel for num_threads(dt) schedule(static) if (dt > 1 && w * Fsz >= kParCols * kParCols)
             for (int64_t j = 0; j < w; ++j) {
                 double* dst = vals + cp[f + j];
                 const double* src = fr + j + j * Fsz;
                 for (int64_t i = 0; i < Fsz - j; ++i) dst[i] = src[i];
             }
         }
-        if (m > 0 && parent[l1 - 1] >= 0) {
-            Update up;
-            up.sn = s;
-            up.fsz = Fsz;
-            up.w = w;
-            up.u.swap(front);  // the front itself carries the update
-            stack.push_back(std::move(up));
-        }
         for (int64_t i = 0; i < Fsz; ++i) relpos[rows[i]] = -1;
+        if (ok && m > 0 && sn_parent[s] >= 0) {
+            upd[s].fsz = Fsz;
+            upd[s].w = w;
+            upd[s].u.swap(front);  // the front itself carries the update
+        } else {
+            wk.recycle(front);
+        }
+        return ok;
+    };
+
+    // subtrees below the top set, largest first, one task each
+    std::vector<int32_t> roots;
+    for (int32_t s = 0; s < nsn; ++s)
+        if (!top[s] && (sn_parent[s] < 0 || top[sn_parent[s]])) roots.push_back(s);
+    std::stable_sort(roots.begin(), roots.end(),
+                     [&](int32_t a, int32_t b) { return sub_flops[a] > sub_flops[b]; });
+    int failed = 0;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1) if (threads > 1 && roots.size() > 1)
+    for (int64_t q = 0; q < (int64_t)roots.size(); ++q) {
+#ifdef _OPENMP
+        Work& wk = work[(size_t)omp_get_thread_num()];
+#else
+        Work& wk = work[0];
+#endif
+        const int32_t r = roots[q];
+        for (int32_t s = first[r]; s <= r; ++s) {
+            int stop;
+#pragma omp atomic read
+            stop = failed;
+            if (stop) break;
+            if (!factor_sn(s, wk, 1)) {
+#pragma omp atomic write
+                failed = 1;
+                break;
+            }
+        }
     }
+    if (!failed)
+        for (int32_t s = 0; s < nsn; ++s)
+            if (top[s] && !factor_sn(s, work[0], threads)) {
+                failed = 1;
+                break;
+            }
+    if (failed) {
+        err = "Matrix is not positive definite!";
+        return ST_NOT_POSDEF;
+    }
+    double flops = 0.0;
+    for (int32_t s = 0; s < nsn; ++s) flops += sn_flops[s];
     F.flops = flops;
     return ST_OK;
 }

@@ -98,12 +98,18 @@ def test_factor_bad_indices(gblib):
         factorize(gblib, 2, [0, 2, 1], [0, 1], [1.0, 1.0], 1)  # non-monotone pointers
 
 
-def test_factor_threads_deterministic(gblib):
-    n, vals, idx = CASES["grid3d_10"]()
+@pytest.mark.parametrize("k", [10, 24])
+def test_factor_threads_deterministic(gblib, k):
+    """The factor is bit-identical for every thread count: subtrees are
+    factorised as independent tasks, children are added in a fixed order and
+    the dense kernels block independently of the threads. k=24 has fronts of
+    several hundred rows, above the triangular solve's row blocks."""
+    n, vals, idx = k ** 3, *workloads.grid3d_coo(k, 1e-3)
     a = factorize(gblib, n, idx[0], idx[1], vals, 2, threads=1)
-    b = factorize(gblib, n, idx[0], idx[1], vals, 2, threads=4)
-    np.testing.assert_array_equal(a[0], b[0])
-    np.testing.assert_allclose(a[3], b[3], rtol=1e-12, atol=1e-14)
+    for t in (2, 3, 8):
+        b = factorize(gblib, n, idx[0], idx[1], vals, 2, threads=t)
+        np.testing.assert_array_equal(a[0], b[0])
+        np.testing.assert_array_equal(a[3], b[3])
 
 
 def test_nested_dissection_fill_reasonable(gblib):
