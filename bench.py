@@ -65,9 +65,9 @@ def parse_args():
 
 # DRAM bytes (read + write) of one FP32 solve, summed over its 5 sweep
 # launches, from one ncu capture of `bench.py --workload solve` at the same
-# size (dram__bytes_read.sum + dram__bytes_write.sum; the table and command
-# are in profiles/sweeps_poisson64_nrhs128_dram.md). Keyed by (k, nrhs).
-MEASURED_SOLVE_TRAFFIC_F32 = {(64, 128): 2128167168}
+# size (dram__bytes_read.sum + dram__bytes_write.sum; the per-kernel table
+# and the command are kept with the ncu summaries). Keyed by (k, nrhs).
+MEASURED_SOLVE_TRAFFIC_F32 = {(64, 128): 1922223616}
 
 
 def measured_traffic(args, f32=True):
