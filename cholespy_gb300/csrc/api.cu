@@ -154,14 +154,14 @@ int analyze_triangle(gbchol_solver* h, Triangle& t, bool lower) {
 template <typename T>
 cudaError_t upload_cast(DevBuf<T>& dst, const std::vector<double>& src) {
     std::vector<T> tmp(src.size());
-    for (size_t k = 0; k < src.size(); ++k) tmp[k] = (T)src[k];
+    const int64_t cnt = (int64_t)src.size();
+#pragma omp parallel for schedule(static) if (cnt >= ((int64_t)1 << 20))
+    for (int64_t k = 0; k < cnt; ++k) tmp[k] = (T)src[k];
     return dst.upload(tmp.data(), tmp.size());
 }
 
 // Builds the solve plan from the factor and the level orders and uploads it.
-int setup_plan(gbchol_solver* h, const std::vector<int32_t>& rp, const std::vector<int32_t>& ci,
-               const std::vector<double>& rv) {
-    (void)rp; (void)ci; (void)rv;
+int setup_plan(gbchol_solver* h) {
     const Factor& F = h->F;
     const int32_t n = F.n;
     SolvePlan& P = h->plan;
@@ -250,10 +250,11 @@ int setup_device(gbchol_solver* h) {
     // L^T in CSR is L in CSC (the reference's "upper" triangle, :280)
     CUDA_TRY(h->upper.rowptr.upload(F.colptr.data(), (size_t)n + 1));
     CUDA_TRY(h->upper.cols.upload(F.rowidx.data(), F.rowidx.size()));
-    // L in CSR (cholmod_transpose, :252): columns ascending, diagonal last
+    // L in CSR (cholmod_transpose, :252): columns ascending, diagonal last;
+    // the analysis reads the pattern only
     std::vector<int32_t> rp, ci;
     std::vector<double> rv;
-    transpose(n, F.colptr, F.rowidx, F.vals, rp, ci, rv);
+    transpose_columns(n, F.colptr, F.rowidx, nullptr, nullptr, rp, ci, rv);
     CUDA_TRY(h->lower.rowptr.upload(rp.data(), rp.size()));
     CUDA_TRY(h->lower.cols.upload(ci.data(), ci.size()));
     if (n > 0) {
@@ -261,7 +262,7 @@ int setup_device(gbchol_solver* h) {
         if (rc) return rc;
         rc = analyze_triangle(h, h->upper, false);
         if (rc) return rc;
-        rc = setup_plan(h, rp, ci, rv);
+        rc = setup_plan(h);
         if (rc) return rc;
     }
     CUDA_TRY(cudaDeviceSynchronize());
@@ -489,9 +490,7 @@ int gbchol_refactorize(gbchol_handle h, int64_t nnz, const int32_t* ii, const in
     h->F.vals.swap(Fn.vals);
     if (h->store & GBCHOL_STORE_A64) CUDA_TRY(h->a_vals.upload(S.vals.data(), S.vals.size()));
     ++h->plan_gen;
-    const std::vector<int32_t> none;
-    const std::vector<double> nonev;
-    if (int rc = setup_plan(h, none, none, nonev)) return rc;
+    if (int rc = setup_plan(h)) return rc;
     CUDA_TRY(cudaDeviceSynchronize());
     return GBCHOL_OK;
 }
@@ -602,9 +601,7 @@ int gbchol_replan(gbchol_handle h, int32_t min_top_width, int32_t part_keep, int
     h->plan_opt.part_group = part_group;
     ++h->plan_gen;
     if (h->n == 0) return GBCHOL_OK;
-    const std::vector<int32_t> none;
-    const std::vector<double> nonev;
-    if (int rc = setup_plan(h, none, none, nonev)) return rc;
+    if (int rc = setup_plan(h)) return rc;
     CUDA_TRY(cudaDeviceSynchronize());
     return GBCHOL_OK;
 }

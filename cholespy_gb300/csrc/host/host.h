@@ -79,10 +79,17 @@ struct FactorOptions {
 // ST_NOT_POSDEF on a non-positive pivot (src/cholesky_solver.cpp:241-242).
 Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string& err);
 
-// Transpose of a CSC pattern+values (gives the CSR of L from its CSC).
+// Transpose of a CSC pattern+values (gives the CSR of L from its CSC); with
+// empty `vals`, of the pattern alone. Indices ascend within each output row.
 void transpose(int32_t n, const std::vector<int32_t>& colptr, const std::vector<int32_t>& rowidx,
                const std::vector<double>& vals, std::vector<int32_t>& tptr,
                std::vector<int32_t>& tidx, std::vector<double>& tvals);
+// The same restricted to the columns c with keep_col[c] != 0 (all columns if
+// keep_col is null); vals may be null (pattern only). Multi-threaded for
+// large inputs, with results independent of the thread count.
+void transpose_columns(int32_t n, const std::vector<int32_t>& colptr, const std::vector<int32_t>& rowidx,
+                       const double* vals, const char* keep_col, std::vector<int32_t>& tptr,
+                       std::vector<int32_t>& tidx, std::vector<double>& tvals);
 
 // Host LL^T solve on a factor in FP64 (the CPU-device solve of the reference,
 // src/cholesky_solver.cpp:435-463). b and x are row-major (n, nrhs) arrays;

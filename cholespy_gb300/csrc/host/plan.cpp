@@ -53,27 +53,55 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
     std::vector<int32_t> unit_of_col((size_t)n, -1);
     std::vector<int32_t> first_unit((size_t)nsn, -1), unit_count((size_t)nsn, 0);
     std::vector<int64_t> rows_off((size_t)nsn, -1), panel_off((size_t)nsn, -1);
-    for (int32_t s = 0; s < nsn; ++s) {
-        if (!P.sn_top[s]) continue;
-        const int32_t f = P.sn_start[s], l1 = P.sn_start[s + 1], w = l1 - f;
+    // offsets first, then the row lists and panels, one supernode per task
+    std::vector<int32_t> tops;
+    {
+        int64_t nrows = 0, npan = 0;
+        for (int32_t s = 0; s < nsn; ++s) {
+            if (!P.sn_top[s]) continue;
+            const int32_t f = P.sn_start[s], w = P.sn_start[s + 1] - f;
+            const int64_t ld = F.colptr[f + 1] - F.colptr[f];
+            rows_off[s] = nrows;
+            panel_off[s] = npan;
+            nrows += ld;
+            npan += ld * w;
+            tops.push_back(s);
+        }
+        P.sn_rows.resize((size_t)nrows);
+        P.panels.resize((size_t)npan);  // zero: a panel column holds no rows above its diagonal
+    }
+    int mismatch = 0;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (size_t q = 0; q < tops.size(); ++q) {
+        const int32_t s = tops[q];
+        const int32_t f = P.sn_start[s], w = P.sn_start[s + 1] - f;
         const int32_t ld = F.colptr[f + 1] - F.colptr[f];
-        rows_off[s] = (int64_t)P.sn_rows.size();
-        P.sn_rows.insert(P.sn_rows.end(), F.rowidx.begin() + F.colptr[f],
-                         F.rowidx.begin() + F.colptr[f + 1]);
-        panel_off[s] = (int64_t)P.panels.size();
-        P.panels.resize(P.panels.size() + (size_t)ld * w, 0.0);
+        std::copy(F.rowidx.begin() + F.colptr[f], F.rowidx.begin() + F.colptr[f + 1],
+                  P.sn_rows.begin() + rows_off[s]);
         const int32_t* rows = P.sn_rows.data() + rows_off[s];
-        for (int32_t j = 0; j < w; ++j) {
+        bool ok = true;
+        for (int32_t j = 0; j < w && ok; ++j) {
             const int32_t c = f + j;
             const int32_t cnt = F.colptr[c + 1] - F.colptr[c];
-            if (cnt != ld - j) throw std::runtime_error("supernode structure mismatch");
+            if (cnt != ld - j) {
+                ok = false;
+                break;
+            }
             double* dst = P.panels.data() + panel_off[s] + (int64_t)j * ld + j;
             for (int32_t t = 0; t < cnt; ++t) {
-                if (F.rowidx[F.colptr[c] + t] != rows[j + t])
-                    throw std::runtime_error("supernode structure mismatch");
+                if (F.rowidx[F.colptr[c] + t] != rows[j + t]) ok = false;
                 dst[t] = F.vals[F.colptr[c] + t];
             }
         }
+        if (!ok) {
+#pragma omp atomic write
+            mismatch = 1;
+        }
+    }
+    if (mismatch) throw std::runtime_error("supernode structure mismatch");
+    for (const int32_t s : tops) {
+        const int32_t f = P.sn_start[s], l1 = P.sn_start[s + 1];
+        const int32_t ld = F.colptr[f + 1] - F.colptr[f];
         first_unit[s] = (int32_t)P.units.size();
         for (int32_t c0 = f; c0 < l1; c0 += kChunk) {
             SnUnit u{};
@@ -290,30 +318,17 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
     P.unit_of_row = unit_of_col;
 
     // ---- leaf region -------------------------------------------------------
-    // CSR of L (columns ascending, diagonal last)
-    std::vector<int32_t> rp, ci;
-    std::vector<double> rv;
-    transpose(n, F.colptr, F.rowidx, F.vals, rp, ci, rv);
-    P.lo_rowptr.assign((size_t)n + 1, 0);
-    for (int32_t i = 0; i < n; ++i) {
-        int32_t cnt = 0;
-        if (!P.row_top[i]) cnt = rp[i + 1] - rp[i];
-        else
-            for (int32_t k = rp[i]; k < rp[i + 1]; ++k) cnt += !P.row_top[ci[k]];
-        P.lo_rowptr[i + 1] = P.lo_rowptr[i] + cnt;
+    // CSR of the leaf columns of L (columns ascending, diagonal last): a leaf
+    // row's whole row (an entry's row is an etree ancestor of its column, and
+    // the ancestors of a top column are top) and the leaf-column terms of a
+    // top row
+    {
+        std::vector<char> leaf_col((size_t)n);
+        for (int32_t j = 0; j < n; ++j) leaf_col[j] = !P.row_top[j];
+        transpose_columns(n, F.colptr, F.rowidx, F.vals.data(), leaf_col.data(), P.lo_rowptr, P.lo_cols,
+                          P.lo_vals);
     }
-    P.lo_cols.resize((size_t)P.lo_rowptr[n]);
-    P.lo_vals.resize((size_t)P.lo_rowptr[n]);
-    for (int32_t i = 0; i < n; ++i) {
-        int32_t d = P.lo_rowptr[i];
-        for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
-            if (P.row_top[i] && P.row_top[ci[k]]) continue;
-            P.lo_cols[d] = ci[k];
-            P.lo_vals[d] = rv[k];
-            ++d;
-        }
-        P.max_row_len = std::max(P.max_row_len, P.lo_rowptr[i + 1] - P.lo_rowptr[i]);
-    }
+    for (int32_t i = 0; i < n; ++i) P.max_row_len = std::max(P.max_row_len, P.lo_rowptr[i + 1] - P.lo_rowptr[i]);
     {
         // leaf rows by their level in L (= etree height: their dependencies
         // are all leaf rows), then the partial tasks of the top rows

@@ -9,6 +9,10 @@
 #include <algorithm>
 #include <numeric>
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 namespace gbchol {
 
 namespace {
@@ -175,22 +179,69 @@ void symmetric_from_lower(const Csc& A, Csc& S) {
     }
 }
 
+void transpose_columns(int32_t n, const std::vector<int32_t>& colptr, const std::vector<int32_t>& rowidx,
+                       const double* vals, const char* keep_col, std::vector<int32_t>& tptr,
+                       std::vector<int32_t>& tidx, std::vector<double>& tvals) {
+    const int64_t nnz = (int64_t)rowidx.size();
+    int nt = 1;
+#ifdef _OPENMP
+    if (nnz >= (int64_t)1 << 20) nt = std::max(1, std::min(omp_get_max_threads(), 64));
+#endif
+    // contiguous column ranges of about nnz / nt entries, in column order: a
+    // range's rows are filled after those of every earlier range, so columns
+    // stay ascending within each row whatever the thread count
+    std::vector<int32_t> c0((size_t)nt + 1, n);
+    c0[0] = 0;
+    for (int t = 1; t < nt; ++t) {
+        const int32_t target = (int32_t)(nnz * t / nt);
+        c0[t] = (int32_t)(std::lower_bound(colptr.begin(), colptr.end() - 1, target) - colptr.begin());
+    }
+    for (int t = 1; t <= nt; ++t) c0[t] = std::max(c0[t], c0[t - 1]);
+    std::vector<int32_t> cnt((size_t)nt * n, 0);  // entries per (range, row)
+#pragma omp parallel for num_threads(nt) schedule(static, 1) if (nt > 1)
+    for (int t = 0; t < nt; ++t) {
+        int32_t* ct = cnt.data() + (size_t)t * n;
+        for (int32_t c = c0[t]; c < c0[t + 1]; ++c) {
+            if (keep_col && !keep_col[c]) continue;
+            for (int32_t k = colptr[c]; k < colptr[c + 1]; ++k) ct[rowidx[k]]++;
+        }
+    }
+    tptr.assign((size_t)n + 1, 0);
+    for (int32_t r = 0; r < n; ++r) {
+        int32_t v = 0;
+        for (int t = 0; t < nt; ++t) v += cnt[(size_t)t * n + r];
+        tptr[r + 1] = tptr[r] + v;
+    }
+    // turn the counts into each range's first slot per row
+#pragma omp parallel for num_threads(nt) schedule(static) if (nt > 1)
+    for (int32_t r = 0; r < n; ++r) {
+        int32_t off = tptr[r];
+        for (int t = 0; t < nt; ++t) {
+            const int32_t v = cnt[(size_t)t * n + r];
+            cnt[(size_t)t * n + r] = off;
+            off += v;
+        }
+    }
+    tidx.resize((size_t)tptr[n]);
+    tvals.resize(vals ? (size_t)tptr[n] : 0);
+#pragma omp parallel for num_threads(nt) schedule(static, 1) if (nt > 1)
+    for (int t = 0; t < nt; ++t) {
+        int32_t* next = cnt.data() + (size_t)t * n;
+        for (int32_t c = c0[t]; c < c0[t + 1]; ++c) {
+            if (keep_col && !keep_col[c]) continue;
+            for (int32_t k = colptr[c]; k < colptr[c + 1]; ++k) {
+                const int32_t d = next[rowidx[k]]++;
+                tidx[d] = c;
+                if (vals) tvals[d] = vals[k];
+            }
+        }
+    }
+}
+
 void transpose(int32_t n, const std::vector<int32_t>& colptr, const std::vector<int32_t>& rowidx,
                const std::vector<double>& vals, std::vector<int32_t>& tptr,
                std::vector<int32_t>& tidx, std::vector<double>& tvals) {
-    const size_t nnz = rowidx.size();
-    tptr.assign((size_t)n + 1, 0);
-    for (size_t k = 0; k < nnz; ++k) tptr[(size_t)rowidx[k] + 1]++;
-    for (int32_t r = 0; r < n; ++r) tptr[r + 1] += tptr[r];
-    tidx.resize(nnz);
-    tvals.resize(vals.empty() ? 0 : nnz);
-    std::vector<int32_t> next(tptr.begin(), tptr.end() - 1);
-    for (int32_t c = 0; c < n; ++c)
-        for (int32_t k = colptr[c]; k < colptr[c + 1]; ++k) {
-            int32_t d = next[rowidx[k]]++;
-            tidx[d] = c;
-            if (!vals.empty()) tvals[d] = vals[k];
-        }
+    transpose_columns(n, colptr, rowidx, vals.empty() ? nullptr : vals.data(), nullptr, tptr, tidx, tvals);
 }
 
 }  // namespace gbchol

@@ -19,6 +19,10 @@
 #include "host.h"
 #include "plan.h"
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 using namespace gbchol;
 
 namespace {
@@ -270,7 +274,67 @@ void grid(int dim, int k, std::vector<int32_t>& ii, std::vector<int32_t>& jj, st
 
 }  // namespace
 
+// transpose_columns against a plain serial transpose, on a random CSC large
+// enough for the multi-threaded path, with and without a column filter and
+// with 1, 3 and 8 threads: identical output every time.
+bool check_transpose() {
+    const int32_t n = 30000, per = 48;
+    std::mt19937 g(11);
+    std::vector<int32_t> colptr((size_t)n + 1, 0), rowidx;
+    std::vector<double> vals;
+    for (int32_t c = 0; c < n; ++c) {
+        const int32_t m = (int32_t)(g() % (2 * per));
+        std::vector<int32_t> rows;
+        for (int32_t k = 0; k < m; ++k) rows.push_back((int32_t)(g() % n));
+        std::sort(rows.begin(), rows.end());
+        rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
+        for (int32_t r : rows) {
+            rowidx.push_back(r);
+            vals.push_back((double)(g() % 1000) - 500.0);
+        }
+        colptr[c + 1] = (int32_t)rowidx.size();
+    }
+    std::vector<char> keep((size_t)n);
+    for (auto& k : keep) k = (char)(g() % 3 != 0);
+    bool ok = rowidx.size() >= ((size_t)1 << 20);
+    for (const char* kc : {(const char*)nullptr, (const char*)keep.data()}) {
+        // plain serial transpose
+        std::vector<int32_t> p0((size_t)n + 1, 0), i0;
+        std::vector<double> v0;
+        for (int32_t c = 0; c < n; ++c)
+            if (!kc || kc[c])
+                for (int32_t k = colptr[c]; k < colptr[c + 1]; ++k) p0[rowidx[k] + 1]++;
+        for (int32_t r = 0; r < n; ++r) p0[r + 1] += p0[r];
+        i0.resize((size_t)p0[n]);
+        v0.resize((size_t)p0[n]);
+        std::vector<int32_t> nx(p0.begin(), p0.end() - 1);
+        for (int32_t c = 0; c < n; ++c)
+            if (!kc || kc[c])
+                for (int32_t k = colptr[c]; k < colptr[c + 1]; ++k) {
+                    i0[nx[rowidx[k]]] = c;
+                    v0[nx[rowidx[k]]++] = vals[k];
+                }
+        for (int t : {1, 3, 8}) {
+#ifdef _OPENMP
+            omp_set_num_threads(t);
+#endif
+            std::vector<int32_t> p1, i1;
+            std::vector<double> v1;
+            transpose_columns(n, colptr, rowidx, vals.data(), kc, p1, i1, v1);
+            ok = ok && p1 == p0 && i1 == i0 && v1 == v0;
+            transpose_columns(n, colptr, rowidx, nullptr, kc, p1, i1, v1);
+            ok = ok && p1 == p0 && i1 == i0 && v1.empty();
+        }
+    }
+#ifdef _OPENMP
+    omp_set_num_threads(omp_get_num_procs());
+#endif
+    std::printf("transpose_columns: %s\n", ok ? "ok" : "MISMATCH");
+    return ok;
+}
+
 int main() {
+    if (!check_transpose()) return 1;
     struct Case { int dim, k, minw, keep, group; };
     const Case cases[] = {
         {2, 8, 1, 16, 32},  {2, 20, 4, 16, 32}, {2, 20, 8, 2, 3},   {2, 40, 1, 1, 2},
