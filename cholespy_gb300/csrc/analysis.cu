@@ -13,9 +13,20 @@
 // level of row i of L^T its depth: the dependencies of a row form a subtree
 // (L) or an ancestor path (L^T) of the etree along which levels strictly
 // increase. The host derives these candidates in O(n) from parent(j) = first
-// off-diagonal row of column j, and level_verify_kernel checks every row
-// against all of its dependencies in one parallel pass. Only a pattern that
-// fails the check runs the general sync-free kernel below.
+// off-diagonal row of column j, and level_verify_kernel checks them against
+// every nonzero of L in one parallel pass over L's columns (no transpose).
+// Only a factor that fails the check runs the general sync-free kernel below.
+//
+// Why an entry-wise check suffices. Lower: the candidate is h(i) = 1 + max
+// h(c) over the etree children c of i (0 for none), and every child is an
+// entry L(i, c) (parent(c) is column c's first off-diagonal row). If every
+// off-diagonal entry L(i, j) satisfies h(i) >= h(j) + 1, then for a row with
+// children the maximum of h(j) + 1 over its entries is attained by a child and
+// equals h(i); a row without children has h(i) = 0, so the inequality admits
+// no entry in it. So h satisfies the level recurrence at every row, whose
+// solution is unique: h is the level. Upper: d(j) = 1 + d(parent(j)) (0 at a
+// root), the parent is an entry of column j, and every entry L(i, j) must
+// satisfy d(j) >= d(i) + 1; the same argument applies.
 //
 // GB300 design of the general kernel: the reference runs n blocks of ONE thread each, handing rows
 // out through a global atomic ticket and spinning without bound. Here one
@@ -79,26 +90,28 @@ __global__ void __launch_bounds__(256) level_kernel(int n, const int* __restrict
     if (lane == 0 && local_max > 0) atomicMax(max_lvl, local_max);
 }
 
-// Checks a candidate level assignment against every row's dependencies in
-// one fully parallel pass (warp per row, no waits): a labeling that satisfies
-// level[i] == (deps ? 1 + max level[dep] : 0) at every row is the unique
-// longest-path labeling, i.e. exactly what the sequential definition gives.
+// Checks candidate levels against every off-diagonal entry of L (CSC,
+// diagonal first in each column), a warp per column, no waits: lower
+// requires cand[i] >= cand[j] + 1, upper cand[j] >= cand[i] + 1, for every
+// entry L(i, j). With candidates built from the elimination tree (see the top
+// of this file) passing means they are exactly the levels.
 template <bool LOWER>
-__global__ void __launch_bounds__(256) level_verify_kernel(int n, const int* __restrict__ rowptr,
-                                                           const int* __restrict__ cols,
+__global__ void __launch_bounds__(256) level_verify_kernel(int n, const int* __restrict__ colptr,
+                                                           const int* __restrict__ rowidx,
                                                            const int* __restrict__ cand,
                                                            int* mismatch) {
     const int lane = threadIdx.x & 31;
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-    for (int row = warp; row < n; row += nwarps) {
-        const int s = rowptr[row], e = rowptr[row + 1];
-        const int lo = LOWER ? s : s + 1;
-        const int hi = LOWER ? e - 1 : e;
-        int lvl = 0;
-        for (int k = lo + lane; k < hi; k += 32) lvl = max(lvl, cand[cols[k]] + 1);
-        lvl = dev::warp_max(lvl);
-        if (lane == 0 && lvl != cand[row]) atomicOr(mismatch, 1);
+    for (int j = warp; j < n; j += nwarps) {
+        const int s = colptr[j] + 1, e = colptr[j + 1];
+        const int cj = cand[j];
+        bool bad = false;
+        for (int k = s + lane; k < e; k += 32) {
+            const int ci = cand[rowidx[k]];
+            bad |= LOWER ? (ci < cj + 1) : (cj < ci + 1);
+        }
+        if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(mismatch, 1);
     }
 }
 
@@ -116,7 +129,7 @@ cudaError_t launch_selftest_wait(const int* flag, int* status, unsigned long lon
     return cudaGetLastError();
 }
 
-cudaError_t launch_level_verify(bool lower, int n, const int* rowptr, const int* cols,
+cudaError_t launch_level_verify(bool lower, int n, const int* colptr, const int* rowidx,
                                 const int* cand, int* mismatch, cudaStream_t stream) {
     if (n == 0) return cudaSuccess;
     int dev = 0, sms = 0;
@@ -124,8 +137,8 @@ cudaError_t launch_level_verify(bool lower, int n, const int* rowptr, const int*
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int grid = (n + 7) / 8;
     if (grid > sms * 16) grid = sms * 16;
-    if (lower) level_verify_kernel<true><<<grid, 256, 0, stream>>>(n, rowptr, cols, cand, mismatch);
-    else level_verify_kernel<false><<<grid, 256, 0, stream>>>(n, rowptr, cols, cand, mismatch);
+    if (lower) level_verify_kernel<true><<<grid, 256, 0, stream>>>(n, colptr, rowidx, cand, mismatch);
+    else level_verify_kernel<false><<<grid, 256, 0, stream>>>(n, colptr, rowidx, cand, mismatch);
     return cudaGetLastError();
 }
 

@@ -119,7 +119,8 @@ int analyze_triangle(gbchol_solver* h, Triangle& t, bool lower) {
         CUDA_TRY(cudaMemcpy(lev.p, t.row_levels.data(), sizeof(int32_t) * (size_t)n,
                             cudaMemcpyHostToDevice));
         CUDA_TRY(cudaMemset(h->max_lvl.p, 0, sizeof(int32_t)));
-        CUDA_TRY(launch_level_verify(lower, n, t.rowptr.p, t.cols.p, lev.p, h->max_lvl.p, nullptr));
+        // both triangles are checked on L's columns (the upper triangle's rows)
+        CUDA_TRY(launch_level_verify(lower, n, h->upper.rowptr.p, h->upper.cols.p, lev.p, h->max_lvl.p, nullptr));
         int32_t mism = 1;
         CUDA_TRY(cudaMemcpy(&mism, h->max_lvl.p, sizeof(int32_t), cudaMemcpyDeviceToHost));
         verified = mism == 0;
@@ -130,6 +131,15 @@ int analyze_triangle(gbchol_solver* h, Triangle& t, bool lower) {
     }
     t.general_kernel = !verified;
     if (!verified) {
+        if (lower && !t.rowptr.p) {
+            // L in CSR (cholmod_transpose, :252): columns ascending, diagonal
+            // last; the general kernel walks rows
+            std::vector<int32_t> rp, ci;
+            std::vector<double> none;
+            transpose_columns(n, h->F.colptr, h->F.rowidx, nullptr, nullptr, rp, ci, none);
+            CUDA_TRY(t.rowptr.upload(rp.data(), rp.size()));
+            CUDA_TRY(t.cols.upload(ci.data(), ci.size()));
+        }
         CUDA_TRY(cudaMemset(h->max_lvl.p, 0, sizeof(int32_t)));
         int ep = h->next_epoch(nullptr);
         CUDA_TRY(launch_level_analysis(lower, n, t.rowptr.p, t.cols.p, lev.p, h->flags.p, ep,
@@ -247,16 +257,10 @@ int setup_device(gbchol_solver* h) {
     CUDA_TRY(h->status.alloc(1));
     CUDA_TRY(cudaMemset(h->status.p, 0, sizeof(int32_t)));
     CUDA_TRY(h->max_lvl.alloc(1));
-    // L^T in CSR is L in CSC (the reference's "upper" triangle, :280)
+    // L^T in CSR is L in CSC (the reference's "upper" triangle, :280); L's
+    // CSR is built only if the general analysis kernel has to run
     CUDA_TRY(h->upper.rowptr.upload(F.colptr.data(), (size_t)n + 1));
     CUDA_TRY(h->upper.cols.upload(F.rowidx.data(), F.rowidx.size()));
-    // L in CSR (cholmod_transpose, :252): columns ascending, diagonal last;
-    // the analysis reads the pattern only
-    std::vector<int32_t> rp, ci;
-    std::vector<double> rv;
-    transpose_columns(n, F.colptr, F.rowidx, nullptr, nullptr, rp, ci, rv);
-    CUDA_TRY(h->lower.rowptr.upload(rp.data(), rp.size()));
-    CUDA_TRY(h->lower.cols.upload(ci.data(), ci.size()));
     if (n > 0) {
         int rc = analyze_triangle(h, h->lower, true);
         if (rc) return rc;

@@ -15,9 +15,10 @@ cudaError_t launch_level_analysis(bool lower, int n, const int* rowptr, const in
                                   int* levels, int* flags, int epoch, int* max_lvl, int* status,
                                   cudaStream_t stream);
 
-// Parallel check of candidate levels against every row's dependencies;
-// sets *mismatch to 1 if any row disagrees.
-cudaError_t launch_level_verify(bool lower, int n, const int* rowptr, const int* cols,
+// Parallel check of elimination-tree candidate levels against every
+// off-diagonal entry of L, given in CSC (diagonal first in each column);
+// sets *mismatch to 1 if any entry disagrees.
+cudaError_t launch_level_verify(bool lower, int n, const int* colptr, const int* rowidx,
                                 const int* cand, int* mismatch, cudaStream_t stream);
 
 // Self-test of the bounded wait: one wait on a flag that nothing sets.
