@@ -57,7 +57,8 @@ def parse_args():
                    help="RHS columns of the bounded CPU sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true",
-                   help="ico6/grid64: keep the default top-region width instead of autotuning it")
+                   help="ico6/grid64: keep the default top-region width instead of autotuning it; "
+                        "batch: keep it instead of the tuned width 16")
     return p.parse_args()
 
 
@@ -495,6 +496,11 @@ def run_batch(args, world, rank, local):
                                        torch.tensor(vals).to(dev), MatrixType.COO))
         bs_h.append(torch.tensor(b, dtype=torch.float32))
     t_ctor = time.perf_counter() - t0
+    if not args.no_autotune:
+        # top-region width 16 for these 2-D systems (one batch, GB300: width
+        # 8 -> 23.7 ms, 16 -> 21.4 ms, 4 -> 31.1 ms, 2 -> 75.6 ms)
+        for s_ in solvers:
+            s_.replan(16)
     nrhs = [b.shape[1] for b in bs_h]
     bs = [b.to(dev) for b in bs_h]
     xs = [torch.zeros_like(b) for b in bs]
@@ -553,6 +559,7 @@ def run_batch(args, world, rank, local):
                  "launch per phase)", value, "RHS-solves/s", t_b, "f32",
                  {"workload": "batch256_grid2d_n1e3-1e5_lam1-50_rhs1-128_seed3",
                   "systems": len(solvers), "total_rhs": total_rhs,
+                  "top_width": 8 if args.no_autotune else 16,
                   "total_rows": sum(i.n for i in infos), "total_nnz_l": sum(i.nnz_l for i in infos),
                   "ctor_s": t_ctor, "l2": "inputs larger than L2"},
                  sequential={"value": value_seq, "unit": "RHS-solves/s",
