@@ -20,6 +20,7 @@
 //     34, 1992) with dense blocked kernels (dense.cpp).
 #include <algorithm>
 #include <cmath>
+#include <memory>
 #include <numeric>
 
 #include "dense.h"
@@ -292,9 +293,18 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     std::vector<char> top((size_t)nsn, 0);
     for (int32_t s = 0; s < nsn; ++s) top[s] = sub_flops[s] > cut;
 
+    // Front storage without value-initialisation: a front is first touched
+    // by the (parallel, for large fronts) zeroing of its lower triangle, not
+    // by a serial fill when it is allocated.
+    struct Buf {
+        std::unique_ptr<double[]> p;
+        size_t cap = 0;
+        double* data() { return p.get(); }
+        const double* data() const { return p.get(); }
+    };
     struct Front {
         int64_t fsz = 0, w = 0;
-        std::vector<double> u;  // the whole front, column-major; the update is u[w.., w..]
+        Buf u;  // the whole front, column-major; the update is u[w.., w..]
     };
     std::vector<Front> upd((size_t)nsn);  // finished fronts waiting for their parent
     constexpr int64_t kParCols = 256;     // columns from which copies go parallel
@@ -303,34 +313,30 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     // front costs its page faults
     struct Work {
         std::vector<int32_t> relpos;
-        std::vector<std::vector<double>> pool;
-        void recycle(std::vector<double>& v) {
-            if (v.capacity() == 0) return;
+        std::vector<Buf> pool;
+        void recycle(Buf& v) {
+            if (v.cap == 0) return;
             pool.push_back(std::move(v));
-            v = std::vector<double>();
+            v = Buf();
             if (pool.size() > 8) {  // drop the smallest
                 size_t k = 0;
                 for (size_t i = 1; i < pool.size(); ++i)
-                    if (pool[i].capacity() < pool[k].capacity()) k = i;
+                    if (pool[i].cap < pool[k].cap) k = i;
                 pool.erase(pool.begin() + (std::ptrdiff_t)k);
             }
         }
-        std::vector<double> take(size_t need) {
-            std::vector<double> v;
+        Buf take(size_t need) {
+            Buf v;
             size_t best = pool.size();
             for (size_t i = 0; i < pool.size(); ++i)
-                if (pool[i].capacity() >= need && (best == pool.size() || pool[i].capacity() < pool[best].capacity()))
-                    best = i;
-            if (best == pool.size() && !pool.empty()) {  // none fits: grow the largest
-                best = 0;
-                for (size_t i = 1; i < pool.size(); ++i)
-                    if (pool[i].capacity() > pool[best].capacity()) best = i;
-            }
+                if (pool[i].cap >= need && (best == pool.size() || pool[i].cap < pool[best].cap)) best = i;
             if (best < pool.size()) {
                 v = std::move(pool[best]);
                 pool.erase(pool.begin() + (std::ptrdiff_t)best);
+            } else {  // none fits: a new buffer, uninitialised
+                v.p.reset(new double[need]);
+                v.cap = need;
             }
-            if (v.size() < need) v.resize(need);
             return v;
         }
     };
@@ -347,7 +353,7 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
         const int64_t Fsz = F.colptr[f + 1] - F.colptr[f];
         const int64_t m = Fsz - w;
         for (int64_t i = 0; i < Fsz; ++i) relpos[rows[i]] = (int32_t)i;
-        std::vector<double> front = wk.take((size_t)(Fsz * Fsz));
+        Buf front = wk.take((size_t)(Fsz * Fsz));
         double* fr = front.data();
         // only the lower triangle of a front is ever read (assembly, the dense
         // kernels and the update all stay on or below the diagonal): zero that
@@ -397,7 +403,7 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
         if (ok && m > 0 && sn_parent[s] >= 0) {
             upd[s].fsz = Fsz;
             upd[s].w = w;
-            upd[s].u.swap(front);  // the front itself carries the update
+            upd[s].u = std::move(front);  // the front itself carries the update
         } else {
             wk.recycle(front);
         }
