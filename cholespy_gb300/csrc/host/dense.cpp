@@ -182,7 +182,7 @@ void trsm_right_lower_t(int64_t m, int64_t n, const double* L, int64_t ldl, doub
     // Rows of B are independent: solve them in fixed blocks of kRows rows
     // (a multiple of the micro-kernel's MR), spread over threads when large.
     // The blocks do not depend on the thread count, and neither do the results.
-    constexpr int64_t kRows = 256;
+    constexpr int64_t kRows = 64;
     const int64_t chunks = (m + kRows - 1) / kRows;
     const double work = (double)m * (double)n * (double)n;
     const int nt = (threads > 1 && work > 8.0e6) ? (int)std::min<int64_t>(threads, chunks) : 1;
