@@ -195,7 +195,7 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     parent = etree(n, rptr, rcol);
     F.parent = parent;
 
-    // ---- pattern of L by row subtrees -----------------------------------
+    // ---- column counts of L by row subtrees -----------------------------
     std::vector<int32_t> mark((size_t)n, -1);
     std::vector<int64_t> cnt((size_t)n, 1);  // diagonal
     for (int32_t i = 0; i < n; ++i) {
@@ -216,21 +216,6 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     F.colptr.resize((size_t)n + 1);
     F.colptr[0] = 0;
     for (int32_t j = 0; j < n; ++j) F.colptr[j + 1] = F.colptr[j] + (int32_t)cnt[j];
-    F.rowidx.resize((size_t)total);
-    {
-        std::vector<int32_t> nxt(F.colptr.begin(), F.colptr.end() - 1);
-        std::fill(mark.begin(), mark.end(), -1);
-        for (int32_t i = 0; i < n; ++i) {
-            F.rowidx[nxt[i]++] = i;  // rows arrive in increasing order: diagonal first
-            mark[i] = i;
-            for (int32_t k = rptr[i]; k < rptr[i + 1]; ++k) {
-                for (int32_t r = rcol[k]; mark[r] != i; r = parent[r]) {
-                    F.rowidx[nxt[r]++] = i;
-                    mark[r] = i;
-                }
-            }
-        }
-    }
 
     // ---- fundamental supernodes -----------------------------------------
     std::vector<int32_t> nchild((size_t)n, 0);
@@ -244,17 +229,6 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     }
     F.sn_start.push_back(n);
     const int32_t nsn = (int32_t)F.sn_start.size() - 1;
-
-    // ---- multifrontal numeric factorisation -----------------------------
-    // Supernodes whose subtree holds more than 1/(4 threads) of the flops (a
-    // set closed towards the roots) are factorised last, one after the other,
-    // with multi-threaded dense kernels; every subtree hanging below that set
-    // is an independent task, factorised by one thread. A finished front is
-    // kept whole and handed to its parent: its trailing m x m block (leading
-    // dimension Fsz) is the update. A parent adds its children's updates in
-    // reverse child order, the order of a serial postorder stack, so results
-    // do not depend on the thread count.
-    F.vals.assign((size_t)total, 0.0);
     std::vector<int32_t> sn_of((size_t)n);
     for (int32_t s = 0; s < nsn; ++s)
         for (int32_t j = F.sn_start[s]; j < F.sn_start[s + 1]; ++j) sn_of[j] = s;
@@ -273,6 +247,68 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
         for (int32_t s = 0; s < nsn; ++s)  // children in increasing order
             if (sn_parent[s] >= 0) children[nx[sn_parent[s]]++] = s;
     }
+
+    // ---- pattern of L by supernodes -------------------------------------
+    // rows(s) = the supernode's columns, the rows of A below them and the
+    // rows of its children's patterns below their own columns (all of which
+    // lie at or below the supernode's first column); every column j of a
+    // fundamental supernode holds the suffix of rows(s) from j on. The lists
+    // are built in postorder (children first), then copied out per column in
+    // parallel.
+    std::vector<int64_t> sptr((size_t)nsn + 1, 0);
+    for (int32_t s = 0; s < nsn; ++s) sptr[s + 1] = sptr[s] + cnt[F.sn_start[s]];
+    std::vector<int32_t> srows((size_t)sptr[nsn]);
+    {
+        std::fill(mark.begin(), mark.end(), -1);
+        for (int32_t s = 0; s < nsn; ++s) {
+            const int32_t f = F.sn_start[s], l1 = F.sn_start[s + 1];
+            int32_t* out = srows.data() + sptr[s];
+            int64_t len = 0;
+            const int64_t cap = sptr[s + 1] - sptr[s];
+            for (int32_t j = f; j < l1; ++j) {
+                out[len++] = j;
+                mark[j] = s;
+            }
+            auto add = [&](int32_t r) {
+                if (mark[r] == s) return;
+                mark[r] = s;
+                if (len < cap) out[len] = r;
+                ++len;
+            };
+            for (int32_t j = f; j < l1; ++j)
+                for (int32_t k = cptr[j]; k < cptr[j + 1]; ++k) add(crow[k]);
+            for (int32_t q = child_ptr[s]; q < child_ptr[s + 1]; ++q) {
+                const int32_t c = children[q];
+                const int32_t cw = F.sn_start[c + 1] - F.sn_start[c];
+                for (int64_t k = sptr[c] + cw; k < sptr[c + 1]; ++k) add(srows[k]);
+            }
+            if (len != cap) {
+                err = "Internal error: supernodal pattern does not match the column counts.";
+                return ST_INTERNAL;
+            }
+            std::sort(out + (l1 - f), out + len);
+        }
+    }
+    F.rowidx.resize((size_t)total);
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 64) if (threads > 1)
+    for (int32_t s = 0; s < nsn; ++s) {
+        const int32_t f = F.sn_start[s], l1 = F.sn_start[s + 1];
+        for (int32_t j = f; j < l1; ++j)
+            std::copy(srows.begin() + sptr[s] + (j - f), srows.begin() + sptr[s + 1],
+                      F.rowidx.begin() + F.colptr[j]);
+    }
+    std::vector<int32_t>().swap(srows);
+
+    // ---- multifrontal numeric factorisation -----------------------------
+    // Supernodes whose subtree holds more than 1/(4 threads) of the flops (a
+    // set closed towards the roots) are factorised last, one after the other,
+    // with multi-threaded dense kernels; every subtree hanging below that set
+    // is an independent task, factorised by one thread. A finished front is
+    // kept whole and handed to its parent: its trailing m x m block (leading
+    // dimension Fsz) is the update. A parent adds its children's updates in
+    // reverse child order, the order of a serial postorder stack, so results
+    // do not depend on the thread count.
+    F.vals.assign((size_t)total, 0.0);
     std::vector<double> sn_flops((size_t)nsn), sub_flops((size_t)nsn);
     std::vector<int32_t> first((size_t)nsn);  // first supernode of each subtree (postorder: contiguous)
     double total_flops = 0.0;
