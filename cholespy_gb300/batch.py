@@ -5,6 +5,7 @@ persistent launch per sweep phase (gbchol_batch_* in include/gbchol.h).
     batch.solve(bs, xs)          # bs[k], xs[k]: CUDA tensors (n_k, r_k)
     g = batch.capture(bs, xs)    # CUDA graph of the bound solve
     g.replay()
+    width, batch = BatchSolver.tune([s0, s1, ...], nrhs=[r0, r1, ...])
 
 No counterpart in the reference (each of its solvers is solved separately).
 """
@@ -93,6 +94,50 @@ class BatchSolver:
         la, z, r = C.c_int32(), C.c_int64(), C.c_int64()
         _ffi.check(_ffi.lib().gbchol_batch_info(self._h, C.byref(la), C.byref(z), C.byref(r)))
         return {"launches": la.value, "nnz_l": z.value, "rows": r.value}
+
+    @classmethod
+    def tune(cls, solvers, nrhs, candidates=(8, 16, 32), reps=3):
+        """Autotuner of the batch: for each candidate top-region width,
+        rebuild every solver's plan with it (`replan`), build the batch and
+        time `reps` batched solves (CUDA events, after one warm-up solve) on
+        zero right-hand sides of the batch's shapes; keep the fastest width
+        for all solvers. Returns (width, BatchSolver built on that width).
+        Batches built earlier from these solvers must be built again. No
+        counterpart in the reference."""
+        import torch
+        if not candidates or reps < 1:
+            raise ValueError("At least one candidate width and one repetition are needed.")
+        solvers = list(solvers)
+        if len(nrhs) != len(solvers):
+            raise ValueError("One RHS count per solver.")
+        if not solvers:
+            raise ValueError("A batch needs at least one solver.")
+        dev = torch.device("cuda", solvers[0]._device)
+        dt = torch.float64 if isinstance(solvers[0], CholeskySolverD) else torch.float32
+        bs = [torch.zeros(s._n, int(r), device=dev, dtype=dt) for s, r in zip(solvers, nrhs)]
+        xs = [torch.zeros_like(b) for b in bs]
+        best, best_t = None, None
+        with torch.cuda.device(dev):
+            for w in candidates:
+                for s in solvers:
+                    s.replan(int(w))
+                batch = cls(solvers, nrhs)
+                batch.solve(bs, xs)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    batch.solve()
+                e1.record()
+                e1.synchronize()
+                batch.check()
+                t = e0.elapsed_time(e1)
+                if best_t is None or t < best_t:
+                    best, best_t = int(w), t
+                del batch
+            for s in solvers:
+                s.replan(best)
+        return best, cls(solvers, nrhs)
 
     def capture(self, bs, xs):
         """CUDA graph of one batched solve on the given arrays (replay() to run)."""

@@ -96,3 +96,24 @@ def test_single_solve_graph_replay(cuda):
         torch.cuda.synchronize()
         assert torch.equal(x, ref)
     s.check()
+
+
+def test_batch_tune(cuda):
+    """BatchSolver.tune: the batch autotuner picks one of the candidate
+    top-region widths, replans every solver with it and returns a batch that
+    solves like the individual (replanned) solvers."""
+    from cholespy_gb300 import BatchSolver, CholeskySolverF
+    torch = cuda
+    systems = _systems(torch, CholeskySolverF, 11, 6)
+    solvers = [s for s, _, _ in systems]
+    width, batch = BatchSolver.tune(solvers, [r for _, _, r in systems], candidates=(4, 16), reps=2)
+    assert width in (4, 16)
+    bs = [torch.randn(n, r, device="cuda") for _, n, r in systems]
+    xs = [torch.zeros_like(b) for b in bs]
+    batch.solve(bs, xs)
+    batch.check()
+    for (s, n, r), b, x in zip(systems, bs, xs):
+        x1 = torch.zeros_like(b)
+        s.solve(b, x1)
+        err = ((x - x1).abs().max() / x1.abs().max()).item()
+        assert err <= 1e-5, err
