@@ -70,6 +70,7 @@ def _declare(lib):
                                          C.POINTER(D)]),
         "gbchol_factor_export": (C.c_int, [P, P, P, P, P]),
         "gbchol_factor_free": (C.c_int, [P]),
+        "gbchol_factor_solve": (C.c_int, [P, I32, I32, P, P, I32]),
         "gbchol_batch_create": (C.c_int, [I32, P, P, I32, C.POINTER(P)]),
         "gbchol_batch_set_io": (C.c_int, [P, P, P]),
         "gbchol_batch_solve": (C.c_int, [P, P]),

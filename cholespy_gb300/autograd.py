@@ -90,6 +90,8 @@ class DifferentiableSolver:
         if _FN is None:
             _FN = _make_function()
         type = MatrixType(int(type))
+        if values.device.type != "cuda":
+            raise ValueError("DifferentiableSolver runs on the GPU: pass CUDA tensors.")
         cls = CholeskySolverF if precision == "float" else CholeskySolverD
         self.solver = cls(n_rows, ii, jj, values.detach(), type)
         rows, cols = _coo_indices(n_rows, ii, jj, type)

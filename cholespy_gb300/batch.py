@@ -28,6 +28,8 @@ class BatchSolver:
             self._precision = 1
         else:
             raise ValueError("A batch holds solvers of one precision.")
+        if any(getattr(s, "is_cpu", False) for s in solvers):
+            raise ValueError("A batch solves on the GPU: build its solvers from CUDA arrays.")
         if len(nrhs) != len(solvers):
             raise ValueError("One RHS count per solver.")
         self._solvers = list(solvers)          # keep the factors alive

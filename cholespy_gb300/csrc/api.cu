@@ -510,6 +510,25 @@ int gbchol_factor_refactorize(gbchol_factor_handle f, int64_t nnz, const int32_t
     return GBCHOL_OK;
 }
 
+int gbchol_factor_solve(gbchol_factor_handle f, int32_t precision, int32_t nrhs, const void* b, void* x,
+                        int32_t threads) {
+    if (!f) return fail(GBCHOL_EINVAL, "Null factor.");
+    if (precision != 0 && precision != 1) return fail(GBCHOL_EINVAL, "precision must be 0 (float) or 1 (double).");
+    if (nrhs < 0) return fail(GBCHOL_EINVAL, "The number of RHS must be non-negative.");
+    if (threads < 0) return fail(GBCHOL_EINVAL, "threads must be non-negative.");
+    if (f->F.n > 0 && nrhs > 0 && (!b || !x)) return fail(GBCHOL_EINVAL, "Null b or x.");
+    try {
+        if (!f->cpu_ready) {
+            cpu_plan(f->F, f->cpu, threads);
+            f->cpu_ready = true;
+        }
+        cpu_solve(f->F, f->cpu, precision, nrhs, b, x, threads);
+    } catch (const std::bad_alloc&) {
+        return fail(GBCHOL_ENOMEM, "Out of host memory.");
+    }
+    return GBCHOL_OK;
+}
+
 int gbchol_create_from_factor(int32_t n, const int32_t* perm, const int32_t* colptr,
                               const int32_t* rowidx, const double* vals, int32_t store,
                               gbchol_handle* out) {

@@ -489,31 +489,4 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     return ST_OK;
 }
 
-void cpu_solve(const Factor& F, int32_t nrhs, const double* b, double* x, int32_t threads) {
-    const int32_t n = F.n;
-    if (n == 0 || nrhs <= 0) return;
-    const int nt = resolve_threads(threads);
-    // RHS columns are independent: split them across threads.
-#pragma omp parallel for num_threads(nt) schedule(dynamic, 1) if (nt > 1 && nrhs > 1)
-    for (int32_t k = 0; k < nrhs; ++k) {
-        std::vector<double> y((size_t)n);
-        for (int32_t i = 0; i < n; ++i) y[i] = b[(int64_t)F.perm[i] * nrhs + k];
-        // forward: column-oriented L y = Pb
-        for (int32_t j = 0; j < n; ++j) {
-            const int32_t s = F.colptr[j], e = F.colptr[j + 1];
-            const double yj = y[j] / F.vals[s];
-            y[j] = yj;
-            for (int32_t p = s + 1; p < e; ++p) y[F.rowidx[p]] -= F.vals[p] * yj;
-        }
-        // backward: L^T z = y, row j of L^T is column j of L
-        for (int32_t j = n - 1; j >= 0; --j) {
-            const int32_t s = F.colptr[j], e = F.colptr[j + 1];
-            double acc = y[j];
-            for (int32_t p = s + 1; p < e; ++p) acc -= F.vals[p] * y[F.rowidx[p]];
-            y[j] = acc / F.vals[s];
-        }
-        for (int32_t i = 0; i < n; ++i) x[(int64_t)F.perm[i] * nrhs + k] = y[i];
-    }
-}
-
 }  // namespace gbchol

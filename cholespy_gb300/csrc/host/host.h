@@ -91,9 +91,31 @@ void transpose_columns(int32_t n, const std::vector<int32_t>& colptr, const std:
                        const double* vals, const char* keep_col, std::vector<int32_t>& tptr,
                        std::vector<int32_t>& tidx, std::vector<double>& tvals);
 
-// Host LL^T solve on a factor in FP64 (the CPU-device solve of the reference,
-// src/cholesky_solver.cpp:435-463). b and x are row-major (n, nrhs) arrays;
-// they may alias.
-void cpu_solve(const Factor& F, int32_t nrhs, const double* b, double* x, int32_t threads);
+// Structure of the host solve of a factor (cpu_solve.cpp), built once per
+// factor pattern: it holds positions into the factor's arrays, not values, so
+// a numeric refactorisation of the same pattern keeps it valid.
+struct CpuSolvePlan {
+    int32_t n = 0;
+    std::vector<int32_t> sn_start;    // supernodes: columns [sn_start[s], sn_start[s+1])
+    std::vector<int32_t> task_first;  // subtree tasks: supernodes [task_first[t], task_last[t]]
+    std::vector<int32_t> task_last;
+    std::vector<int64_t> task_cost;   // nnz(L) of a task's columns (tasks sorted by it, descending)
+    std::vector<int32_t> top_sn;      // supernodes outside every task, ascending
+    std::vector<int32_t> top_rows;    // their columns, ascending
+    std::vector<int64_t> pt_ptr;      // per top row: its entries L(i, j) in task columns j
+    std::vector<int32_t> pt_col;
+    std::vector<int64_t> pt_pos;      // position of L(i, j) in rowidx / vals
+    int32_t max_nr = 0;               // most off-diagonal rows of one supernode
+};
+
+void cpu_plan(const Factor& F, CpuSolvePlan& P, int32_t threads);
+
+// Host solve x = P^T L^-T L^-1 P b in FP64 (the CPU-array solve of the
+// reference, src/cholesky_solver.cpp:435-463). b and x are row-major
+// (n, nrhs) arrays of float (precision 0) or double (1), read and rounded like
+// the reference's copies in and out; they may alias. threads = 0 uses every
+// host core; the result does not depend on the thread count.
+void cpu_solve(const Factor& F, const CpuSolvePlan& P, int32_t precision, int32_t nrhs, const void* b, void* x,
+               int32_t threads);
 
 }  // namespace gbchol

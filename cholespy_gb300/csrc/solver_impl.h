@@ -105,6 +105,8 @@ using namespace gbchol;
 
 struct gbchol_host_factor {
     Factor F;
+    CpuSolvePlan cpu;         // host solve structure, built at the first host solve
+    bool cpu_ready = false;
 };
 
 struct gbchol_solver {

@@ -4,10 +4,12 @@ Mirrors the reference's nanobind module (src/main.cpp:16-136): the same
 constructor ``(n_rows, ii, jj, x, type)`` and ``solve(b, x)``, the same
 argument checks and error messages, and the same asynchronous in-place write
 of ``x``. Arrays may be torch tensors, NumPy arrays or anything exporting
-DLPack / ``__cuda_array_interface__`` (CuPy, JAX, ...). Solves run on the
-GB300 through the gbchol C ABI; the solver lives on the CUDA device of the
-constructor's arrays (the reference always uses device 0,
-src/cuda_driver.cpp:124).
+DLPack / ``__cuda_array_interface__`` (CuPy, JAX, ...). A solver built from
+CUDA arrays solves on the GB300 through the gbchol C ABI and lives on the
+CUDA device of those arrays (the reference always uses device 0,
+src/cuda_driver.cpp:124). A solver built from CPU arrays solves CPU arrays
+on the host cores (gbchol_factor_solve, the reference's solve_cpu path,
+src/main.cpp:68-70, 83-91); the two never stand in for each other.
 
 Extensions beyond the reference (keyword-only, off by default):
 ``CholeskySolverD(..., refine=True)`` keeps an FP32 factor plus the FP64
@@ -153,6 +155,8 @@ class _CholeskySolver:
     def __init__(self, n_rows, ii, jj, x, type, *, refine=False, tol=1e-10, max_iter=10):
         lib = _ffi.lib()
         self._h = None
+        self._fh = None
+        self._cpu = False
         n_rows = int(n_rows)
         if n_rows < 0 or n_rows > np.iinfo(np.uint32).max:
             raise ValueError("n_rows out of range.")
@@ -165,9 +169,8 @@ class _CholeskySolver:
         if dev_type != "cuda" and dev_type != "cpu":
             raise ValueError("Unsupported input device! Only CPU and CUDA arrays are supported.")
         if dev_type == "cpu":
-            raise ValueError(
-                "The GB300 solver runs on CUDA: pass CUDA arrays (CPU-array solvers are "
-                "not provided by this build).")
+            self._init_cpu(n_rows, nx, ii, jj, x, type)
+            return
         device = _device_of(x)[1]
         self._device = device
         self._refine = bool(refine) and self._precision == 1
@@ -188,6 +191,24 @@ class _CholeskySolver:
         self._h = h
         self._n = n_rows
 
+    def _init_cpu(self, n_rows, nx, ii, jj, x, type):
+        # CPU arrays: factorise on the host and keep the factor there; solves
+        # take CPU arrays only (src/main.cpp:68-70, cholesky_solver.cpp:435-463)
+        self._cpu = True
+        self._device = None
+        self._refine = False
+        self._tol = 1e-10
+        self._max_iter = 10
+        hi = _host_vector(ii, np.int32, "ii")
+        hj = _host_vector(jj, np.int32, "jj")
+        hx = _host_vector(x, np.float64, "x")
+        fh = C.c_void_p()
+        st = _ffi.lib().gbchol_factorize(n_rows, int(nx), _ptr(hi), _ptr(hj), _ptr(hx), int(type), 0,
+                                         C.byref(fh))
+        _ffi.check(st)
+        self._fh = fh
+        self._n = n_rows
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
@@ -196,6 +217,22 @@ class _CholeskySolver:
             except Exception:
                 pass
             self._h = None
+        fh = getattr(self, "_fh", None)
+        if fh:
+            try:
+                _ffi.lib().gbchol_factor_free(fh)
+            except Exception:
+                pass
+            self._fh = None
+
+    @property
+    def is_cpu(self):
+        """True for a solver built from CPU arrays (it solves CPU arrays)."""
+        return self._cpu
+
+    def _gpu_only(self, what):
+        if self._cpu:
+            raise RuntimeError(f"{what} needs a solver built from CUDA arrays.")
 
     # -- checks of src/main.cpp:83-100 --------------------------------------
     def _prepare(self, b, x, dtype):
@@ -209,10 +246,14 @@ class _CholeskySolver:
         if db[0] != dx[0]:
             raise ValueError("x and b should be on the same device.")
         if db[0] == "cpu":
-            raise ValueError("Input device is CPU but the solver was initialized for CUDA.")
-        if db[0] != "cuda":
+            if not self._cpu:
+                raise ValueError("Input device is CPU but the solver was initialized for CUDA.")
+        elif db[0] == "cuda":
+            if self._cpu:
+                raise ValueError("Input device is CUDA but the solver was initialized for CPU.")
+        else:
             raise ValueError("Unsupported input device! Only CPU and CUDA arrays are supported.")
-        if tb.device.index != self._device or tx.device.index != self._device:
+        if not self._cpu and (tb.device.index != self._device or tx.device.index != self._device):
             raise ValueError("x and b should be on the device the solver was created on.")
         if tb.dtype != dtype or tx.dtype != dtype:
             raise TypeError(f"solve(): b and x must be {dtype} arrays (no implicit conversion).")
@@ -221,6 +262,8 @@ class _CholeskySolver:
         if tb.shape[0] != self._n:
             raise ValueError("b and x must have n_rows rows.")
         nrhs = tb.shape[1] if tb.dim() == 2 else 1
+        if self._cpu:
+            return tb, tx, nrhs, None
         stream = torch.cuda.current_stream(self._device).cuda_stream
         return tb, tx, nrhs, stream
 
@@ -230,11 +273,22 @@ class _CholeskySolver:
         torch = _torch()
         dtype = torch.float32 if self._precision == 0 else torch.float64
         tb, tx, nrhs, stream = self._prepare(b, x, dtype)
+        if self._cpu:
+            self._solve_cpu(tb, tx, nrhs)
+            return
         if self._refine:
             self._solve_refined(tb, tx, nrhs, stream, self._tol, self._max_iter, stats=False)
             return
         st = _ffi.lib().gbchol_solve(self._h, self._precision, nrhs, C.c_void_p(tb.data_ptr()),
                                      C.c_void_p(tx.data_ptr()), C.c_void_p(stream))
+        _ffi.check(st)
+
+    def _solve_cpu(self, tb, tx, nrhs):
+        # host solve in FP64 (blocks until x is written, like cholmod_solve)
+        if tx.numel() and not _writable(tx):
+            raise ValueError("solve(): x must be writable.")
+        st = _ffi.lib().gbchol_factor_solve(self._fh, self._precision, int(nrhs), C.c_void_p(tb.data_ptr()),
+                                            C.c_void_p(tx.data_ptr()), 0)
         _ffi.check(st)
 
     def _solve_refined(self, tb, tx, nrhs, stream, tol, max_iter, stats):
@@ -250,11 +304,15 @@ class _CholeskySolver:
         return None
 
     def check(self):
-        """Synchronise and raise if a device-side wait expired in a solve."""
+        """Synchronise and raise if a device-side wait expired in a solve
+        (nothing to check for a CPU solver: its solves are synchronous)."""
+        if self._cpu:
+            return
         _ffi.check(_ffi.lib().gbchol_check(self._h))
 
     def reserve(self, n_rhs):
         """Preallocate scratch for up to n_rhs RHS (before CUDA-graph capture)."""
+        self._gpu_only("reserve")
         _ffi.check(_ffi.lib().gbchol_reserve(self._h, int(n_rhs)))
 
     def refactorize(self, ii, jj, x, type):
@@ -269,6 +327,10 @@ class _CholeskySolver:
         hi = _host_vector(ii, np.int32, "ii")
         hj = _host_vector(jj, np.int32, "jj")
         hx = _host_vector(x, np.float64, "x")
+        if self._cpu:
+            _ffi.check(_ffi.lib().gbchol_factor_refactorize(self._fh, int(nx), _ptr(hi), _ptr(hj), _ptr(hx),
+                                                            int(type), 0))
+            return
         torch = _torch()
         with torch.cuda.device(self._device):
             st = _ffi.lib().gbchol_refactorize(self._h, int(nx), _ptr(hi), _ptr(hj), _ptr(hx), int(type))
@@ -281,6 +343,7 @@ class _CholeskySolver:
         and hand the rest to partial sums of about `part_group` blocks.
         Results change only by rounding. Batches built from this solver must
         be built again. No counterpart in the reference."""
+        self._gpu_only("replan")
         _ffi.check(_ffi.lib().gbchol_replan(self._h, int(min_top_width), int(part_keep), int(part_group)))
 
     def autotune(self, n_rhs, precision=None, candidates=(4, 8, 16, 32), reps=3):
@@ -289,6 +352,7 @@ class _CholeskySolver:
         width. `precision`: "float" / "double" (default: the precision the
         solver's solves run in; FP32 for a refining CholeskySolverD). No
         counterpart in the reference."""
+        self._gpu_only("autotune")
         if precision is None:
             prec = 0 if (self._precision == 0 or self._refine) else 1
         else:
@@ -300,6 +364,7 @@ class _CholeskySolver:
         return int(chosen.value)
 
     def info(self) -> SolverInfo:
+        self._gpu_only("info")
         inf = _ffi.Info()
         _ffi.check(_ffi.lib().gbchol_get_info(self._h, C.byref(inf)))
         return SolverInfo(inf.n, inf.device, inf.nnz_a, inf.nnz_l, inf.levels_lower,
@@ -309,6 +374,7 @@ class _CholeskySolver:
 
     def levels(self, lower=True):
         """(row_levels, order, max_lvl) of the analysis of L (lower) or L^T."""
+        self._gpu_only("levels")
         n = self._n
         lev = np.zeros(n, np.int32)
         order = np.zeros(n, np.int32)
@@ -320,6 +386,17 @@ class _CholeskySolver:
     def factor(self):
         """Host copy (perm, colptr, rowidx, vals) of the factor L (CSC, diagonal first)."""
         n = self._n
+        if self._cpu:
+            nn, nz, nsn, fl = C.c_int32(), C.c_int64(), C.c_int32(), C.c_double()
+            _ffi.check(_ffi.lib().gbchol_factor_info(self._fh, C.byref(nn), C.byref(nz), C.byref(nsn),
+                                                     C.byref(fl)))
+            perm = np.zeros(n, np.int32)
+            colptr = np.zeros(n + 1, np.int32)
+            rowidx = np.zeros(nz.value, np.int32)
+            vals = np.zeros(nz.value, np.float64)
+            _ffi.check(_ffi.lib().gbchol_factor_export(self._fh, _ptr(perm), _ptr(colptr), _ptr(rowidx),
+                                                       _ptr(vals)))
+            return perm, colptr, rowidx, vals
         nnz = self.info().nnz_l
         perm = np.zeros(n, np.int32)
         colptr = np.zeros(n + 1, np.int32)
@@ -360,6 +437,8 @@ class _CholeskySolver:
             raise ValueError("Inconsistent factor arrays in the file.")
         self = cls.__new__(cls)
         self._h = None
+        self._fh = None
+        self._cpu = False
         self._device = int(device)
         self._refine = False
         self._tol = 1e-10
@@ -378,6 +457,13 @@ class _CholeskySolver:
     @property
     def handle(self):
         return self._h
+
+
+def _writable(t):
+    try:
+        return bool(t.numpy().flags.writeable)
+    except (RuntimeError, TypeError, ValueError):
+        return True
 
 
 def _len(a):
@@ -405,6 +491,7 @@ class CholeskySolverD(_CholeskySolver):
 
     def solve_refined(self, b, x, tol=None, max_iter=None) -> RefineResult:
         """FP32 solve + FP64 iterative refinement; synchronises and returns stats."""
+        self._gpu_only("solve_refined")
         if not self._refine:
             raise RuntimeError("solve_refined needs CholeskySolverD(..., refine=True).")
         torch = _torch()
@@ -416,6 +503,9 @@ class CholeskySolverD(_CholeskySolver):
         """Plain FP64 solve regardless of ``refine``."""
         torch = _torch()
         tb, tx, nrhs, stream = self._prepare(b, x, torch.float64)
+        if self._cpu:
+            self._solve_cpu(tb, tx, nrhs)
+            return
         st = _ffi.lib().gbchol_solve(self._h, 1, nrhs, C.c_void_p(tb.data_ptr()),
                                      C.c_void_p(tx.data_ptr()), C.c_void_p(stream))
         _ffi.check(st)

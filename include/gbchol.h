@@ -120,6 +120,22 @@ int gbchol_factor_free(gbchol_factor_handle f);
 int gbchol_factor_refactorize(gbchol_factor_handle f, int64_t nnz, const int32_t* ii, const int32_t* jj,
                               const double* x, int32_t matrix_type, int32_t threads);
 
+/*
+ * x = A^{-1} b on HOST arrays with a host factor: the solve of solvers built
+ * from CPU arrays. Replaces CholeskySolver<Float>::solve_cpu
+ * (src/cholesky_solver.cpp:435-463), i.e. cholmod_solve(CHOLMOD_A) on the
+ * reference's CPU-side factor (src/main.cpp:68-70, 83-91): b is read as FP64,
+ * the solve runs in FP64 on the factor's values and x is rounded to the
+ * arrays' type. precision 0 = float b/x, 1 = double b/x; row-major (n, nrhs);
+ * any nrhs >= 0 (the reference's CPU path has no 128 limit); b and x may
+ * alias. threads = 0 uses every host core; the result does not depend on the
+ * thread count. The first call builds the solve's structure (kept until the
+ * factor is freed; a refactorisation keeps it). Blocks until x is written.
+ * This path never runs for CUDA arrays: those go through gbchol_solve.
+ */
+int gbchol_factor_solve(gbchol_factor_handle f, int32_t precision, int32_t nrhs, const void* b, void* x,
+                        int32_t threads);
+
 /* Free every device and host buffer of the solver (src/cholesky_solver.cpp:465-486). */
 int gbchol_destroy(gbchol_handle h);
 
