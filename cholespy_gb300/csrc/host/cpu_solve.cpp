@@ -42,7 +42,7 @@ namespace gbchol {
 namespace {
 
 constexpr int32_t PB = 64;   // panel width of the blocked triangular solves
-constexpr int32_t QB = 256;  // rows per block of a panel's update
+constexpr int32_t QB = 1024;  // rows per block of a panel's update
 constexpr int32_t JB = 16;   // columns per block of a backward dot product
 constexpr int WMAX = 8;      // widest RHS chunk
 
@@ -69,6 +69,39 @@ struct Fac {
     const double* v;    // values
 };
 
+// Chunk rows of W doubles (W even) as W/2 pairs in GCC vector types (SSE2 /
+// NEON registers on both host architectures; no ISA-specific code). Written
+// out so that the arithmetic runs along the RHS columns: left alone, the
+// compiler's vectoriser paired values of different factor columns and reduced
+// them with scalar adds, which ran at a third of this speed.
+typedef double v2d __attribute__((vector_size(16)));
+
+template <int W>
+struct Row {
+    v2d v[W / 2];
+    static Row zero() {
+        Row r;
+        for (int c = 0; c < W / 2; ++c) r.v[c] = v2d{0.0, 0.0};
+        return r;
+    }
+    static Row load(const double* p) {
+        Row r;
+        std::memcpy(r.v, p, sizeof(double) * W);
+        return r;
+    }
+    void store(double* p) const { std::memcpy(p, v, sizeof(double) * W); }
+    void add_scaled(double l, const double* y) {  // this += l * y
+        const v2d s = {l, l};
+        const Row yr = load(y);
+        for (int c = 0; c < W / 2; ++c) v[c] += s * yr.v[c];
+    }
+    void sub_from(double* p) const {  // p -= this
+        Row r = load(p);
+        for (int c = 0; c < W / 2; ++c) r.v[c] -= v[c];
+        r.store(p);
+    }
+};
+
 // Column-block kernels on one RHS chunk Y (n rows of W doubles).
 template <int W>
 struct Kern {
@@ -79,69 +112,130 @@ struct Kern {
             const double* col = f.v + f.cp[j];
             double* yj = Y + (int64_t)j * W;
             const double d = col[0];
-            for (int c = 0; c < W; ++c) yj[c] /= d;
-            for (int32_t i = j + 1; i < p1; ++i) {
-                const double l = col[i - j];
-                double* yi = Y + (int64_t)i * W;
-                for (int c = 0; c < W; ++c) yi[c] -= l * yj[c];
+            if constexpr (W == 1) {
+                yj[0] /= d;
+                for (int32_t i = j + 1; i < p1; ++i) Y[i] -= col[i - j] * yj[0];
+            } else {
+                Row<W> y = Row<W>::load(yj);
+                const v2d dv = {d, d};
+                for (int c = 0; c < W / 2; ++c) y.v[c] /= dv;
+                y.store(yj);
+                for (int32_t i = j + 1; i < p1; ++i) {
+                    Row<W> t = Row<W>::zero();
+                    t.add_scaled(col[i - j], yj);
+                    t.sub_from(Y + (int64_t)i * W);
+                }
             }
         }
     }
 
     // Rows q in [q0, q1) below panel [p0, p1) of a supernode ending at column
     // c1: below-row q is row p1 + q for q < c1 - p1, else R[q - (c1 - p1)],
-    // and sits at offset (p1 - j) + q of column j. y_row -= sum_j L(row, j) y_j.
+    // and sits at offset (p1 - j) + q of column j. y_row -= sum_j L(row, j) y_j,
+    // the sum taken over j ascending from zero into `acc`. One RHS: columns
+    // outer, a vector update across rows; wider chunks: blocks of 8 columns,
+    // rows outer (the same order of operations).
     static void fwd_rect(const Fac& f, const int32_t* R, int32_t c1, int32_t p0, int32_t p1, int32_t q0,
                          int32_t q1, double* Y, double* acc) {
-        const int32_t nq = q1 - q0;
-        std::fill(acc, acc + (int64_t)nq * W, 0.0);
-        for (int32_t j = p0; j < p1; ++j) {
-            const double* lj = f.v + f.cp[j] + (p1 - j) + q0;
-            const double* yj = Y + (int64_t)j * W;
-            double yv[W];
-            for (int c = 0; c < W; ++c) yv[c] = yj[c];
-            for (int32_t q = 0; q < nq; ++q) {
-                const double l = lj[q];
-                double* a = acc + (int64_t)q * W;
-                for (int c = 0; c < W; ++c) a[c] += l * yv[c];
-            }
-        }
         const int32_t nin = c1 - p1;
-        for (int32_t q = 0; q < nq; ++q) {
-            const int32_t qq = q0 + q;
-            const int32_t row = qq < nin ? p1 + qq : R[qq - nin];
-            double* yr = Y + (int64_t)row * W;
-            const double* a = acc + (int64_t)q * W;
-            for (int c = 0; c < W; ++c) yr[c] -= a[c];
+        const int32_t nq = q1 - q0;
+        auto row_of = [&](int32_t qq) { return qq < nin ? p1 + qq : R[qq - nin]; };
+        std::fill(acc, acc + (int64_t)nq * W, 0.0);
+        if constexpr (W == 1) {
+            for (int32_t j = p0; j < p1; ++j) {
+                const double* lj = f.v + f.cp[j] + (p1 - j) + q0;
+                const double yj = Y[j];
+                for (int32_t q = 0; q < nq; ++q) acc[q] += lj[q] * yj;
+            }
+            for (int32_t q = 0; q < nq; ++q) Y[row_of(q0 + q)] -= acc[q];
+        } else {
+            for (int32_t kb = p0; kb < p1; kb += 8) {
+                const int32_t nk = std::min(8, p1 - kb);
+                const double* col[8];
+                for (int32_t k = 0; k < nk; ++k) col[k] = f.v + f.cp[kb + k] + (p1 - kb - k) + q0;
+                const double* yk = Y + (int64_t)kb * W;
+                if (nk == 8) {
+                    int32_t q = 0;
+                    for (; q + 2 <= nq; q += 2) {  // two rows share each y load
+                        Row<W> t0 = Row<W>::load(acc + (int64_t)q * W);
+                        Row<W> t1 = Row<W>::load(acc + (int64_t)(q + 1) * W);
+                        for (int k = 0; k < 8; ++k) {
+                            const double l0 = col[k][q], l1 = col[k][q + 1];
+                            const v2d s0 = {l0, l0}, s1 = {l1, l1};
+                            const Row<W> y = Row<W>::load(yk + k * W);
+                            for (int c = 0; c < W / 2; ++c) {
+                                t0.v[c] += s0 * y.v[c];
+                                t1.v[c] += s1 * y.v[c];
+                            }
+                        }
+                        t0.store(acc + (int64_t)q * W);
+                        t1.store(acc + (int64_t)(q + 1) * W);
+                    }
+                    for (; q < nq; ++q) {
+                        Row<W> t = Row<W>::load(acc + (int64_t)q * W);
+                        for (int k = 0; k < 8; ++k) t.add_scaled(col[k][q], yk + k * W);
+                        t.store(acc + (int64_t)q * W);
+                    }
+                } else {
+                    for (int32_t q = 0; q < nq; ++q) {
+                        Row<W> t = Row<W>::load(acc + (int64_t)q * W);
+                        for (int32_t k = 0; k < nk; ++k) t.add_scaled(col[k][q], yk + (int64_t)k * W);
+                        t.store(acc + (int64_t)q * W);
+                    }
+                }
+            }
+            for (int32_t q = 0; q < nq; ++q) Row<W>::load(acc + (int64_t)q * W).sub_from(Y + (int64_t)row_of(q0 + q) * W);
         }
     }
 
     // y_j -= sum_{q < m} L(below q, j) z_q for j in [j0, j1), where below-row
-    // q of column j sits at offset (base - j) + q. Four partial sums over q
-    // (q mod 4), combined in a fixed order.
+    // q of column j sits at offset (base - j) + q. The sum over q is split
+    // into partial sums (4 for one RHS, 2 for two, 1 for wider chunks) that
+    // are combined in a fixed order; wider chunks take two columns at a time.
     static void bwd_dot(const Fac& f, int32_t base, int32_t j0, int32_t j1, int32_t m, const double* Z,
                         double* Y) {
-        for (int32_t j = j0; j < j1; ++j) {
-            const double* lj = f.v + f.cp[j] + (base - j);
-            double s0[W] = {}, s1[W] = {}, s2[W] = {}, s3[W] = {};
-            int32_t q = 0;
-            for (; q + 4 <= m; q += 4) {
-                const double l0 = lj[q], l1 = lj[q + 1], l2 = lj[q + 2], l3 = lj[q + 3];
-                const double* z = Z + (int64_t)q * W;
-                for (int c = 0; c < W; ++c) {
-                    s0[c] += l0 * z[c];
-                    s1[c] += l1 * z[W + c];
-                    s2[c] += l2 * z[2 * W + c];
-                    s3[c] += l3 * z[3 * W + c];
+        if constexpr (W == 1) {
+            for (int32_t j = j0; j < j1; ++j) {
+                const double* lj = f.v + f.cp[j] + (base - j);
+                double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                int32_t q = 0;
+                for (; q + 4 <= m; q += 4) {
+                    s0 += lj[q] * Z[q];
+                    s1 += lj[q + 1] * Z[q + 1];
+                    s2 += lj[q + 2] * Z[q + 2];
+                    s3 += lj[q + 3] * Z[q + 3];
                 }
+                for (; q < m; ++q) s0 += lj[q] * Z[q];
+                Y[j] -= (s0 + s1) + (s2 + s3);
             }
-            for (; q < m; ++q) {
-                const double l = lj[q];
-                const double* z = Z + (int64_t)q * W;
-                for (int c = 0; c < W; ++c) s0[c] += l * z[c];
+        } else {
+            constexpr int NP = W == 2 ? 2 : 1;  // partial sums per column
+            for (int32_t j = j0; j < j1; j += 2) {
+                const bool two = j + 1 < j1;
+                const double* la = f.v + f.cp[j] + (base - j);
+                const double* lb = two ? f.v + f.cp[j + 1] + (base - j - 1) : la;
+                Row<W> sa[NP], sb[NP];
+                for (int p = 0; p < NP; ++p) sa[p] = sb[p] = Row<W>::zero();
+                int32_t q = 0;
+                for (; q + NP <= m; q += NP)
+                    for (int p = 0; p < NP; ++p) {
+                        const double* z = Z + (int64_t)(q + p) * W;
+                        sa[p].add_scaled(la[q + p], z);
+                        sb[p].add_scaled(lb[q + p], z);
+                    }
+                for (; q < m; ++q) {
+                    const double* z = Z + (int64_t)q * W;
+                    sa[0].add_scaled(la[q], z);
+                    sb[0].add_scaled(lb[q], z);
+                }
+                for (int p = 1; p < NP; ++p)
+                    for (int c = 0; c < W / 2; ++c) {
+                        sa[0].v[c] += sa[p].v[c];
+                        sb[0].v[c] += sb[p].v[c];
+                    }
+                sa[0].sub_from(Y + (int64_t)j * W);
+                if (two) sb[0].sub_from(Y + (int64_t)(j + 1) * W);
             }
-            double* yj = Y + (int64_t)j * W;
-            for (int c = 0; c < W; ++c) yj[c] -= (s0[c] + s1[c]) + (s2[c] + s3[c]);
         }
     }
 
@@ -150,15 +244,19 @@ struct Kern {
     static void bwd_tri(const Fac& f, int32_t p0, int32_t p1, double* Y) {
         for (int32_t j = p1 - 1; j >= p0; --j) {
             const double* col = f.v + f.cp[j];
-            double a[W] = {};
-            for (int32_t i = j + 1; i < p1; ++i) {
-                const double l = col[i - j];
-                const double* yi = Y + (int64_t)i * W;
-                for (int c = 0; c < W; ++c) a[c] += l * yi[c];
-            }
-            double* yj = Y + (int64_t)j * W;
             const double d = col[0];
-            for (int c = 0; c < W; ++c) yj[c] = (yj[c] - a[c]) / d;
+            if constexpr (W == 1) {
+                double a = 0;
+                for (int32_t i = j + 1; i < p1; ++i) a += col[i - j] * Y[i];
+                Y[j] = (Y[j] - a) / d;
+            } else {
+                Row<W> a = Row<W>::zero();
+                for (int32_t i = j + 1; i < p1; ++i) a.add_scaled(col[i - j], Y + (int64_t)i * W);
+                Row<W> y = Row<W>::load(Y + (int64_t)j * W);
+                const v2d dv = {d, d};
+                for (int c = 0; c < W / 2; ++c) y.v[c] = (y.v[c] - a.v[c]) / dv;
+                y.store(Y + (int64_t)j * W);
+            }
         }
     }
 };
@@ -250,14 +348,16 @@ struct Io {
 template <int W>
 void top_gather(const CpuSolvePlan& P, const Fac& f, int32_t t, double* Y) {
     const int32_t i = P.top_rows[t];
-    double a[W] = {};
-    for (int64_t e = P.pt_ptr[t]; e < P.pt_ptr[t + 1]; ++e) {
-        const double l = f.v[P.pt_pos[e]];
-        const double* yj = Y + (int64_t)P.pt_col[e] * W;
-        for (int c = 0; c < W; ++c) a[c] += l * yj[c];
+    if constexpr (W == 1) {
+        double a = 0;
+        for (int64_t e = P.pt_ptr[t]; e < P.pt_ptr[t + 1]; ++e) a += f.v[P.pt_pos[e]] * Y[P.pt_col[e]];
+        Y[i] -= a;
+    } else {
+        Row<W> a = Row<W>::zero();
+        for (int64_t e = P.pt_ptr[t]; e < P.pt_ptr[t + 1]; ++e)
+            a.add_scaled(f.v[P.pt_pos[e]], Y + (int64_t)P.pt_col[e] * W);
+        a.sub_from(Y + (int64_t)i * W);
     }
-    double* yi = Y + (int64_t)i * W;
-    for (int c = 0; c < W; ++c) yi[c] -= a[c];
 }
 
 template <typename T>
