@@ -239,3 +239,39 @@ def test_cpu_solver_refactorize_and_factor(gblib):
     x = np.zeros_like(b)
     s.solve(b, x)
     np.testing.assert_allclose(x, spsolve_ref(n, vals2, idx, b), rtol=1e-10, atol=1e-12)
+
+
+def _structural_cases():
+    import scipy.sparse as sp
+    blocks = []
+    for k in range(40):  # a forest: 40 disconnected grids of different sizes
+        m = 5 + (k * 7) % 23
+        vals, idx = workloads.grid2d_coo(m, 10.0, 1.0)
+        blocks.append(sp.coo_matrix((vals, idx), shape=(m * m, m * m)).tocsr())
+    forest = sp.block_diag(blocks).tocoo()
+    n = 3000  # a star: one row coupled to every other
+    rows = np.r_[np.arange(n), np.arange(1, n)]
+    cols = np.r_[np.arange(n), np.zeros(n - 1, int)]
+    vals = np.r_[np.full(n, 4.0), np.full(n - 1, -1.0 / np.sqrt(n))]
+    star = sp.coo_matrix((vals, (rows, cols)), shape=(n, n))
+    star = (star + sp.tril(star, -1).T).tocoo()
+    return {"forest": forest, "star": star, "diagonal": (sp.identity(500) * 3.0).tocoo()}
+
+
+@pytest.mark.parametrize("case", ["forest", "star", "diagonal"])
+def test_host_solve_structures(gblib, case):
+    """Elimination forests (several roots), a dense row and no off-diagonal
+    entries: solutions vs spsolve, bit-identical for 1 and all threads."""
+    from scipy.sparse.linalg import spsolve
+    A = _structural_cases()[case]
+    n = A.shape[0]
+    f, _ = _factorize(gblib, n, A.data, (A.row, A.col))
+    try:
+        for r in (1, 5, 40):
+            b = np.random.default_rng(r).standard_normal((n, r))
+            x = _host_solve(gblib, f, b, 1, 0)
+            xr = spsolve(A.tocsc(), b).reshape(b.shape)
+            assert np.abs(x - xr).max() <= 1e-10 * np.abs(xr).max()
+            assert np.array_equal(x, _host_solve(gblib, f, b, 1, 1))
+    finally:
+        gblib.gbchol_factor_free(f)
