@@ -41,13 +41,14 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["poisson64", "batch", "autograd", "ico6", "grid64", "solve"],
+    p.add_argument("--workload", choices=["poisson64", "batch", "autograd", "ico6", "grid64", "solve", "cpu"],
                    default="poisson64",
                    help="poisson64 (default, headline): 64^3 FP32+IR; batch: 256 grid systems "
                         "in one graph-captured persistent launch; autograd: icosphere-7 forward+"
                         "backward; ico6: icosphere-6 FP32 n_rhs=3; grid64: 64x64 FP64 n_rhs=1; "
                         "solve: plain solves of the k^3 Poisson system (--k, --nrhs, --fp64), "
-                        "the program profiled with ncu")
+                        "the program profiled with ncu; cpu: the CPU-array path (no GPU) on the "
+                        "reference's published configuration, icosphere 6 with --nrhs float32 RHS")
     p.add_argument("--fp64", action="store_true", help="solve workload: FP64 instead of FP32")
     p.add_argument("--k", type=int, default=64, help="grid side (n = k^3)")
     p.add_argument("--nrhs", type=int, default=128)
@@ -734,6 +735,65 @@ def run_solve(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+# published: cholespy CPU solve, icosphere 6, 128 float32 RHS, 194.82 ms on a
+# Ryzen 3990X (tests/benchmark.jpg of the reference)
+PUBLISHED_CPU_SOLVE_S = 0.19482
+
+
+def run_cpu(args, world, rank):
+    """cpu: solvers built from CPU arrays, on the host cores (no GPU). The
+    reference's benchmark procedure (tests/Benchmark.ipynb:238-275 with CPU
+    arrays): icosphere 6, A = I + lambda L for lambda = 1, 2, ... (one
+    construction each), then solves of --nrhs float32 RHS b ~ U[0,1), each
+    timed with its torch.zeros_like as in the notebook."""
+    import scipy.sparse as sp
+    import torch
+
+    from cholespy_gb300 import CholeskySolverF, MatrixType, _build, workloads
+    _build.build()
+    if rank != 0:
+        return
+    n, faces, _ = workloads.icosphere(6)
+    t_ctor = []
+    for lam in range(1, 1 + max(3, min(args.steps, 20))):
+        vals, idx = workloads.laplacian_coo(n, faces, float(lam))
+        ii, jj, xx = torch.tensor(idx[0]), torch.tensor(idx[1]), torch.tensor(vals)
+        c0 = time.perf_counter()
+        s = CholeskySolverF(n, ii, jj, xx, MatrixType.COO)
+        t_ctor.append(time.perf_counter() - c0)
+    b = torch.rand(n, args.nrhs, generator=torch.Generator().manual_seed(0))
+    for _ in range(args.warmup):
+        x = torch.zeros_like(b)
+        s.solve(b, x)
+    ts = []
+    for _ in range(args.steps):
+        c0 = time.perf_counter()
+        x = torch.zeros_like(b)
+        s.solve(b, x)
+        ts.append(time.perf_counter() - c0)
+    t = float(sum(ts))
+    A = sp.csr_matrix((vals, (idx[0], idx[1])), shape=(n, n))
+    xb, bb = x.numpy().astype(np.float64), b.numpy().astype(np.float64)
+    res = float((np.linalg.norm(A @ xb - bb, axis=0) / np.linalg.norm(bb, axis=0)).max())
+    perm, Lp, Li, Lx = s.factor()
+    v_or, cores = _cpu_sample(perm, Lp, Li, Lx, b.numpy().astype(np.float64), args.nrhs)
+    value = args.nrhs * args.steps / t
+    line = _line(args, world, "RHS-solves/s (CPU arrays)", value, "RHS-solves/s", t, "f64",
+                 {"workload": f"icosphere6_I+lambdaL_coo_cpu_arrays_f32_nrhs{args.nrhs}", "n": n,
+                  "lambda": len(t_ctor), "constructions": len(t_ctor),
+                  "nnz_l": int(len(Li)), "n_rhs": args.nrhs, "rhs": "U[0,1) float32 seed 0",
+                  "construction_ms_median": 1e3 * float(np.median(t_ctor)),
+                  "solve_ms_median": 1e3 * float(np.median(ts)),
+                  "max_rel_residual": res, "host_cores": cores},
+                 cpu_baseline={"value": v_or, "unit": "RHS-solves/s", "cores": cores, "kind": "port",
+                               "sample": "one FP64 solve of all RHS (cholmod_solve semantics), same factor"},
+                 gpu_launches=0)
+    line["n_gpus"] = 0
+    if args.nrhs == 128:
+        line["vs_baseline"] = value / (128 / PUBLISHED_CPU_SOLVE_S)
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup(args)
@@ -748,6 +808,8 @@ def main():
             run_mesh(args, world, rank, local)
         elif args.workload == "solve":
             run_solve(args, world, rank, local)
+        elif args.workload == "cpu":
+            run_cpu(args, world, rank)
         else:
             run_ours(args, world, rank, local)
     finally:

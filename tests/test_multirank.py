@@ -56,3 +56,16 @@ def test_reference_arm_two_ranks():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["metric"].startswith("RHS-solves/s")
+
+
+def test_bench_cpu_workload_line():
+    """`bench.py --workload cpu` (the CPU-array path, no GPU) prints one JSON
+    line with the contract keys and a converged FP32-rounded solution."""
+    out = subprocess.run([sys.executable, "bench.py", "--workload", "cpu", "--steps", "2", "--warmup", "1",
+                          "--nrhs", "16"], cwd=str(ROOT), capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "config", "cpu_baseline"):
+        assert key in line
+    assert line["value"] > 0 and line["gpu_launches"] == 0
+    assert line["config"]["max_rel_residual"] < 1e-5
