@@ -432,6 +432,7 @@ int gbchol_create(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t*
     h->t_factor = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (st == ST_NOT_POSDEF) return fail(GBCHOL_ENOTPOSDEF, "Matrix is not positive definite!");
     if (st != ST_OK) return fail(st == ST_NOMEM ? GBCHOL_ENOMEM : GBCHOL_EINVAL, err);
+    record_input(h->F, nnz, ii, jj, matrix_type);
     if (store & GBCHOL_STORE_A64) {
         Csc S;
         symmetric_from_lower(A, S);
@@ -457,7 +458,14 @@ int refactor_values(const Factor& old, int32_t n, int64_t nnz, const int32_t* ii
     if (matrix_type != GBCHOL_COO && !ii) return fail(GBCHOL_EINVAL, "Null pointer array.");
     if ((int32_t)old.perm.size() != n) return fail(GBCHOL_ESTATE, "No factor to refactorise.");
     std::string err;
-    Status st = build_csc(n, nnz, ii, jj, x, matrix_type, A, err);
+    Status st = ST_OK;
+    // the input pattern the factor was made from: numeric phase only
+    if (refactor_cached(old, nnz, ii, jj, x, matrix_type, threads, A, Fn.vals, Fn.flops, st, err)) {
+        if (st == ST_NOT_POSDEF) return fail(GBCHOL_ENOTPOSDEF, "Matrix is not positive definite!");
+        if (st != ST_OK) return fail(st == ST_NOMEM ? GBCHOL_ENOMEM : GBCHOL_EINVAL, err);
+        return GBCHOL_OK;
+    }
+    st = build_csc(n, nnz, ii, jj, x, matrix_type, A, err);
     if (st != ST_OK) return fail(GBCHOL_EINVAL, err);
     FactorOptions opt;
     opt.threads = threads;
@@ -573,6 +581,7 @@ int gbchol_factorize(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32
     st = factorize(A, opt, f->F, err);
     if (st == ST_NOT_POSDEF) return fail(GBCHOL_ENOTPOSDEF, "Matrix is not positive definite!");
     if (st != ST_OK) return fail(st == ST_NOMEM ? GBCHOL_ENOMEM : GBCHOL_EINVAL, err);
+    record_input(f->F, nnz, ii, jj, matrix_type);
     *out = f.release();
     return GBCHOL_OK;
 }

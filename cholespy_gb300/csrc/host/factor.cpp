@@ -20,6 +20,7 @@
 //     34, 1992) with dense blocked kernels (dense.cpp).
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <memory>
 #include <numeric>
 
@@ -46,10 +47,14 @@ int resolve_threads(int32_t t) {
 // CSR pattern of the strictly lower triangle of P A P^T: row i lists the
 // columns j < i with a structural entry. Also returns the CSC of the lower
 // triangle with values (diagonal included) for numeric assembly.
+// With `amap`, also records for every entry k of A its position in the
+// lower CSC (-1 for entries above the diagonal).
 void permuted_lower(const Csc& A, const std::vector<int32_t>& pinv, std::vector<int32_t>& rptr,
                     std::vector<int32_t>& rcol, std::vector<int32_t>& cptr,
-                    std::vector<int32_t>& crow, std::vector<double>& cval) {
+                    std::vector<int32_t>& crow, std::vector<double>& cval,
+                    std::vector<int32_t>* amap = nullptr) {
     const int32_t n = A.n;
+    if (amap) amap->assign(A.rowidx.size(), -1);
     rptr.assign((size_t)n + 1, 0);
     cptr.assign((size_t)n + 1, 0);
     for (int32_t c = 0; c < n; ++c)
@@ -78,6 +83,7 @@ void permuted_lower(const Csc& A, const std::vector<int32_t>& pinv, std::vector<
             int32_t d = cn[lo]++;
             crow[d] = hi;
             cval[d] = A.vals[k];
+            if (amap) (*amap)[k] = d;
             if (hi != lo) rcol[rn[hi]++] = lo;
         }
 }
@@ -191,7 +197,8 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
         for (int32_t k = 0; k < n; ++k) F.perm[k] = perm0[post[k]];
         for (int32_t k = 0; k < n; ++k) pinv[F.perm[k]] = k;
     }
-    permuted_lower(A, pinv, rptr, rcol, cptr, crow, cval);
+    auto sym = std::make_shared<SymbolicCache>();
+    permuted_lower(A, pinv, rptr, rcol, cptr, crow, cval, &sym->amap);
     parent = etree(n, rptr, rcol);
     F.parent = parent;
 
@@ -299,6 +306,35 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     }
     std::vector<int32_t>().swap(srows);
 
+    // ---- the symbolic analysis kept for refactorisations ---------------
+    sym->n = n;
+    sym->a_colptr = A.colptr;
+    sym->a_rowidx = A.rowidx;
+    sym->cptr = std::move(cptr);
+    sym->crow = std::move(crow);
+    sym->sn_parent = std::move(sn_parent);
+    sym->child_ptr = std::move(child_ptr);
+    sym->children = std::move(children);
+    F.sym = sym;
+    return numeric_factor(F, *sym, cval, threads, F.vals, F.flops, err);
+}
+
+Status numeric_factor(const Factor& F, const SymbolicCache& S, const std::vector<double>& cval, int32_t nthreads,
+                      std::vector<double>& vals_out, double& flops_out, std::string& err) {
+    const int32_t n = F.n;
+    const int threads = resolve_threads(nthreads);
+    const int32_t nsn = (int32_t)F.sn_start.size() - 1;
+    const int64_t total = F.nnz();
+    const std::vector<int32_t>& cptr = S.cptr;
+    const std::vector<int32_t>& crow = S.crow;
+    const std::vector<int32_t>& sn_parent = S.sn_parent;
+    const std::vector<int32_t>& child_ptr = S.child_ptr;
+    const std::vector<int32_t>& children = S.children;
+    if (n == 0) {
+        vals_out.clear();
+        flops_out = 0.0;
+        return ST_OK;
+    }
     // ---- multifrontal numeric factorisation -----------------------------
     // Supernodes whose subtree holds more than 1/(4 threads) of the flops (a
     // set closed towards the roots) are factorised last, one after the other,
@@ -308,7 +344,7 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     // dimension Fsz) is the update. A parent adds its children's updates in
     // reverse child order, the order of a serial postorder stack, so results
     // do not depend on the thread count.
-    F.vals.assign((size_t)total, 0.0);
+    vals_out.assign((size_t)total, 0.0);
     std::vector<double> sn_flops((size_t)nsn), sub_flops((size_t)nsn);
     std::vector<int32_t> first((size_t)nsn);  // first supernode of each subtree (postorder: contiguous)
     double total_flops = 0.0;
@@ -426,7 +462,7 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
             dense::gemm_nt_sub(m, m, w, fr + w, Fsz, fr + w, Fsz, fr + w + w * Fsz, Fsz, true, dt);
         }
         if (ok) {  // store the columns of L
-            double* vals = F.vals.data();
+            double* vals = vals_out.data();
             const int32_t* cp = F.colptr.data();
 #pragma omp parallel for num_threads(dt) schedule(static) if (dt > 1 && w * Fsz >= kParCols * kParCols)
             for (int64_t j = 0; j < w; ++j) {
@@ -485,8 +521,67 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     }
     double flops = 0.0;
     for (int32_t s = 0; s < nsn; ++s) flops += sn_flops[s];
-    F.flops = flops;
+    flops_out = flops;
     return ST_OK;
+}
+
+void record_input(Factor& F, int64_t nnz, const int32_t* ii, const int32_t* jj, int32_t fmt) {
+    if (!F.sym) return;
+    SymbolicCache& S = *F.sym;
+    const int32_t n = F.n;
+    const size_t ni = fmt == FMT_COO ? (size_t)nnz : (size_t)n + 1;
+    S.fmt = fmt;
+    S.in_i.assign(ii, ii + ni);
+    S.in_j.assign(jj, jj + nnz);
+    S.inmap.resize((size_t)nnz);
+    // entry e of the input sits at (row, col) of A; its CSC position is found
+    // in the (sorted, duplicate-free) column
+    auto place = [&](int64_t e, int32_t r, int32_t c) {
+        const int32_t* b0 = S.a_rowidx.data() + S.a_colptr[c];
+        const int32_t* b1 = S.a_rowidx.data() + S.a_colptr[c + 1];
+        S.inmap[e] = (int32_t)(std::lower_bound(b0, b1, r) - S.a_rowidx.data());
+    };
+    if (fmt == FMT_COO) {
+        for (int64_t e = 0; e < nnz; ++e) place(e, ii[e], jj[e]);
+    } else {
+        for (int32_t o = 0; o < n; ++o)  // o owns entries ii[o]..ii[o+1]: a row (CSR) or a column (CSC)
+            for (int32_t e = ii[o]; e < ii[o + 1]; ++e) {
+                if (fmt == FMT_CSR) place(e, o, jj[e]);
+                else place(e, jj[e], o);
+            }
+    }
+}
+
+bool refactor_cached(const Factor& F, int64_t nnz, const int32_t* ii, const int32_t* jj, const double* x,
+                     int32_t fmt, int32_t threads, Csc& A, std::vector<double>& vals_out, double& flops_out,
+                     Status& st, std::string& err) {
+    if (!F.sym || F.sym->fmt < 0 || fmt != F.sym->fmt) return false;
+    const SymbolicCache& S = *F.sym;
+    const int32_t n = F.n;
+    const size_t ni = fmt == FMT_COO ? (size_t)nnz : (size_t)n + 1;
+    if (S.in_i.size() != ni || S.in_j.size() != (size_t)nnz) return false;
+    if (ni && std::memcmp(ii, S.in_i.data(), ni * sizeof(int32_t)) != 0) return false;
+    if (nnz && std::memcmp(jj, S.in_j.data(), (size_t)nnz * sizeof(int32_t)) != 0) return false;
+    // duplicates summed in input order, from the first one on (as build_csc)
+    A.n = n;
+    A.colptr = S.a_colptr;
+    A.rowidx = S.a_rowidx;
+    A.vals.assign(S.a_rowidx.size(), 0.0);
+    std::vector<char> seen(S.a_rowidx.size(), 0);
+    for (int64_t e = 0; e < nnz; ++e) {
+        const int32_t p = S.inmap[e];
+        if (seen[p]) {
+            A.vals[p] += x[e];
+        } else {
+            A.vals[p] = x[e];
+            seen[p] = 1;
+        }
+    }
+    std::vector<double> cval((size_t)S.cptr[n], 0.0);
+    for (size_t k = 0; k < S.amap.size(); ++k)
+        if (S.amap[k] >= 0) cval[(size_t)S.amap[k]] = A.vals[k];
+    st = numeric_factor(F, S, cval, threads, vals_out, flops_out, err);
+    return true;
 }
 
 }  // namespace gbchol

@@ -8,6 +8,7 @@
 // the diagonal first in each column (cholmod_factor_to_sparse).
 #pragma once
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -54,6 +55,21 @@ void symmetric_from_lower(const Csc& A, Csc& S);
 std::vector<int32_t> nested_dissection(int32_t n, const std::vector<int32_t>& xadj,
                                        const std::vector<int32_t>& adj);
 
+// Symbolic analysis of a factorisation, kept so that new values on the same
+// sparsity pattern are factorised without ordering, symbolic factorisation or
+// input sorting again (numeric refactorisation).
+struct SymbolicCache {
+    int32_t n = 0;
+    std::vector<int32_t> a_colptr, a_rowidx;  // A's CSC pattern (sorted, duplicates merged)
+    std::vector<int32_t> amap;                // A's CSC entry -> position in the permuted lower CSC (-1: upper)
+    std::vector<int32_t> cptr, crow;          // lower CSC of P A P^T (pattern)
+    std::vector<int32_t> sn_parent, child_ptr, children;  // supernodal elimination tree
+    // the raw input the analysis was made for (empty if not recorded):
+    int32_t fmt = -1;
+    std::vector<int32_t> in_i, in_j;  // index arrays as given
+    std::vector<int32_t> inmap;       // input entry -> position in A's CSC
+};
+
 struct Factor {
     int32_t n = 0;
     std::vector<int32_t> perm;    // perm[k] = original row at position k
@@ -63,6 +79,7 @@ struct Factor {
     std::vector<int32_t> parent;  // elimination tree of P A P^T (-1 = root)
     std::vector<int32_t> sn_start;// fundamental supernodes: columns [sn_start[s], sn_start[s+1])
     double flops = 0.0;           // numeric factorisation flop count
+    std::shared_ptr<SymbolicCache> sym;  // set by factorize()
     int64_t nnz() const { return (int64_t)rowidx.size(); }
 };
 
@@ -78,6 +95,28 @@ struct FactorOptions {
 // Numeric: supernodal multifrontal with dense blocked kernels. Returns
 // ST_NOT_POSDEF on a non-positive pivot (src/cholesky_solver.cpp:241-242).
 Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string& err);
+
+// Numeric phase of factorize on its symbolic analysis: cval holds the values
+// of the lower CSC of P A P^T (pattern S.cptr / S.crow); the values of L go to
+// vals_out (F's pattern). ST_NOT_POSDEF on a non-positive pivot.
+Status numeric_factor(const Factor& F, const SymbolicCache& S, const std::vector<double>& cval, int32_t threads,
+                      std::vector<double>& vals_out, double& flops_out, std::string& err);
+
+// Records in F's symbolic analysis the raw input it was made from (index
+// arrays and format, as given to build_csc), so that refactor_cached can
+// recognise the same input pattern.
+void record_input(Factor& F, int64_t nnz, const int32_t* ii, const int32_t* jj, int32_t fmt);
+
+// Numeric refactorisation of F for new values x of the recorded input
+// pattern: the duplicates are summed in input order exactly as build_csc does,
+// the values are placed by the cached maps and factorised by numeric_factor.
+// Returns false (nothing done) when F has no recorded input or the given
+// index arrays / format differ from it. On true, `st` is the numeric status,
+// A the matrix with the new values (CSC, as build_csc gives it) and vals_out /
+// flops_out the new factor values.
+bool refactor_cached(const Factor& F, int64_t nnz, const int32_t* ii, const int32_t* jj, const double* x,
+                     int32_t fmt, int32_t threads, Csc& A, std::vector<double>& vals_out, double& flops_out,
+                     Status& st, std::string& err);
 
 // Transpose of a CSC pattern+values (gives the CSR of L from its CSC); with
 // empty `vals`, of the pattern alone. Indices ascend within each output row.

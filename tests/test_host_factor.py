@@ -173,3 +173,55 @@ def test_factor_refactorize(gblib):
             assert np.array_equal(_export(gblib, f, n)[3], vals)
     finally:
         gblib.gbchol_factor_free(f)
+
+
+@pytest.mark.parametrize("fmt", ["COO", "CSR", "CSC"])
+def test_refactorize_cached_symbolic_bit_identical(gblib, fmt):
+    """New values with the very index arrays the factor was made from take the
+    cached symbolic analysis (no input sort, ordering or symbolic step); the
+    result is bit-identical to a fresh factorisation of the new values and to
+    the full refactorisation path (reached here by giving the same matrix in
+    another format). Duplicate COO entries are summed in input order."""
+    import scipy.sparse as sp
+    n, faces, _ = workloads.icosphere(3)
+    v1, idx = workloads.laplacian_coo(n, faces, 2.0)   # duplicate diagonal entries
+    v2, _ = workloads.laplacian_coo(n, faces, 7.5)
+    if fmt == "COO":
+        a1 = (idx[0], idx[1], v1)
+        a2 = (idx[0], idx[1], v2)
+        other = sp.csr_matrix((v2, (idx[0], idx[1])), shape=(n, n))
+        other = (other.indptr, other.indices, other.data, 1)
+        code = 2
+    else:
+        mk = sp.csr_matrix if fmt == "CSR" else sp.csc_matrix
+        m1 = mk((v1, (idx[0], idx[1])), shape=(n, n))
+        m2 = mk((v2, (idx[0], idx[1])), shape=(n, n))
+        assert np.array_equal(m1.indices, m2.indices)
+        a1 = (m1.indptr, m1.indices, m1.data)
+        a2 = (m2.indptr, m2.indices, m2.data)
+        other = (idx[0], idx[1], v2, 2)
+        code = 1 if fmt == "CSR" else 0
+    arr = [np.ascontiguousarray(a, t) for a, t in zip(a1, (np.int32, np.int32, np.float64))]
+    new = [np.ascontiguousarray(a, t) for a, t in zip(a2, (np.int32, np.int32, np.float64))]
+    f = C.c_void_p()
+    _ffi.check(gblib.gbchol_factorize(n, len(arr[2]), arr[0].ctypes.data, arr[1].ctypes.data, arr[2].ctypes.data,
+                                      code, 2, C.byref(f)))
+    g = C.c_void_p()
+    _ffi.check(gblib.gbchol_factorize(n, len(arr[2]), arr[0].ctypes.data, arr[1].ctypes.data, arr[2].ctypes.data,
+                                      code, 2, C.byref(g)))
+    try:
+        _ffi.check(gblib.gbchol_factor_refactorize(f, len(new[2]), new[0].ctypes.data, new[1].ctypes.data,
+                                                   new[2].ctypes.data, code, 2))
+        cached = _export(gblib, f, n)
+        fresh = factorize(gblib, n, new[0], new[1], new[2], code)
+        assert np.array_equal(cached[0], fresh[0]) and np.array_equal(cached[2], fresh[2])
+        assert np.array_equal(cached[3], fresh[3])
+        oi, oj, ox, ocode = (np.ascontiguousarray(other[0], np.int32), np.ascontiguousarray(other[1], np.int32),
+                             np.ascontiguousarray(other[2], np.float64), other[3])
+        _ffi.check(gblib.gbchol_factor_refactorize(g, len(ox), oi.ctypes.data, oj.ctypes.data, ox.ctypes.data,
+                                                   ocode, 2))
+        full = _export(gblib, g, n)
+        assert np.array_equal(cached[3], full[3])
+    finally:
+        gblib.gbchol_factor_free(f)
+        gblib.gbchol_factor_free(g)
