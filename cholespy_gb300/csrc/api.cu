@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -526,10 +527,7 @@ int gbchol_factor_solve(gbchol_factor_handle f, int32_t precision, int32_t nrhs,
     if (threads < 0) return fail(GBCHOL_EINVAL, "threads must be non-negative.");
     if (f->F.n > 0 && nrhs > 0 && (!b || !x)) return fail(GBCHOL_EINVAL, "Null b or x.");
     try {
-        if (!f->cpu_ready) {
-            cpu_plan(f->F, f->cpu, threads);
-            f->cpu_ready = true;
-        }
+        std::call_once(f->cpu_once, [&] { cpu_plan(f->F, f->cpu, threads); });
         cpu_solve(f->F, f->cpu, precision, nrhs, b, x, threads);
     } catch (const std::bad_alloc&) {
         return fail(GBCHOL_ENOMEM, "Out of host memory.");

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -106,7 +107,7 @@ using namespace gbchol;
 struct gbchol_host_factor {
     Factor F;
     CpuSolvePlan cpu;         // host solve structure, built at the first host solve
-    bool cpu_ready = false;
+    std::once_flag cpu_once;  // (solves only read the factor and the plan: they may run concurrently)
 };
 
 struct gbchol_solver {

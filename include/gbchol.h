@@ -131,6 +131,8 @@ int gbchol_factor_refactorize(gbchol_factor_handle f, int64_t nnz, const int32_t
  * alias. threads = 0 uses every host core; the result does not depend on the
  * thread count. The first call builds the solve's structure (kept until the
  * factor is freed; a refactorisation keeps it). Blocks until x is written.
+ * Solves only read the factor, so several threads may solve with one factor
+ * at once; a refactorisation must not overlap them.
  * This path never runs for CUDA arrays: those go through gbchol_solve.
  */
 int gbchol_factor_solve(gbchol_factor_handle f, int32_t precision, int32_t nrhs, const void* b, void* x,

@@ -275,3 +275,33 @@ def test_host_solve_structures(gblib, case):
             assert np.array_equal(x, _host_solve(gblib, f, b, 1, 1))
     finally:
         gblib.gbchol_factor_free(f)
+
+
+def test_cpu_solver_concurrent_solves(gblib):
+    """Solves of one CPU solver from several threads at once (the first ones
+    included, which build the host solve's structure) give the results of
+    sequential solves: a solve only reads the factor."""
+    import threading
+    from cholespy_gb300 import CholeskySolverD, MatrixType
+    n, vals, idx = 18 ** 3, *workloads.grid3d_coo(18, 1e-3)
+    s = CholeskySolverD(n, idx[0], idx[1], vals, MatrixType.COO)
+    bs = [np.random.default_rng(k).standard_normal((n, 1 + 3 * k)) for k in range(6)]
+    xs = [np.zeros_like(b) for b in bs]
+    errs = []
+
+    def work(k):
+        try:
+            s.solve(bs[k], xs[k])
+        except Exception as e:  # pragma: no cover - reported below
+            errs.append(e)
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(len(bs))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errs
+    for b, x in zip(bs, xs):
+        y = np.zeros_like(b)
+        s.solve(b, y)
+        assert np.array_equal(x, y)
