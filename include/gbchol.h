@@ -115,6 +115,8 @@ int gbchol_factor_free(gbchol_factor_handle f);
  * factor's ordering is reused (no new ordering); GBCHOL_EINVAL if the new
  * pattern gives another factor pattern, GBCHOL_ENOTPOSDEF if the new matrix
  * is not positive definite (the factor keeps its old values on any error).
+ * With the very index arrays and format the factor was made from, the kept
+ * symbolic analysis is reused and only the numeric phase runs (same result).
  * No counterpart in the reference (it refactors through a new solver).
  */
 int gbchol_factor_refactorize(gbchol_factor_handle f, int64_t nnz, const int32_t* ii, const int32_t* jj,
@@ -294,8 +296,9 @@ int gbchol_autotune(gbchol_handle h, int32_t precision, int32_t nrhs, const int3
  * Numeric refactorisation of a solver: new values of the same sparsity
  * pattern (same n and input format as at creation). Keeps the ordering, the
  * symbolic factor and the level analysis; recomputes the numeric factor on the
- * host (reusing the ordering) and uploads it with the solve plan. Errors as
- * gbchol_factor_refactorize; the solver keeps its old factor on any error.
+ * host (reusing the ordering, and the whole symbolic analysis when the index
+ * arrays are those of the constructor) and uploads it with the solve plan.
+ * Errors as gbchol_factor_refactorize; the solver keeps its old factor on any error.
  * Synchronises the device; batches built from this solver must be built
  * again. No counterpart in the reference, whose users build a new solver per
  * set of values.
