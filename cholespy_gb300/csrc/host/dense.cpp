@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <memory>
 #include <vector>
 
 #ifdef _OPENMP
@@ -112,7 +113,9 @@ void gemm_small(int64_t m, int64_t n, int64_t k, const double* A, int64_t lda, c
 void gemm_nt_sub(int64_t m, int64_t n, int64_t k, const double* A, int64_t lda, const double* B,
                  int64_t ldb, double* C, int64_t ldc, bool lower_only, int threads) {
     if (m <= 0 || n <= 0 || k <= 0) return;
-    if (m * n * k <= 32 * 32 * 32) {
+    // small products, and thin ones (k <= 8: the rank-k update of a narrow
+    // supernode), are column updates; the choice depends on the sizes only
+    if (k <= 8 || m * n * k <= 32 * 32 * 32) {
         gemm_small(m, n, k, A, lda, B, ldb, C, ldc, lower_only);
         return;
     }
@@ -132,13 +135,17 @@ void gemm_nt_sub(int64_t m, int64_t n, int64_t k, const double* A, int64_t lda, 
     nt = std::max(1, std::min<int>(nt, (int)tiles.size()));
 #pragma omp parallel num_threads(nt) if (nt > 1)
     {
-        std::vector<double> Ap((size_t)(MC * KC)), Bp((size_t)(NC * KC));
+        // packing buffers kept per thread (packing writes every entry it uses)
+        static thread_local std::unique_ptr<double[]> Ap, Bp;
+        if (!Ap) {
+            Ap.reset(new double[(size_t)(MC * KC)]);
+            Bp.reset(new double[(size_t)(NC * KC)]);
+        }
 #pragma omp for schedule(dynamic, 1)
         for (int64_t t = 0; t < (int64_t)tiles.size(); ++t) {
             int64_t i0 = tiles[t].i0, j0 = tiles[t].j0;
             int64_t mc = std::min(MC, m - i0), nc = std::min(NC, n - j0);
-            gemm_tile(mc, nc, k, A + i0, lda, B + j0, ldb, C + i0 + j0 * ldc, ldc, Ap.data(),
-                      Bp.data());
+            gemm_tile(mc, nc, k, A + i0, lda, B + j0, ldb, C + i0 + j0 * ldc, ldc, Ap.get(), Bp.get());
         }
     }
 }
