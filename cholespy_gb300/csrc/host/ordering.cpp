@@ -14,6 +14,12 @@
 //     (bit-set elimination graph).
 // Separator vertices are numbered after the two halves they split, so the
 // resulting permutation puts the top separator last.
+//
+// Every piece is a range [lo, hi) of the permutation under construction and
+// touches only its own vertices (BFS queue in queue[lo, hi), per-vertex
+// level/side marks; a vertex belongs to the piece whose tag it carries), so
+// the two pieces of a split are ordered as parallel tasks and the result is
+// the same whatever the order in which pieces are processed.
 #include "host.h"
 
 #include <algorithm>
@@ -28,18 +34,21 @@ struct NDState {
     const std::vector<int32_t>& xadj;
     const std::vector<int32_t>& adj;
     std::vector<int32_t> verts;   // permutation under construction
-    std::vector<int32_t> tag;     // task label of each vertex
+    std::vector<int32_t> tag;     // piece label of each vertex (read across pieces: atomic access)
     std::vector<int32_t> level;   // BFS level scratch
-    std::vector<int32_t> queue;
+    std::vector<int32_t> queue;   // BFS queue: piece [lo, hi) uses queue[lo, hi)
     std::vector<int32_t> side;    // 0 = A, 1 = B, 2 = separator (scratch)
-    int32_t next_tag = 1;
+    int32_t next_tag = 1;         // atomic
+
+    int32_t tag_of(int32_t v) const { return __atomic_load_n(&tag[v], __ATOMIC_RELAXED); }
+    void set_tag(int32_t v, int32_t t) { __atomic_store_n(&tag[v], t, __ATOMIC_RELAXED); }
 
     NDState(int32_t n_, const std::vector<int32_t>& xa, const std::vector<int32_t>& ad)
         : n(n_), xadj(xa), adj(ad), verts(n_), tag(n_, 0), level(n_, -1), queue(n_), side(n_, 0) {}
 
     // BFS from `root` over vertices with tag t. Returns the number of
     // vertices reached; fills queue[0..count) in BFS order and level[].
-    int32_t bfs(int32_t root, int32_t t, int32_t* depth_out) {
+    int32_t bfs(int32_t* queue, int32_t root, int32_t t, int32_t* depth_out) {
         int32_t head = 0, tail = 0;
         queue[tail++] = root;
         level[root] = 0;
@@ -50,7 +59,7 @@ struct NDState {
             depth = lv;
             for (int32_t k = xadj[v]; k < xadj[v + 1]; ++k) {
                 int32_t u = adj[k];
-                if (tag[u] == t && level[u] < 0) {
+                if (tag_of(u) == t && level[u] < 0) {
                     level[u] = lv + 1;
                     queue[tail++] = u;
                 }
@@ -59,12 +68,12 @@ struct NDState {
         if (depth_out) *depth_out = depth;
         return tail;
     }
-    void clear_levels(int32_t count) {
+    void clear_levels(const int32_t* queue, int32_t count) {
         for (int32_t i = 0; i < count; ++i) level[queue[i]] = -1;
     }
     int32_t degree_in(int32_t v, int32_t t) const {
         int32_t d = 0;
-        for (int32_t k = xadj[v]; k < xadj[v + 1]; ++k) d += (tag[adj[k]] == t);
+        for (int32_t k = xadj[v]; k < xadj[v + 1]; ++k) d += (tag_of(adj[k]) == t);
         return d;
     }
 
@@ -84,7 +93,7 @@ struct NDState {
             int32_t v = local[i];
             for (int32_t k = xadj[v]; k < xadj[v + 1]; ++k) {
                 int32_t u = adj[k];
-                if (tag[u] == t) b |= (uint64_t)1 << level[u];
+                if (tag_of(u) == t) b |= (uint64_t)1 << level[u];
             }
             nb[i] = b;
         }
@@ -109,13 +118,13 @@ struct NDState {
     }
 
     // Finds a pseudo-peripheral vertex of the piece tagged t containing `start`.
-    int32_t pseudo_peripheral(int32_t start, int32_t t, int32_t* count_out) {
+    int32_t pseudo_peripheral(int32_t* queue, int32_t start, int32_t t, int32_t* count_out) {
         int32_t root = start, depth = -1;
         int32_t count = 0;
         for (int it = 0; it < 8; ++it) {
             int32_t d;
-            count = bfs(root, t, &d);
-            if (d <= depth) { clear_levels(count); break; }
+            count = bfs(queue, root, t, &d);
+            if (d <= depth) { clear_levels(queue, count); break; }
             depth = d;
             // vertex of minimum degree in the last level
             int32_t cand = root, cd = 1 << 30;
@@ -123,7 +132,7 @@ struct NDState {
                 int32_t dv = degree_in(queue[i], t);
                 if (dv < cd) { cd = dv; cand = queue[i]; }
             }
-            clear_levels(count);
+            clear_levels(queue, count);
             if (cand == root) break;
             root = cand;
         }
@@ -131,33 +140,47 @@ struct NDState {
         return root;
     }
 
+    void piece(int32_t lo, int32_t hi);
     void run();
 };
 
-struct Task { int32_t lo, hi; };
+// Pieces at least this large are handed to other threads.
+constexpr int32_t kTaskMin = 4096;
 
 void NDState::run() {
     for (int32_t i = 0; i < n; ++i) verts[i] = i;
-    std::vector<Task> stack;
-    stack.push_back({0, n});
+#pragma omp parallel if (n >= 2 * kTaskMin)
+#pragma omp single
+    piece(0, n);
+}
+
+// Orders piece [lo, hi) of verts (and, recursively, its sub-pieces).
+void NDState::piece(int32_t lo, int32_t hi) {
+    auto sub = [&](int32_t a, int32_t b) {
+        if (b - a >= kTaskMin) {
+#pragma omp task default(shared) firstprivate(a, b)
+            piece(a, b);
+        } else {
+            piece(a, b);
+        }
+    };
     std::vector<int32_t> buf;
-    while (!stack.empty()) {
-        Task tk = stack.back();
-        stack.pop_back();
-        const int32_t lo = tk.lo, hi = tk.hi, m = hi - lo;
-        if (m <= 0) continue;
-        const int32_t t = next_tag++;
-        for (int32_t i = lo; i < hi; ++i) tag[verts[i]] = t;
+    int32_t* queue = this->queue.data() + lo;  // room for the piece's m vertices
+    {
+        const int32_t m = hi - lo;
+        if (m <= 0) return;
+        const int32_t t = __atomic_fetch_add(&next_tag, 1, __ATOMIC_RELAXED);
+        for (int32_t i = lo; i < hi; ++i) set_tag(verts[i], t);
         if (m <= 64) {
             order_small(lo, hi, t);
-            continue;
+            return;
         }
         // Split off connected components.
-        int32_t cnt = bfs(verts[lo], t, nullptr);
+        int32_t cnt = bfs(queue, verts[lo], t, nullptr);
         if (cnt < m) {
-            // The reached component goes first, the rest becomes another task.
-            buf.assign(queue.begin(), queue.begin() + cnt);
-            clear_levels(cnt);
+            // The reached component goes first, the rest becomes another piece.
+            buf.assign(queue, queue + cnt);
+            clear_levels(queue, cnt);
             for (int32_t v : buf) side[v] = 1;
             int32_t w = lo;
             std::vector<int32_t> rest;
@@ -168,16 +191,16 @@ void NDState::run() {
             }
             for (int32_t v : rest) verts[w++] = v;
             for (int32_t v : buf) side[v] = 0;
-            stack.push_back({lo + cnt, hi});
-            stack.push_back({lo, lo + cnt});
-            continue;
+            sub(lo + cnt, hi);
+            sub(lo, lo + cnt);
+            return;
         }
-        clear_levels(cnt);
+        clear_levels(queue, cnt);
         // Level structure from a pseudo-peripheral vertex.
         int32_t count;
-        int32_t root = pseudo_peripheral(verts[lo], t, &count);
+        int32_t root = pseudo_peripheral(queue, verts[lo], t, &count);
         int32_t depth;
-        count = bfs(root, t, &depth);
+        count = bfs(queue, root, t, &depth);
         std::vector<int32_t> lvl_size((size_t)depth + 2, 0);
         for (int32_t i = 0; i < count; ++i) lvl_size[level[queue[i]]]++;
         int32_t split = -1;
@@ -208,16 +231,16 @@ void NDState::run() {
             // Too shallow to split (near-clique): minimum-degree-free fallback,
             // keep BFS order.
             for (int32_t i = 0; i < count; ++i) verts[lo + i] = queue[i];
-            clear_levels(count);
+            clear_levels(queue, count);
             // order in chunks of 64 is meaningless for cliques; keep as is
-            continue;
+            return;
         }
         for (int32_t i = 0; i < count; ++i) {
             int32_t v = queue[i];
             int32_t l = level[v];
             side[v] = l < split ? 0 : (l > split ? 1 : 2);
         }
-        clear_levels(count);
+        clear_levels(queue, count);
         // Trim the separator: a separator vertex with no neighbour on one side
         // can join the other side.
         for (int pass = 0; pass < 2; ++pass) {
@@ -227,7 +250,7 @@ void NDState::run() {
                 bool hasA = false, hasB = false;
                 for (int32_t k = xadj[v]; k < xadj[v + 1]; ++k) {
                     int32_t u = adj[k];
-                    if (tag[u] != t) continue;
+                    if (tag_of(u) != t) continue;
                     hasA |= side[u] == 0;
                     hasB |= side[u] == 1;
                 }
@@ -251,10 +274,10 @@ void NDState::run() {
         for (int32_t i = lo; i < hi; ++i) side[verts[i]] = 0;
         if (ns == 0 || na == 0 || nb_ == 0) {
             // degenerate split: order the piece as is (tiny pieces handled above)
-            if (na + nb_ == 0) continue;
+            if (na + nb_ == 0) return;
         }
-        stack.push_back({lo + na, lo + na + nb_});
-        stack.push_back({lo, lo + na});
+        sub(lo + na, lo + na + nb_);
+        sub(lo, lo + na);
         (void)ns;
     }
 }
