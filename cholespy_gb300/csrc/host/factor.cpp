@@ -203,16 +203,35 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     F.parent = parent;
 
     // ---- column counts of L by row subtrees -----------------------------
-    std::vector<int32_t> mark((size_t)n, -1);
+    // Rows are independent: each thread walks its rows' subtrees with its own
+    // marks and counts, and the integer counts are summed.
     std::vector<int64_t> cnt((size_t)n, 1);  // diagonal
-    for (int32_t i = 0; i < n; ++i) {
-        mark[i] = i;
-        for (int32_t k = rptr[i]; k < rptr[i + 1]; ++k) {
-            for (int32_t r = rcol[k]; mark[r] != i; r = parent[r]) {
-                cnt[r]++;
-                mark[r] = i;
+    {
+        const int nt = (threads > 1 && n >= 32768) ? threads : 1;
+        std::vector<std::vector<int32_t>> part((size_t)nt);
+#pragma omp parallel num_threads(nt) if (nt > 1)
+        {
+#ifdef _OPENMP
+            std::vector<int32_t>& pc = part[(size_t)omp_get_thread_num()];
+#else
+            std::vector<int32_t>& pc = part[0];
+#endif
+            pc.assign((size_t)n, 0);
+            std::vector<int32_t> mk((size_t)n, -1);
+#pragma omp for schedule(dynamic, 1024)
+            for (int32_t i = 0; i < n; ++i) {
+                mk[i] = i;
+                for (int32_t k = rptr[i]; k < rptr[i + 1]; ++k) {
+                    for (int32_t r = rcol[k]; mk[r] != i; r = parent[r]) {
+                        pc[r]++;
+                        mk[r] = i;
+                    }
+                }
             }
         }
+#pragma omp parallel for num_threads(nt) schedule(static) if (nt > 1)
+        for (int32_t j = 0; j < n; ++j)
+            for (int t = 0; t < nt; ++t) cnt[j] += part[(size_t)t][j];
     }
     int64_t total = 0;
     for (int32_t j = 0; j < n; ++j) total += cnt[j];
@@ -266,19 +285,42 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     for (int32_t s = 0; s < nsn; ++s) sptr[s + 1] = sptr[s] + cnt[F.sn_start[s]];
     std::vector<int32_t> srows((size_t)sptr[nsn]);
     {
-        std::fill(mark.begin(), mark.end(), -1);
+        // Subtrees below a size cut are independent (a supernode needs only
+        // its children's lists): they are built as parallel tasks, each with
+        // its own marks, then the supernodes above the cut in order.
+        std::vector<int64_t> sub((size_t)nsn);
+        std::vector<int32_t> sfirst((size_t)nsn);
         for (int32_t s = 0; s < nsn; ++s) {
+            sub[s] = sptr[s + 1] - sptr[s];
+            sfirst[s] = s;
+        }
+        for (int32_t s = 0; s < nsn; ++s)
+            if (sn_parent[s] >= 0) {
+                sub[sn_parent[s]] += sub[s];
+                sfirst[sn_parent[s]] = std::min(sfirst[sn_parent[s]], sfirst[s]);
+            }
+        const int64_t cut = threads > 1 ? std::max<int64_t>(sptr[nsn] / (8 * threads), 1 << 16) : -1;
+        std::vector<int32_t> roots;
+        std::vector<char> above((size_t)nsn, 0);
+        for (int32_t s = 0; s < nsn; ++s) {
+            above[s] = sub[s] > cut;
+            if (sub[s] <= cut && (sn_parent[s] < 0 || sub[sn_parent[s]] > cut)) roots.push_back(s);
+        }
+        int bad = 0;
+        // rows(s): its columns, A's rows below them, its children's rows below
+        // their own columns; the rows after the columns sorted
+        auto build = [&](int32_t s, std::vector<int32_t>& mk) {
             const int32_t f = F.sn_start[s], l1 = F.sn_start[s + 1];
             int32_t* out = srows.data() + sptr[s];
             int64_t len = 0;
             const int64_t cap = sptr[s + 1] - sptr[s];
             for (int32_t j = f; j < l1; ++j) {
                 out[len++] = j;
-                mark[j] = s;
+                mk[j] = s;
             }
             auto add = [&](int32_t r) {
-                if (mark[r] == s) return;
-                mark[r] = s;
+                if (mk[r] == s) return;
+                mk[r] = s;
                 if (len < cap) out[len] = r;
                 ++len;
             };
@@ -289,11 +331,28 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
                 const int32_t cw = F.sn_start[c + 1] - F.sn_start[c];
                 for (int64_t k = sptr[c] + cw; k < sptr[c + 1]; ++k) add(srows[k]);
             }
-            if (len != cap) {
-                err = "Internal error: supernodal pattern does not match the column counts.";
-                return ST_INTERNAL;
-            }
+            if (len != cap) return false;
             std::sort(out + (l1 - f), out + len);
+            return true;
+        };
+        const int nt = threads > 1 && roots.size() > 1 ? threads : 1;
+#pragma omp parallel num_threads(nt) if (nt > 1)
+        {
+            std::vector<int32_t> mk((size_t)n, -1);
+#pragma omp for schedule(dynamic, 1)
+            for (int64_t q = 0; q < (int64_t)roots.size(); ++q)
+                for (int32_t s = sfirst[roots[q]]; s <= roots[q]; ++s)
+                    if (!build(s, mk)) {
+#pragma omp atomic write
+                        bad = 1;
+                    }
+        }
+        std::vector<int32_t> mk((size_t)n, -1);
+        for (int32_t s = 0; s < nsn && !bad; ++s)
+            if (above[s] && !build(s, mk)) bad = 1;
+        if (bad) {
+            err = "Internal error: supernodal pattern does not match the column counts.";
+            return ST_INTERNAL;
         }
     }
     F.rowidx.resize((size_t)total);
