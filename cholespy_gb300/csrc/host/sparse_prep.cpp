@@ -7,6 +7,7 @@
 #include "host.h"
 
 #include <algorithm>
+#include <cstring>
 #include <numeric>
 
 #ifdef _OPENMP
@@ -17,60 +18,136 @@ namespace gbchol {
 
 namespace {
 
+int prep_threads(int64_t nnz) {
+#ifdef _OPENMP
+    if (nnz >= (int64_t)1 << 18) return std::max(1, std::min(omp_get_max_threads(), 64));
+#endif
+    (void)nnz;
+    return 1;
+}
+
 // Counting-sort placement of (row, col, val) triples into columns, keeping
 // input order inside a column. `row_of(e)` / `col_of(e)` give the entry e.
+// Large inputs: contiguous chunks of entries count per column, and chunk t's
+// entries of a column go after those of chunks < t, so the placement (and
+// everything after it) is the same for any thread count.
 template <class RowOf, class ColOf>
 void place_by_column(int32_t n, int64_t nnz, RowOf row_of, ColOf col_of, const double* x,
                      Csc& out) {
     out.n = n;
     out.colptr.assign((size_t)n + 1, 0);
-    for (int64_t e = 0; e < nnz; ++e) out.colptr[(size_t)col_of(e) + 1]++;
-    for (int32_t c = 0; c < n; ++c) out.colptr[c + 1] += out.colptr[c];
     out.rowidx.resize((size_t)nnz);
     out.vals.resize((size_t)nnz);
-    std::vector<int32_t> next(out.colptr.begin(), out.colptr.end() - 1);
-    for (int64_t e = 0; e < nnz; ++e) {
-        int32_t c = col_of(e);
-        int32_t dst = next[c]++;
-        out.rowidx[dst] = row_of(e);
-        out.vals[dst] = x[e];
+    const int nt = prep_threads(nnz);
+    if (nt == 1) {
+        for (int64_t e = 0; e < nnz; ++e) out.colptr[(size_t)col_of(e) + 1]++;
+        for (int32_t c = 0; c < n; ++c) out.colptr[c + 1] += out.colptr[c];
+        std::vector<int32_t> next(out.colptr.begin(), out.colptr.end() - 1);
+        for (int64_t e = 0; e < nnz; ++e) {
+            int32_t c = col_of(e);
+            int32_t dst = next[c]++;
+            out.rowidx[dst] = row_of(e);
+            out.vals[dst] = x[e];
+        }
+        return;
+    }
+    std::vector<int32_t> cnt((size_t)nt * n, 0);  // entries per (chunk, column), then offsets
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+    for (int t = 0; t < nt; ++t) {
+        int32_t* ct = cnt.data() + (size_t)t * n;
+        for (int64_t e = nnz * t / nt; e < nnz * (t + 1) / nt; ++e) ct[col_of(e)]++;
+    }
+    int32_t run = 0;
+    for (int32_t c = 0; c < n; ++c) {
+        out.colptr[c] = run;
+        for (int t = 0; t < nt; ++t) {
+            const int32_t k = cnt[(size_t)t * n + c];
+            cnt[(size_t)t * n + c] = run;
+            run += k;
+        }
+    }
+    out.colptr[n] = run;
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+    for (int t = 0; t < nt; ++t) {
+        int32_t* next = cnt.data() + (size_t)t * n;
+        for (int64_t e = nnz * t / nt; e < nnz * (t + 1) / nt; ++e) {
+            int32_t dst = next[col_of(e)]++;
+            out.rowidx[dst] = row_of(e);
+            out.vals[dst] = x[e];
+        }
     }
 }
 
+// Stable sort of column c's entries [start, end) by row index, then
+// summation of equal rows (in their input order, from the first one); the
+// merged entries are written from `w` on. Returns the merged count.
+int32_t sort_sum_column(Csc& A, int32_t start, int32_t end, int32_t w,
+                        std::vector<std::pair<int32_t, double>>& tmp) {
+    bool sorted = true;
+    for (int32_t k = start + 1; k < end; ++k)
+        if (A.rowidx[k] < A.rowidx[k - 1]) { sorted = false; break; }
+    if (!sorted) {
+        tmp.resize((size_t)(end - start));
+        for (int32_t k = start; k < end; ++k) tmp[k - start] = {A.rowidx[k], A.vals[k]};
+        std::stable_sort(tmp.begin(), tmp.end(),
+                         [](const auto& a, const auto& b) { return a.first < b.first; });
+        for (int32_t k = start; k < end; ++k) {
+            A.rowidx[k] = tmp[k - start].first;
+            A.vals[k] = tmp[k - start].second;
+        }
+    }
+    const int32_t w0 = w;
+    int32_t k = start;
+    while (k < end) {
+        int32_t r = A.rowidx[k];
+        double v = A.vals[k++];
+        while (k < end && A.rowidx[k] == r) v += A.vals[k++];
+        A.rowidx[w] = r;
+        A.vals[w] = v;
+        ++w;
+    }
+    return w - w0;
+}
+
 // Stable sort of each column by row index, then summation of equal rows.
+// Large inputs: columns are sorted and merged in place in parallel, then
+// compacted by the merged counts (same result as the serial pass).
 void sort_and_sum(Csc& A) {
     const int32_t n = A.n;
-    std::vector<std::pair<int32_t, double>> tmp;
-    int32_t w = 0;
-    int32_t start = 0;
-    for (int32_t c = 0; c < n; ++c) {
-        int32_t end = A.colptr[c + 1];
-        bool sorted = true;
-        for (int32_t k = start + 1; k < end; ++k)
-            if (A.rowidx[k] < A.rowidx[k - 1]) { sorted = false; break; }
-        if (!sorted) {
-            tmp.resize((size_t)(end - start));
-            for (int32_t k = start; k < end; ++k) tmp[k - start] = {A.rowidx[k], A.vals[k]};
-            std::stable_sort(tmp.begin(), tmp.end(),
-                             [](const auto& a, const auto& b) { return a.first < b.first; });
-            for (int32_t k = start; k < end; ++k) {
-                A.rowidx[k] = tmp[k - start].first;
-                A.vals[k] = tmp[k - start].second;
+    const int nt = prep_threads(A.nnz());
+    if (nt == 1) {
+        std::vector<std::pair<int32_t, double>> tmp;
+        int32_t w = 0, start = 0;
+        for (int32_t c = 0; c < n; ++c) {
+            const int32_t end = A.colptr[c + 1];
+            A.colptr[c] = w;
+            w += sort_sum_column(A, start, end, w, tmp);
+            start = end;
+        }
+        A.colptr[n] = w;
+    } else {
+        std::vector<int32_t> merged((size_t)n + 1, 0);
+#pragma omp parallel num_threads(nt)
+        {
+            std::vector<std::pair<int32_t, double>> tmp;
+#pragma omp for schedule(dynamic, 256)
+            for (int32_t c = 0; c < n; ++c)
+                merged[c + 1] = sort_sum_column(A, A.colptr[c], A.colptr[c + 1], A.colptr[c], tmp);
+        }
+        for (int32_t c = 0; c < n; ++c) merged[c + 1] += merged[c];
+        // compaction: column c's merged entries move down from colptr[c] to
+        // merged[c] <= colptr[c]; columns in order, so nothing is overwritten
+        // before it is read
+        for (int32_t c = 0; c < n; ++c) {
+            const int32_t src = A.colptr[c], dst = merged[c], len = merged[c + 1] - merged[c];
+            if (src != dst) {
+                std::memmove(A.rowidx.data() + dst, A.rowidx.data() + src, sizeof(int32_t) * len);
+                std::memmove(A.vals.data() + dst, A.vals.data() + src, sizeof(double) * len);
             }
         }
-        A.colptr[c] = w;
-        int32_t k = start;
-        while (k < end) {
-            int32_t r = A.rowidx[k];
-            double v = A.vals[k++];
-            while (k < end && A.rowidx[k] == r) v += A.vals[k++];
-            A.rowidx[w] = r;
-            A.vals[w] = v;
-            ++w;
-        }
-        start = end;
+        A.colptr.swap(merged);
     }
-    A.colptr[n] = w;
+    const int32_t w = A.colptr[n];
     A.rowidx.resize((size_t)w);
     A.vals.resize((size_t)w);
     A.rowidx.shrink_to_fit();
