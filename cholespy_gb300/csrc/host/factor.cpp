@@ -3,9 +3,11 @@
 // Replaces the reference's CHOLMOD calls (src/cholesky_solver.cpp:200-297):
 // cholmod_analyze (ordering + symbolic) and cholmod_factorize (numeric, LL^T,
 // simplicial). The exported factor has exactly the simplicial symbolic
-// pattern (fundamental supernodes only, no amalgamation, so no explicit
-// zeros are added) and is laid out like cholmod_factor_to_sparse: CSC, rows
-// sorted, diagonal first in each column.
+// pattern (no explicit zeros) and is laid out like cholmod_factor_to_sparse:
+// CSC, rows sorted, diagonal first in each column. Only the numeric phase
+// works on amalgamated fronts (chains of supernodes merged with explicit
+// zeros); each column of L is then read back at its own pattern (entries
+// outside it are exact zeros: every product feeding them has a zero factor).
 //
 // Published methods followed (no CHOLMOD source used):
 //   * elimination tree: Liu's algorithm with path compression
@@ -17,7 +19,8 @@
 //   * fundamental supernodes (Liu, Ng & Peyton, SIAM J. Matrix Anal. Appl.
 //     14, 1993);
 //   * multifrontal numeric factorisation (Duff & Reid 1983; Liu, SIAM Review
-//     34, 1992) with dense blocked kernels (dense.cpp).
+//     34, 1992) with dense blocked kernels (dense.cpp), on fronts from relaxed
+//     supernode amalgamation (Ashcraft & Grimes, ACM TOMS 15, 1989).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -365,6 +368,63 @@ Status factorize(const Csc& A, const FactorOptions& opt, Factor& F, std::string&
     }
     std::vector<int32_t>().swap(srows);
 
+    // ---- fronts of the numeric phase (relaxed amalgamation) -------------
+    // Supernode s joins its parent p's front when its columns end where p's
+    // begin (s is p's last child) and the merged front stays narrow or adds
+    // few explicit zeros: always up to 4 columns, up to 16 columns with at
+    // most half zeros, up to 48 with at most 10%, any width with at most 5%
+    // (the zeros of the merged trapezoid of columns against its rows). The
+    // rule depends on the pattern only.
+    {
+        std::vector<int32_t> gstart((size_t)nsn);
+        std::vector<int64_t> gnz((size_t)nsn, 0);
+        std::vector<char> merged((size_t)nsn, 0);
+        for (int32_t s = 0; s < nsn; ++s) {
+            gstart[s] = F.sn_start[s];
+            for (int32_t j = F.sn_start[s]; j < F.sn_start[s + 1]; ++j) gnz[s] += cnt[j];
+        }
+        for (int32_t s = 0; s < nsn; ++s) {
+            const int32_t p = sn_parent[s];
+            if (p < 0 || F.sn_start[s + 1] != F.sn_start[p]) continue;
+            const int64_t wp = F.sn_start[p + 1] - F.sn_start[p];
+            const int64_t w = F.sn_start[p + 1] - gstart[s];
+            const int64_t fsz = w + (cnt[F.sn_start[p]] - wp);
+            const double trap = (double)w * (double)fsz - 0.5 * (double)w * (double)(w - 1);
+            const double zeros = trap - (double)(gnz[s] + gnz[p]);
+            const double frac = zeros / trap;
+            if (w <= 4 || (w <= 16 && frac <= 0.5) || (w <= 48 && frac <= 0.1) || frac <= 0.05) {
+                merged[s] = 1;
+                gstart[p] = gstart[s];
+                gnz[p] += gnz[s];
+            }
+        }
+        std::vector<int32_t> front_of((size_t)nsn, -1), top_of((size_t)nsn);
+        for (int32_t s = nsn - 1; s >= 0; --s) top_of[s] = merged[s] ? top_of[sn_parent[s]] : s;
+        for (int32_t s = 0; s < nsn; ++s)
+            if (!merged[s]) {
+                front_of[s] = (int32_t)sym->fr_nr.size();
+                const int32_t w = F.sn_start[s + 1] - F.sn_start[s];
+                sym->fr_col.push_back(gstart[s]);
+                sym->fr_rpos.push_back((int64_t)F.colptr[F.sn_start[s]] + w);
+                sym->fr_nr.push_back((int32_t)cnt[F.sn_start[s]] - w);
+            }
+        const int32_t nfr = (int32_t)sym->fr_nr.size();
+        sym->fr_col.push_back(n);
+        sym->fr_parent.assign((size_t)nfr, -1);
+        sym->fr_child_ptr.assign((size_t)nfr + 1, 0);
+        for (int32_t s = 0; s < nsn; ++s)
+            if (!merged[s] && sn_parent[s] >= 0) {
+                const int32_t f = front_of[s], pf = front_of[top_of[sn_parent[s]]];
+                sym->fr_parent[f] = pf;
+                sym->fr_child_ptr[pf + 1]++;
+            }
+        for (int32_t f = 0; f < nfr; ++f) sym->fr_child_ptr[f + 1] += sym->fr_child_ptr[f];
+        sym->fr_children.resize((size_t)sym->fr_child_ptr[nfr]);
+        std::vector<int32_t> nx(sym->fr_child_ptr.begin(), sym->fr_child_ptr.end() - 1);
+        for (int32_t f = 0; f < nfr; ++f)  // children in increasing order
+            if (sym->fr_parent[f] >= 0) sym->fr_children[nx[sym->fr_parent[f]]++] = f;
+    }
+
     // ---- the symbolic analysis kept for refactorisations ---------------
     sym->n = n;
     sym->a_colptr = A.colptr;
@@ -382,21 +442,22 @@ Status numeric_factor(const Factor& F, const SymbolicCache& S, const std::vector
                       std::vector<double>& vals_out, double& flops_out, std::string& err) {
     const int32_t n = F.n;
     const int threads = resolve_threads(nthreads);
-    const int32_t nsn = (int32_t)F.sn_start.size() - 1;
+    const int32_t nsn = (int32_t)S.fr_nr.size();  // fronts
     const int64_t total = F.nnz();
     const std::vector<int32_t>& cptr = S.cptr;
     const std::vector<int32_t>& crow = S.crow;
-    const std::vector<int32_t>& sn_parent = S.sn_parent;
-    const std::vector<int32_t>& child_ptr = S.child_ptr;
-    const std::vector<int32_t>& children = S.children;
+    const std::vector<int32_t>& sn_parent = S.fr_parent;
+    const std::vector<int32_t>& child_ptr = S.fr_child_ptr;
+    const std::vector<int32_t>& children = S.fr_children;
     if (n == 0) {
         vals_out.clear();
         flops_out = 0.0;
         return ST_OK;
     }
     // ---- multifrontal numeric factorisation -----------------------------
-    // Supernodes whose subtree holds more than 1/(4 threads) of the flops (a
-    // set closed towards the roots) are factorised last, one after the other,
+    // On the fronts of the relaxed amalgamation (S.fr_*). Fronts whose
+    // subtree holds more than 1/(4 threads) of the flops (a set closed
+    // towards the roots) are factorised last, one after the other,
     // with multi-threaded dense kernels; every subtree hanging below that set
     // is an independent task, factorised by one thread. A finished front is
     // kept whole and handed to its parent: its trailing m x m block (leading
@@ -408,8 +469,8 @@ Status numeric_factor(const Factor& F, const SymbolicCache& S, const std::vector
     std::vector<int32_t> first((size_t)nsn);  // first supernode of each subtree (postorder: contiguous)
     double total_flops = 0.0;
     for (int32_t s = 0; s < nsn; ++s) {
-        const double w = F.sn_start[s + 1] - F.sn_start[s];
-        const double m = (double)(F.colptr[F.sn_start[s] + 1] - F.colptr[F.sn_start[s]]) - w;
+        const double w = S.fr_col[s + 1] - S.fr_col[s];
+        const double m = S.fr_nr[s];
         sn_flops[s] = w * w * w / 3.0 + m * w * w + m * m * w;
         total_flops += sn_flops[s];
         sub_flops[s] = sn_flops[s];
@@ -478,12 +539,13 @@ Status numeric_factor(const Factor& F, const SymbolicCache& S, const std::vector
     auto factor_sn = [&](int32_t s, Work& wk, int dt) -> bool {
         if (wk.relpos.empty()) wk.relpos.assign((size_t)n, -1);
         int32_t* relpos = wk.relpos.data();
-        const int32_t f = F.sn_start[s], l1 = F.sn_start[s + 1];
+        const int32_t f = S.fr_col[s], l1 = S.fr_col[s + 1];
         const int64_t w = l1 - f;
-        const int32_t* rows = F.rowidx.data() + F.colptr[f];
-        const int64_t Fsz = F.colptr[f + 1] - F.colptr[f];
-        const int64_t m = Fsz - w;
-        for (int64_t i = 0; i < Fsz; ++i) relpos[rows[i]] = (int32_t)i;
+        const int32_t* below = F.rowidx.data() + S.fr_rpos[s];  // rows below the front's columns
+        const int64_t m = S.fr_nr[s];
+        const int64_t Fsz = w + m;
+        for (int64_t i = 0; i < w; ++i) relpos[f + i] = (int32_t)i;
+        for (int64_t i = 0; i < m; ++i) relpos[below[i]] = (int32_t)(w + i);
         Buf front = wk.take((size_t)(Fsz * Fsz));
         double* fr = front.data();
         // only the lower triangle of a front is ever read (assembly, the dense
@@ -499,9 +561,8 @@ Status numeric_factor(const Factor& F, const SymbolicCache& S, const std::vector
         for (int32_t q = child_ptr[s + 1] - 1; q >= child_ptr[s]; --q) {
             const int32_t c = children[q];
             Front& up = upd[c];
-            const int32_t cf = F.sn_start[c];
             const int32_t cw = (int32_t)up.w;
-            const int32_t* crows = F.rowidx.data() + F.colptr[cf] + cw;
+            const int32_t* crows = F.rowidx.data() + S.fr_rpos[c];
             const int64_t cm = up.fsz - cw, ld = up.fsz;
             const double* ub = up.u.data() + cw + cw * ld;  // update block (lower part)
 #pragma omp parallel for num_threads(dt) schedule(dynamic, 16) if (dt > 1 && cm >= kParCols)
@@ -520,17 +581,25 @@ Status numeric_factor(const Factor& F, const SymbolicCache& S, const std::vector
             dense::trsm_right_lower_t(m, w, fr, Fsz, fr + w, Fsz, dt);
             dense::gemm_nt_sub(m, m, w, fr + w, Fsz, fr + w, Fsz, fr + w + w * Fsz, Fsz, true, dt);
         }
-        if (ok) {  // store the columns of L
+        if (ok) {  // store the columns of L: each column's own pattern
             double* vals = vals_out.data();
             const int32_t* cp = F.colptr.data();
+            const int32_t* ri = F.rowidx.data();
 #pragma omp parallel for num_threads(dt) schedule(static) if (dt > 1 && w * Fsz >= kParCols * kParCols)
             for (int64_t j = 0; j < w; ++j) {
                 double* dst = vals + cp[f + j];
-                const double* src = fr + j + j * Fsz;
-                for (int64_t i = 0; i < Fsz - j; ++i) dst[i] = src[i];
+                const int64_t len = cp[f + j + 1] - cp[f + j];
+                const double* src = fr + j * Fsz;
+                if (len == Fsz - j) {  // the column fills the front below its diagonal
+                    for (int64_t i = 0; i < len; ++i) dst[i] = src[j + i];
+                } else {
+                    const int32_t* pr = ri + cp[f + j];
+                    for (int64_t i = 0; i < len; ++i) dst[i] = src[relpos[pr[i]]];
+                }
             }
         }
-        for (int64_t i = 0; i < Fsz; ++i) relpos[rows[i]] = -1;
+        for (int64_t i = 0; i < w; ++i) relpos[f + i] = -1;
+        for (int64_t i = 0; i < m; ++i) relpos[below[i]] = -1;
         if (ok && m > 0 && sn_parent[s] >= 0) {
             upd[s].fsz = Fsz;
             upd[s].w = w;
@@ -578,8 +647,13 @@ Status numeric_factor(const Factor& F, const SymbolicCache& S, const std::vector
         err = "Matrix is not positive definite!";
         return ST_NOT_POSDEF;
     }
+    // reported: the flop count of the supernodal (unamalgamated) factorisation
     double flops = 0.0;
-    for (int32_t s = 0; s < nsn; ++s) flops += sn_flops[s];
+    for (size_t t = 0; t + 1 < F.sn_start.size(); ++t) {
+        const double w = F.sn_start[t + 1] - F.sn_start[t];
+        const double m = (double)(F.colptr[F.sn_start[t] + 1] - F.colptr[F.sn_start[t]]) - w;
+        flops += w * w * w / 3.0 + m * w * w + m * m * w;
+    }
     flops_out = flops;
     return ST_OK;
 }

@@ -64,6 +64,13 @@ struct SymbolicCache {
     std::vector<int32_t> amap;                // A's CSC entry -> position in the permuted lower CSC (-1: upper)
     std::vector<int32_t> cptr, crow;          // lower CSC of P A P^T (pattern)
     std::vector<int32_t> sn_parent, child_ptr, children;  // supernodal elimination tree
+    // fronts of the numeric phase (relaxed amalgamation): chains of
+    // supernodes, each the last child of the next, merged into one front with
+    // explicit zeros; front f has columns [fr_col[f], fr_col[f+1]) and below
+    // them the fr_nr[f] rows rowidx[fr_rpos[f]...] of its top supernode. L
+    // keeps its own (simplicial) pattern.
+    std::vector<int32_t> fr_col, fr_nr, fr_parent, fr_child_ptr, fr_children;
+    std::vector<int64_t> fr_rpos;
     // the raw input the analysis was made for (empty if not recorded):
     int32_t fmt = -1;
     std::vector<int32_t> in_i, in_j;  // index arrays as given
