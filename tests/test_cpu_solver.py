@@ -305,3 +305,38 @@ def test_cpu_solver_concurrent_solves(gblib):
         y = np.zeros_like(b)
         s.solve(b, y)
         assert np.array_equal(x, y)
+
+
+class _DLPackOnly:
+    """An array known only through the DLPack protocol (no NumPy or torch
+    type), as TensorFlow, JAX or Dr.Jit arrays reach the solver."""
+
+    def __init__(self, a):
+        self._a = a
+
+    def __dlpack__(self, *args, **kwargs):
+        return self._a.__dlpack__(*args, **kwargs)
+
+    def __dlpack_device__(self):
+        return self._a.__dlpack_device__()
+
+    @property
+    def shape(self):
+        return self._a.shape
+
+
+def test_frameworks_dlpack_cpu(gblib):
+    """tests/test_cholesky.py:88-199 for frameworks that are not installed
+    here: the same case through arrays that expose only DLPack."""
+    from cholespy_gb300 import CholeskySolverF, MatrixType
+    n, vals, idx, _ = reference_problem("cube")
+    np.random.seed(45)
+    b = np.random.random(size=(n, 32)).astype(np.float32)
+    x_ref = spsolve_ref(n, vals, idx, b)
+    solver = CholeskySolverF(n, _DLPackOnly(np.ascontiguousarray(idx[0], np.int32)),
+                             _DLPackOnly(np.ascontiguousarray(idx[1], np.int32)),
+                             _DLPackOnly(np.ascontiguousarray(vals)), MatrixType.COO)
+    assert solver.is_cpu
+    x = np.zeros_like(b)
+    solver.solve(_DLPackOnly(b), _DLPackOnly(x))
+    assert np.allclose(x, x_ref)
