@@ -23,8 +23,10 @@
 //     product with the rows below it, blocks of columns in parallel; then the
 //     panels' triangles in reverse), then the tasks in parallel (they read
 //     only finished ancestors);
-//   * right-hand sides in chunks of 8 (then 4, 2, 1), each packed row-major;
-//     with at least one chunk per thread, threads take whole chunks.
+//   * one-column supernodes (most of a mesh factor's) update rows directly
+//     and take their backward dot product in place;
+//   * right-hand sides in chunks of 16 (then 8, 4, 2, 1), each packed
+//     row-major; with at least one chunk per thread, threads take whole chunks.
 // Every value is summed in an order fixed by the factor and the RHS count, so
 // results do not depend on the thread count.
 #include <algorithm>
@@ -44,7 +46,7 @@ namespace {
 constexpr int32_t PB = 64;   // panel width of the blocked triangular solves
 constexpr int32_t QB = 1024;  // rows per block of a panel's update
 constexpr int32_t JB = 16;   // columns per block of a backward dot product
-constexpr int WMAX = 8;      // widest RHS chunk
+constexpr int WMAX = 16;     // widest RHS chunk
 
 int host_threads(int32_t t) {
     if (t > 0) return t;
@@ -264,6 +266,7 @@ struct Kern {
 template <class Fn>
 void with_width(int w, Fn&& fn) {
     switch (w) {
+        case 16: fn(std::integral_constant<int, 16>{}); break;
         case 8: fn(std::integral_constant<int, 8>{}); break;
         case 4: fn(std::integral_constant<int, 4>{}); break;
         case 2: fn(std::integral_constant<int, 2>{}); break;
@@ -292,6 +295,26 @@ inline Sn sn_of(const CpuSolvePlan& P, const Fac& f, int32_t s) {
 // to `nr_eff` of R (the rows inside the caller's subtree).
 template <int W>
 void fwd_sn(const Fac& f, const Sn& s, int32_t nr_eff, double* Y, double* acc) {
+    if (s.c1 - s.c0 == 1) {  // one column: y_j /= L(j,j), then y_r -= L(r,j) y_j straight into each row
+        const double* col = f.v + f.cp[s.c0];
+        double* yj = Y + (int64_t)s.c0 * W;
+        if constexpr (W == 1) {
+            const double y = yj[0] / col[0];
+            yj[0] = y;
+            for (int32_t q = 0; q < nr_eff; ++q) Y[s.R[q]] -= col[1 + q] * y;
+        } else {
+            Row<W> y = Row<W>::load(yj);
+            const v2d dv = {col[0], col[0]};
+            for (int c = 0; c < W / 2; ++c) y.v[c] /= dv;
+            y.store(yj);
+            for (int32_t q = 0; q < nr_eff; ++q) {
+                Row<W> t = Row<W>::zero();
+                t.add_scaled(col[1 + q], yj);
+                t.sub_from(Y + (int64_t)s.R[q] * W);
+            }
+        }
+        return;
+    }
     for (int32_t p0 = s.c0; p0 < s.c1; p0 += PB) {
         const int32_t p1 = std::min(p0 + PB, s.c1);
         Kern<W>::fwd_tri(f, p0, p1, Y);
@@ -304,6 +327,34 @@ void fwd_sn(const Fac& f, const Sn& s, int32_t nr_eff, double* Y, double* acc) {
 // Backward sweep of one supernode on one chunk; Z holds nr rows of W.
 template <int W>
 void bwd_sn(const Fac& f, const Sn& s, double* Y, double* Z) {
+    if (s.c1 - s.c0 == 1) {  // one column: a dot product over its rows, read in place
+        const double* col = f.v + f.cp[s.c0];
+        if constexpr (W == 1) {
+            double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+            int32_t q = 0;
+            for (; q + 4 <= s.nr; q += 4) {
+                s0 += col[1 + q] * Y[s.R[q]];
+                s1 += col[2 + q] * Y[s.R[q + 1]];
+                s2 += col[3 + q] * Y[s.R[q + 2]];
+                s3 += col[4 + q] * Y[s.R[q + 3]];
+            }
+            for (; q < s.nr; ++q) s0 += col[1 + q] * Y[s.R[q]];
+            Y[s.c0] = (Y[s.c0] - ((s0 + s1) + (s2 + s3))) / col[0];
+        } else {
+            Row<W> a = Row<W>::zero(), b = Row<W>::zero();
+            int32_t q = 0;
+            for (; q + 2 <= s.nr; q += 2) {
+                a.add_scaled(col[1 + q], Y + (int64_t)s.R[q] * W);
+                b.add_scaled(col[2 + q], Y + (int64_t)s.R[q + 1] * W);
+            }
+            if (q < s.nr) a.add_scaled(col[1 + q], Y + (int64_t)s.R[q] * W);
+            Row<W> y = Row<W>::load(Y + (int64_t)s.c0 * W);
+            const v2d dv = {col[0], col[0]};
+            for (int c = 0; c < W / 2; ++c) y.v[c] = (y.v[c] - (a.v[c] + b.v[c])) / dv;
+            y.store(Y + (int64_t)s.c0 * W);
+        }
+        return;
+    }
     if (s.nr > 0) {
         for (int32_t k = 0; k < s.nr; ++k) std::memcpy(Z + (int64_t)k * W, Y + (int64_t)s.R[k] * W, sizeof(double) * W);
         Kern<W>::bwd_dot(f, s.c1, s.c0, s.c1, s.nr, Z, Y);
@@ -468,7 +519,8 @@ void solve_impl(const Factor& F, const CpuSolvePlan& P, int32_t nrhs, const T* b
     std::vector<Step> steps;
     for (int32_t i = 0; i < (int32_t)P.top_sn.size(); ++i) {
         const Sn sn = sn_of(P, f, P.top_sn[i]);
-        const bool large = (int64_t)(sn.c1 - sn.c0) * (sn.c1 - sn.c0 + sn.nr) * nrhs >= big;
+        // (one-column supernodes have their own formulas: never split)
+        const bool large = sn.c1 - sn.c0 > 1 && (int64_t)(sn.c1 - sn.c0) * (sn.c1 - sn.c0 + sn.nr) * nrhs >= big;
         if (!large && !steps.empty() && !steps.back().split && steps.back().b == i)
             steps.back().b = i + 1;
         else
