@@ -102,6 +102,12 @@ struct Row {
         for (int c = 0; c < W / 2; ++c) r.v[c] -= v[c];
         r.store(p);
     }
+    void sub_scaled_from(double* p, double l) const {  // p -= l * this
+        const v2d s = {l, l};
+        Row r = load(p);
+        for (int c = 0; c < W / 2; ++c) r.v[c] -= s * v[c];
+        r.store(p);
+    }
 };
 
 // Column-block kernels on one RHS chunk Y (n rows of W doubles).
@@ -122,11 +128,7 @@ struct Kern {
                 const v2d dv = {d, d};
                 for (int c = 0; c < W / 2; ++c) y.v[c] /= dv;
                 y.store(yj);
-                for (int32_t i = j + 1; i < p1; ++i) {
-                    Row<W> t = Row<W>::zero();
-                    t.add_scaled(col[i - j], yj);
-                    t.sub_from(Y + (int64_t)i * W);
-                }
+                for (int32_t i = j + 1; i < p1; ++i) y.sub_scaled_from(Y + (int64_t)i * W, col[i - j]);
             }
         }
     }
@@ -307,11 +309,7 @@ void fwd_sn(const Fac& f, const Sn& s, int32_t nr_eff, double* Y, double* acc) {
             const v2d dv = {col[0], col[0]};
             for (int c = 0; c < W / 2; ++c) y.v[c] /= dv;
             y.store(yj);
-            for (int32_t q = 0; q < nr_eff; ++q) {
-                Row<W> t = Row<W>::zero();
-                t.add_scaled(col[1 + q], yj);
-                t.sub_from(Y + (int64_t)s.R[q] * W);
-            }
+            for (int32_t q = 0; q < nr_eff; ++q) y.sub_scaled_from(Y + (int64_t)s.R[q] * W, col[1 + q]);
         }
         return;
     }
