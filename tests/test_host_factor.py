@@ -2,6 +2,7 @@
 through the C ABI, checked against the oracle's up-looking LL^T on the same
 permutation, and of the input checks."""
 import ctypes as C
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -9,6 +10,8 @@ import scipy.sparse as sp
 
 import oracle
 from cholespy_gb300 import _ffi, workloads
+
+ROOT = Path(__file__).resolve().parent.parent
 
 
 def factorize(gblib, n, ii, jj, x, fmt, threads=2):
@@ -225,3 +228,31 @@ def test_refactorize_cached_symbolic_bit_identical(gblib, fmt):
     finally:
         gblib.gbchol_factor_free(f)
         gblib.gbchol_factor_free(g)
+
+
+def test_factor_identical_for_one_openmp_thread(gblib, tmp_path):
+    """Ordering (its piece tasks take the OpenMP team size), symbolic and
+    numeric factorisation give the same factor, bit for bit, in a process
+    limited to one OpenMP thread as in this one (34^3: large enough for
+    every parallel path)."""
+    import os
+    import subprocess
+    import sys
+    k = 34
+    vals, idx = workloads.grid3d_coo(k, 1e-3)
+    n = k ** 3
+    here = factorize(gblib, n, idx[0], idx[1], vals, 2, threads=0)
+    script = (
+        "import sys, numpy as np\n"
+        f"sys.path.insert(0, {str(ROOT)!r}); sys.path.insert(0, {str(ROOT / 'tests')!r})\n"
+        "from cholespy_gb300 import _ffi, workloads\n"
+        "from test_host_factor import factorize\n"
+        f"vals, idx = workloads.grid3d_coo({k}, 1e-3)\n"
+        f"p, c, r, v, _ = factorize(_ffi.lib(), {n}, idx[0], idx[1], vals, 2, threads=0)\n"
+        f"np.savez({str(tmp_path / 'f.npz')!r}, p=p, c=c, r=r, v=v)\n")
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    out = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    with np.load(tmp_path / "f.npz") as z:
+        for a, b in zip(here[:4], (z["p"], z["c"], z["r"], z["v"])):
+            assert np.array_equal(a, b)
