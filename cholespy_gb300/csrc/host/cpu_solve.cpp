@@ -696,8 +696,9 @@ void cpu_plan(const Factor& F, CpuSolvePlan& P, int32_t threads) {
         for (int32_t s = 0; s < nsn; ++s) {
             const int32_t e = P.sn_start[s + 1] - 1;  // last column
             if (cost[e] > cut) continue;
+            // maximal: the parent supernode (cost of its last column) is above the cut
             const int32_t pe = cp[e + 1] - cp[e] > 1 ? ri[cp[e] + 1] : -1;
-            if (pe >= 0 && cost[pe] <= cut) continue;  // not maximal
+            if (pe >= 0 && cost[P.sn_start[sn_of_col[pe] + 1] - 1] <= cut) continue;
             const int32_t first = sn_of_col[e - size[e] + 1];
             P.task_first.push_back(first);
             P.task_last.push_back(s);
