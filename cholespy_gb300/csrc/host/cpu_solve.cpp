@@ -738,23 +738,48 @@ void cpu_plan(const Factor& F, CpuSolvePlan& P, int32_t threads) {
         const int32_t lo = P.sn_start[P.task_first[t]], hi = P.sn_start[P.task_last[t] + 1] - 1;
         for (int32_t j = lo; j <= hi; ++j) task_hi_of_col[j] = hi;
     }
-    for (int32_t j = 0; j < n; ++j) {
-        if (task_hi_of_col[j] < 0) continue;
-        const int32_t* b0 = ri + cp[j], *b1 = ri + cp[j + 1];
-        for (const int32_t* p = std::upper_bound(b0, b1, task_hi_of_col[j]); p < b1; ++p)
-            P.pt_ptr[(size_t)top_index[*p] + 1]++;
+    // contiguous column ranges (in column order) count their entries per top
+    // row, then fill: columns ascend within each row for any thread count
+    const int ntp = F.nnz() > (1 << 22) ? nt : 1;
+    std::vector<int32_t> c0((size_t)ntp + 1, n);
+    c0[0] = 0;
+    for (int t = 1; t < ntp; ++t)
+        c0[t] = (int32_t)(std::lower_bound(F.colptr.begin(), F.colptr.end() - 1, (int32_t)(F.nnz() * t / ntp)) -
+                          F.colptr.begin());
+    for (int t = 1; t <= ntp; ++t) c0[t] = std::max(c0[t], c0[t - 1]);
+    std::vector<int64_t> cnt((size_t)ntp * ntop, 0);
+#pragma omp parallel for num_threads(ntp) schedule(static, 1) if (ntp > 1)
+    for (int t = 0; t < ntp; ++t) {
+        int64_t* ct = cnt.data() + (size_t)t * ntop;
+        for (int32_t j = c0[t]; j < c0[t + 1]; ++j) {
+            if (task_hi_of_col[j] < 0) continue;
+            const int32_t *b0 = ri + cp[j], *b1 = ri + cp[j + 1];
+            for (const int32_t* p = std::upper_bound(b0, b1, task_hi_of_col[j]); p < b1; ++p) ct[top_index[*p]]++;
+        }
     }
-    for (int32_t t = 0; t < ntop; ++t) P.pt_ptr[t + 1] += P.pt_ptr[t];
-    P.pt_col.resize((size_t)P.pt_ptr[ntop]);
-    P.pt_pos.resize((size_t)P.pt_ptr[ntop]);
-    std::vector<int64_t> fill(P.pt_ptr.begin(), P.pt_ptr.end() - 1);
-    for (int32_t j = 0; j < n; ++j) {
-        if (task_hi_of_col[j] < 0) continue;
-        const int32_t* b0 = ri + cp[j], *b1 = ri + cp[j + 1];
-        for (const int32_t* p = std::upper_bound(b0, b1, task_hi_of_col[j]); p < b1; ++p) {
-            const int64_t d = fill[(size_t)top_index[*p]]++;
-            P.pt_col[d] = j;
-            P.pt_pos[d] = p - ri;
+    int64_t run = 0;
+    for (int32_t r = 0; r < ntop; ++r) {
+        P.pt_ptr[r] = run;
+        for (int t = 0; t < ntp; ++t) {
+            const int64_t k = cnt[(size_t)t * ntop + r];
+            cnt[(size_t)t * ntop + r] = run;
+            run += k;
+        }
+    }
+    P.pt_ptr[ntop] = run;
+    P.pt_col.resize((size_t)run);
+    P.pt_pos.resize((size_t)run);
+#pragma omp parallel for num_threads(ntp) schedule(static, 1) if (ntp > 1)
+    for (int t = 0; t < ntp; ++t) {
+        int64_t* next = cnt.data() + (size_t)t * ntop;
+        for (int32_t j = c0[t]; j < c0[t + 1]; ++j) {
+            if (task_hi_of_col[j] < 0) continue;
+            const int32_t *b0 = ri + cp[j], *b1 = ri + cp[j + 1];
+            for (const int32_t* p = std::upper_bound(b0, b1, task_hi_of_col[j]); p < b1; ++p) {
+                const int64_t d = next[top_index[*p]]++;
+                P.pt_col[d] = j;
+                P.pt_pos[d] = p - ri;
+            }
         }
     }
 }

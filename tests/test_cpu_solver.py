@@ -340,3 +340,22 @@ def test_frameworks_dlpack_cpu(gblib):
     x = np.zeros_like(b)
     solver.solve(_DLPackOnly(b), _DLPackOnly(x))
     assert np.allclose(x, x_ref)
+
+
+def test_host_solve_plan_independent_of_threads(gblib):
+    """The host solve's structure (built at a factor's first solve, in
+    parallel for large factors) is the same whatever thread count builds it:
+    two factors of one matrix, first solved with 1 and with all threads, give
+    bit-identical solutions (32^3: above the parallel-build size)."""
+    n, vals, idx = 32 ** 3, *workloads.grid3d_coo(32, 1e-3)
+    f1, _ = _factorize(gblib, n, vals, idx)
+    f2, _ = _factorize(gblib, n, vals, idx)
+    try:
+        b = np.random.default_rng(4).standard_normal((n, 3))
+        x1 = _host_solve(gblib, f1, b, 1, 1)
+        x2 = _host_solve(gblib, f2, b, 1, 0)
+        assert np.array_equal(x1, x2)
+        assert np.array_equal(_host_solve(gblib, f1, b, 1, 0), x1)
+    finally:
+        gblib.gbchol_factor_free(f1)
+        gblib.gbchol_factor_free(f2)
