@@ -359,3 +359,23 @@ def test_host_solve_plan_independent_of_threads(gblib):
     finally:
         gblib.gbchol_factor_free(f1)
         gblib.gbchol_factor_free(f2)
+
+
+@pytest.mark.parametrize("name", ["cube", "ico3"])
+@pytest.mark.parametrize("variant", ["float", "double"])
+def test_cpu_solver_golden(gblib, name, variant):
+    """The CPU-array solver against the committed golden solutions of the
+    reference's test recipe (tests/golden/, spsolve answers; the reference's
+    own tests/test_cholesky.py:31-44 check np.allclose against spsolve)."""
+    from pathlib import Path
+    from cholespy_gb300 import MatrixType
+    d = np.load(Path(__file__).resolve().parent / "golden" / f"spsolve_{name}.npz")
+    n = int(d["n"])
+    dt = np.float32 if variant == "float" else np.float64
+    s = _solver_cls(variant)(n, d["idx"][0], d["idx"][1], d["vals"], MatrixType.COO)
+    b = np.ascontiguousarray(d["b"], dt)
+    x = np.zeros_like(b)
+    s.solve(b, x)
+    assert np.allclose(x, d["x"])
+    if variant == "double":
+        assert np.abs(x - d["x"]).max() <= 1e-12 * np.abs(d["x"]).max()
