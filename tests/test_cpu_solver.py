@@ -379,3 +379,18 @@ def test_cpu_solver_golden(gblib, name, variant):
     assert np.allclose(x, d["x"])
     if variant == "double":
         assert np.abs(x - d["x"]).max() <= 1e-12 * np.abs(d["x"]).max()
+
+
+def test_reference_import_name(gblib):
+    """`from cholespy import ...` (the reference's import name) gives this
+    build's classes, so code written for the reference runs unchanged."""
+    import cholespy
+    import cholespy_gb300
+    assert cholespy.CholeskySolverF is cholespy_gb300.CholeskySolverF
+    assert cholespy.CholeskySolverD is cholespy_gb300.CholeskySolverD
+    assert cholespy.MatrixType is cholespy_gb300.MatrixType
+    n, vals, idx, b = reference_problem("cube", ncols=4)
+    s = cholespy.CholeskySolverD(n, idx[0], idx[1], vals, cholespy.MatrixType.COO)
+    x = np.zeros_like(b)
+    s.solve(b, x)
+    assert np.allclose(x, spsolve_ref(n, vals, idx, b))
