@@ -31,6 +31,7 @@
 // results do not depend on the thread count.
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <type_traits>
 
 #include "host.h"
@@ -421,10 +422,14 @@ void solve_impl(const Factor& F, const CpuSolvePlan& P, int32_t nrhs, const T* b
         for (int w = WMAX / 2; w >= 1; w /= 2)
             if (nrhs - c >= w) { chunks.push_back({c, w, nullptr, nullptr}); c += w; }
     }
-    std::vector<double> ybuf((size_t)n * nrhs), zbuf((size_t)std::max(P.max_nr, 1) * nrhs);
+    // work arrays without value-initialisation: every row of Y is loaded from
+    // b (task columns by their task, the others as top rows) and every scratch
+    // entry is written before it is read
+    std::unique_ptr<double[]> ybuf(new double[(size_t)n * nrhs]);
+    std::unique_ptr<double[]> zbuf(new double[(size_t)std::max(P.max_nr, 1) * nrhs]);
     for (Chunk& ch : chunks) {
-        ch.Y = ybuf.data() + (int64_t)n * ch.col0;
-        ch.Z = zbuf.data() + (int64_t)std::max(P.max_nr, 1) * ch.col0;
+        ch.Y = ybuf.get() + (int64_t)n * ch.col0;
+        ch.Z = zbuf.get() + (int64_t)std::max(P.max_nr, 1) * ch.col0;
     }
     const int32_t nc = (int32_t)chunks.size();
     const Io<T> io{b, x, nrhs, F.perm.data()};
@@ -435,7 +440,8 @@ void solve_impl(const Factor& F, const CpuSolvePlan& P, int32_t nrhs, const T* b
     const int T_ = threads;
     // per thread: a panel update's accumulator and a supernode's gathered rows
     const int64_t zrows = std::max(P.max_nr, 1);
-    std::vector<double> accbuf((size_t)T_ * QB * WMAX), zthr((size_t)T_ * zrows * WMAX);
+    std::unique_ptr<double[]> accbuf(new double[(size_t)T_ * QB * WMAX]);
+    std::unique_ptr<double[]> zthr(new double[(size_t)T_ * zrows * WMAX]);
 
     auto task_cols = [&](int32_t t, int32_t& lo, int32_t& hi) {
         lo = P.sn_start[P.task_first[t]];
@@ -479,8 +485,8 @@ void solve_impl(const Factor& F, const CpuSolvePlan& P, int32_t nrhs, const T* b
 #pragma omp parallel for num_threads(T_) schedule(dynamic, 1) if (T_ > 1 && nc > 1)
         for (int32_t ci = 0; ci < nc; ++ci) {
             const Chunk& ch = chunks[(size_t)ci];
-            double* acc = accbuf.data() + (size_t)thread_id() * QB * WMAX;
-            double* Z = zthr.data() + (size_t)thread_id() * zrows * WMAX;
+            double* acc = accbuf.get() + (size_t)thread_id() * QB * WMAX;
+            double* Z = zthr.get() + (size_t)thread_id() * zrows * WMAX;
             for (int32_t t = 0; t < ntask; ++t) task_fwd(t, ch, acc);
             top_rows_fwd(ch, 0, ntop);
             with_width(ch.w, [&](auto Wc) {
@@ -526,8 +532,8 @@ void solve_impl(const Factor& F, const CpuSolvePlan& P, int32_t nrhs, const T* b
     }
 #pragma omp parallel num_threads(T_)
     {
-        double* acc = accbuf.data() + (size_t)thread_id() * QB * WMAX;
-        double* Z = zthr.data() + (size_t)thread_id() * zrows * WMAX;
+        double* acc = accbuf.get() + (size_t)thread_id() * QB * WMAX;
+        double* Z = zthr.get() + (size_t)thread_id() * zrows * WMAX;
 #pragma omp for schedule(dynamic, 1)
         for (int64_t it = 0; it < (int64_t)ntask * nc; ++it) task_fwd((int32_t)(it / nc), chunks[(size_t)(it % nc)], acc);
 #pragma omp for schedule(dynamic, 1)
