@@ -26,7 +26,7 @@
 //   * one-column supernodes (most of a mesh factor's) update rows directly
 //     and take their backward dot product in place;
 //   * right-hand sides in chunks of 16 (then 8, 4, 2, 1), each packed
-//     row-major; with at least one chunk per thread, threads take whole chunks.
+//     row-major; the parallel phases run over (task or row block, chunk).
 // Every value is summed in an order fixed by the factor and the RHS count, so
 // results do not depend on the thread count.
 #include <algorithm>
@@ -480,13 +480,12 @@ void solve_impl(const Factor& F, const CpuSolvePlan& P, int32_t nrhs, const T* b
         for (int32_t t = t0; t < t1; ++t) io.store(ch, P.top_rows[t], P.top_rows[t] + 1);
     };
 
-    if (nc >= T_ || T_ == 1) {
-        // whole chunks per thread
-#pragma omp parallel for num_threads(T_) schedule(dynamic, 1) if (T_ > 1 && nc > 1)
+    if (T_ == 1) {
+        // one thread: each chunk through the whole solve
+        double* acc = accbuf.get();
+        double* Z = zthr.get();
         for (int32_t ci = 0; ci < nc; ++ci) {
             const Chunk& ch = chunks[(size_t)ci];
-            double* acc = accbuf.get() + (size_t)thread_id() * QB * WMAX;
-            double* Z = zthr.get() + (size_t)thread_id() * zrows * WMAX;
             for (int32_t t = 0; t < ntask; ++t) task_fwd(t, ch, acc);
             top_rows_fwd(ch, 0, ntop);
             with_width(ch.w, [&](auto Wc) {
@@ -503,8 +502,10 @@ void solve_impl(const Factor& F, const CpuSolvePlan& P, int32_t nrhs, const T* b
         return;
     }
 
-    // Fewer chunks than threads: tasks x chunks, then the top region with
-    // the work of each large supernode split across threads.
+    // Several threads: tasks x chunks, then the top region with the work of
+    // each large supernode split across threads (measured better balanced
+    // than whole chunks per thread even when there are as many chunks as
+    // threads).
     const int32_t nrb = (ntop + QB - 1) / QB;  // blocks of top rows
     const int64_t big = 1 << 16;                // supernode work worth a split across threads
     // Split sizes of a large supernode's steps: about four items per thread
