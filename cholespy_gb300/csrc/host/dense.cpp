@@ -186,6 +186,22 @@ void trsm_rec(int64_t m, int64_t n, const double* L, int64_t ldl, double* B, int
 void trsm_right_lower_t(int64_t m, int64_t n, const double* L, int64_t ldl, double* B, int64_t ldb,
                         int threads) {
     if (m <= 0 || n <= 0) return;
+    // Large solves: blocks of kCols columns, left to right. Each block of B is
+    // solved against its diagonal block of L (rows independent, in fixed
+    // 64-row pieces), then the columns to its right are updated by one large
+    // GEMM, which spreads well over threads. The blocking depends on the sizes
+    // only, so the results do not depend on the thread count.
+    constexpr int64_t kCols = 256;
+    if (n > 2 * kCols && (double)m * (double)n * (double)n > 6.4e7) {
+        for (int64_t j0 = 0; j0 < n; j0 += kCols) {
+            const int64_t nb = std::min(kCols, n - j0);
+            trsm_right_lower_t(m, nb, L + j0 + j0 * ldl, ldl, B + j0 * ldb, ldb, threads);
+            if (j0 + nb < n)
+                gemm_nt_sub(m, n - j0 - nb, nb, B + j0 * ldb, ldb, L + (j0 + nb) + j0 * ldl, ldl,
+                            B + (j0 + nb) * ldb, ldb, false, threads);
+        }
+        return;
+    }
     // Rows of B are independent: solve them in fixed blocks of kRows rows
     // (a multiple of the micro-kernel's MR), spread over threads when large.
     // The blocks do not depend on the thread count, and neither do the results.
