@@ -484,7 +484,8 @@ class CholeskySolverD(_CholeskySolver):
 
     ``refine=True`` keeps an FP32 copy of the factor and the FP64 matrix; then
     ``solve`` runs FP32 solves with FP64-residual iterative refinement to
-    ``tol`` and ``solve_fp64`` the plain FP64 solve.
+    ``tol`` and ``solve_fp64`` the plain FP64 solve. (A solver built from CPU
+    arrays solves in FP64 on the host and ignores ``refine``.)
     """
 
     _precision = 1
