@@ -208,6 +208,9 @@ class _CholeskySolver:
         _ffi.check(st)
         self._fh = fh
         self._n = n_rows
+        # build the host solve's structure now (a zero-RHS solve), so that the
+        # first solve is not slower than the others
+        _ffi.check(_ffi.lib().gbchol_factor_solve(fh, self._precision, 0, None, None, 0))
 
     def __del__(self):
         h = getattr(self, "_h", None)
