@@ -60,6 +60,7 @@ __global__ void __launch_bounds__(256) level_kernel(int n, const int* __restrict
         const int lo = LOWER ? s : s + 1;
         const int hi = LOWER ? e - 1 : e;
         int lvl = 0;
+        bool gave_up = false;
         // flags of 4 entries per lane are loaded together (independent
         // relaxed loads); only entries not yet published take the bounded
         // wait; one acquire fence then orders the level reads.
@@ -74,11 +75,19 @@ __global__ void __launch_bounds__(256) level_kernel(int n, const int* __restrict
             for (int u = 0; u < 4; ++u) f[u] = c[u] >= 0 ? dev::ld_volatile(flags + c[u]) : epoch;
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (f[u] < epoch) dev::wait_geq(flags + c[u], epoch, status);
+                if (f[u] < epoch && !dev::wait_geq(flags + c[u], epoch, status)) gave_up = true;
             dev::fence_acquire();
 #pragma unroll
             for (int u = 0; u < 4; ++u)
                 if (c[u] >= 0) lvl = max(lvl, __ldcg(levels + c[u]) + 1);
+        }
+        // An abandoned wait (status already records the timeout) means a
+        // dependency's level was never published: mark the row invalid
+        // (-1), publish nothing built from unpublished data, and stop; the
+        // other warps give up at their next wait.
+        if (__any_sync(0xffffffffu, gave_up)) {
+            if (lane == 0) levels[row] = -1;
+            break;
         }
         lvl = dev::warp_max(lvl);
         local_max = max(local_max, lvl);

@@ -781,8 +781,10 @@ int gbchol_solve_refined(gbchol_handle h, int32_t nrhs, const double* b, double*
         RefineState hs;
         CUDA_TRY(cudaMemcpyAsync(&hs, h->rstate.p, sizeof(RefineState), cudaMemcpyDeviceToHost, s));
         CUDA_TRY(cudaStreamSynchronize(s));
-        stats->iterations = hs.converged ? hs.iterations : max_iter;
-        stats->converged = hs.converged;
+        // A non-finite or too-large residual never counts as converged.
+        const int conv_ok = hs.converged && hs.max_rel <= tol;
+        stats->iterations = conv_ok ? hs.iterations : max_iter;
+        stats->converged = conv_ok;
         stats->max_rel_residual = hs.max_rel;
     }
     return GBCHOL_OK;

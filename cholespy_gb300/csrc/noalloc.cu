@@ -1,11 +1,10 @@
 // gbchol_solve_noalloc: the solve of gbchol_solve for callers that must not
 // allocate GPU memory while solving. No counterpart in the reference.
 //
-// Some callers can't call cudaMalloc at solve time: code running inside a
-// CUDA-graph capture that must not allocate, real-time or embedded loops
-// whose memory is fixed up front, or hosts whose allocator owns all device
-// memory (a framework's caching allocator or a memory pool the solver may not
-// bypass). gbchol_solve may grow the solver's work array (cudaMalloc) when a
+// Some callers can't call cudaMalloc at solve time: real-time or embedded
+// loops whose device memory is fixed up front (an allocation there can stall
+// or fail), and hosts whose allocator owns all device memory (a framework's
+// caching allocator, or a memory pool the solver may not bypass). gbchol_solve may grow the solver's work array (cudaMalloc) when a
 // call brings more right-hand sides than any call before; this entry point
 // never allocates: its permuted-space work array is the file-scope device
 // array below, of a fixed size, which every GPU that loads the library holds
@@ -13,8 +12,10 @@
 //
 // Set-up: the first call on a device looks up the array's device address
 // with cudaGetSymbolAddress (host code cannot use the array's name as a
-// device pointer) and caches it per device. Make that first call outside any
-// stream capture.
+// device pointer) and caches it per device. Make that first call before any
+// stream capture. The cached address holds for the life of the process's
+// context on that device; a process that calls cudaDeviceReset must not
+// call this entry point afterwards.
 //
 // Sharing: every call (on any solver) uses the same array and leaves its
 // last contents there. The solve writes every element it reads before

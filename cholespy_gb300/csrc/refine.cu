@@ -10,6 +10,8 @@
 // No counterpart in the reference (the reference has no refinement).
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "device.cuh"
 #include "refine.h"
 
@@ -101,12 +103,20 @@ __global__ void __launch_bounds__(kThreads) residual_kernel(ResidualArgs a) {
     }
     __syncthreads();
     if (threadIdx.x == 0) {
+        // The maximum carries NaN (fmax would drop it), and a RHS converges
+        // only when its ratio compares <= tol, which NaN never does: a NaN
+        // or Inf anywhere in b, x or the factor leaves the solve unconverged
+        // and reports a non-finite max_rel.
         double m = 0.0;
-        for (int j = 0; j < nrhs; ++j) m = fmax(m, ratio[j]);
-        // NaN never converges
+        bool all_ok = true;
+        for (int j = 0; j < nrhs; ++j) {
+            const double v = ratio[j];
+            if (!(v <= a.tol)) all_ok = false;
+            if (!(v <= m) && !isnan(m)) m = v;
+        }
         st->max_rel = m;
         st->checks += 1;
-        if (m <= a.tol) {
+        if (all_ok) {
             st->converged = 1;
             st->iterations = a.iter;
         }
@@ -125,15 +135,18 @@ cudaError_t launch_residual(const ResidualArgs& a, int grid, cudaStream_t stream
 }
 
 int residual_grid(int n) {
-    static int cached_dev = -1, cached_sms = 0;
+    // Per-device SM counts, filled once per device; relaxed atomics make
+    // concurrent callers on any thread or device safe (a race only repeats
+    // the same attribute query).
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> sm_count[kMaxDevices];
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
-    if (dev == cached_dev) {
-        sms = cached_sms;
-    } else {
+    if (dev >= 0 && dev < kMaxDevices) sms = sm_count[dev].load(std::memory_order_relaxed);
+    if (sms <= 0) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cached_dev = dev;
-        cached_sms = sms;
+        if (sms <= 0) sms = 1;
+        if (dev >= 0 && dev < kMaxDevices) sm_count[dev].store(sms, std::memory_order_relaxed);
     }
     int need = (n + kWarps - 1) / kWarps;
     int g = sms * 8;

@@ -21,6 +21,7 @@ from __future__ import annotations
 
 import ctypes as C
 import enum
+import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -60,6 +61,14 @@ class RefineResult:
     iterations: int
     converged: bool
     max_rel_residual: float
+
+
+def _refine_result(iterations: int, converged: bool, max_rel: float, tol: float) -> RefineResult:
+    """Stats of a refined solve as returned to the caller. A residual that is
+    not finite, or above tol, is never reported as converged, whatever the
+    device flag says."""
+    ok = bool(converged) and math.isfinite(max_rel) and max_rel <= tol
+    return RefineResult(int(iterations), ok, float(max_rel))
 
 
 def _torch():
@@ -303,7 +312,7 @@ class _CholeskySolver:
             int(max_iter), C.c_void_p(stream), C.byref(rs) if stats else None)
         _ffi.check(st)
         if stats:
-            return RefineResult(int(rs.iterations), bool(rs.converged), float(rs.max_rel_residual))
+            return _refine_result(int(rs.iterations), bool(rs.converged), float(rs.max_rel_residual), tol)
         return None
 
     def check(self):

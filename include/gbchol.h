@@ -156,17 +156,18 @@ int gbchol_solve(gbchol_handle h, int32_t precision, int32_t nrhs, const void* b
 
 /*
  * gbchol_solve for callers that cannot allocate GPU memory while solving:
- * code inside a CUDA-graph capture that must not allocate, real-time loops
- * whose memory is fixed up front, or hosts whose allocator owns all device
- * memory. gbchol_solve may grow the solver's work array with cudaMalloc when
+ * real-time loops whose device memory is fixed up front, or hosts whose
+ * allocator owns all device memory (a framework's caching allocator, a pool
+ * the solver may not bypass). gbchol_solve may grow the solver's work array with cudaMalloc when
  * a call brings more RHS than any before; this call allocates nothing. Its
  * work array is a fixed 16 MiB file-scope device array that every GPU
  * loading the library holds until exit, so it fails with GBCHOL_EINVAL when
  * the solve's work array exceeds 16 MiB: n * nrhs * element size (4 bytes
  * FP32, 8 FP64), plus 32 * nrhs * element size (rounded up to the RHS slice
  * width) per partial sum of the supernodal lower sweep. The first
- * call on a device looks up the array's device address; make it outside any
- * stream capture. All calls share the array, so calls that overlap on the
+ * call on a device looks up the array's device address; make it before any
+ * stream capture. The address is cached for the life of the process's
+ * context on that device (no calls after cudaDeviceReset). All calls share the array, so calls that overlap on the
  * GPU race: serialise them. Same arguments and results as gbchol_solve.
  * No counterpart in the reference.
  */

@@ -21,7 +21,13 @@ REF_DIR = HERE / "_ref"
 CUBIN = REF_DIR / "ref_kernels.cubin"
 LAUNCHER_SRC = HERE / "ref_gpu.cpp"
 LAUNCHER = REF_DIR / "libref_gpu.so"
-REFERENCE_KERNELS = Path("/root/reference/kernels/kernels.cu")
+# The reference checkout: $CHOLESPY_REFERENCE_DIR, or the --reference argument
+# of this script, else the build container's read-only checkout.
+REFERENCE_DIR = Path(os.environ.get("CHOLESPY_REFERENCE_DIR", "/root/reference"))
+
+
+def reference_kernels() -> Path:
+    return REFERENCE_DIR / "kernels" / "kernels.cu"
 
 
 def _nvcc():
@@ -32,18 +38,19 @@ def _nvcc():
 
 
 def build_cubin() -> bool:
-    if not REFERENCE_KERNELS.exists():
+    src = reference_kernels()
+    if not src.exists():
         return CUBIN.exists()
     nvcc = _nvcc()
     if nvcc is None:
         return CUBIN.exists()
     REF_DIR.mkdir(exist_ok=True)
-    src_stamp = f"{REFERENCE_KERNELS.stat().st_mtime_ns}"
+    src_stamp = f"{src.stat().st_mtime_ns}"
     stamp = REF_DIR / "ref_kernels.stamp"
     if CUBIN.exists() and stamp.exists() and stamp.read_text() == src_stamp:
         return True
     subprocess.run([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
-                    "-o", str(CUBIN), str(REFERENCE_KERNELS)], check=True)
+                    "-o", str(CUBIN), str(src)], check=True)
     stamp.write_text(src_stamp)
     return True
 
@@ -77,4 +84,10 @@ def build_if_present() -> bool:
 
 
 if __name__ == "__main__":
+    import argparse
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--reference", help="path of the reference checkout")
+    args = ap.parse_args()
+    if args.reference:
+        REFERENCE_DIR = Path(args.reference)
     print("cubin:", build_cubin(), "launcher:", build_launcher())

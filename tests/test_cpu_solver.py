@@ -394,3 +394,15 @@ def test_reference_import_name(gblib):
     x = np.zeros_like(b)
     s.solve(b, x)
     assert np.allclose(x, spsolve_ref(n, vals, idx, b))
+
+
+def test_refine_result_never_reports_nonfinite_as_converged():
+    """The Python edge reports a refined solve as converged only when its
+    max relative residual is finite and within tol, whatever the device
+    flag says (a NaN residual must not read as converged)."""
+    from cholespy_gb300.solver import _refine_result
+    assert _refine_result(1, True, 5e-14, 1e-10).converged
+    assert not _refine_result(1, True, float("nan"), 1e-10).converged
+    assert not _refine_result(1, True, float("inf"), 1e-10).converged
+    assert not _refine_result(1, True, 2e-10, 1e-10).converged
+    assert not _refine_result(3, False, 5e-14, 1e-10).converged

@@ -442,3 +442,33 @@ def test_save_load(cuda, tmp_path):
     np.savez(tmp_path / "bad.npz", format=np.array("other"), n=np.int64(1))
     with pytest.raises(ValueError):
         cg.CholeskySolverF.load(tmp_path / "bad.npz")
+
+
+@pytest.mark.parametrize("where", ["one_column", "all_columns", "inf"])
+def test_refined_solve_nonfinite_rhs_never_converges(cuda, where):
+    """A NaN or Inf in b must leave the refined solve unconverged with a
+    non-finite max relative residual (a maximum that dropped NaN would
+    report convergence at residual 0)."""
+    from cholespy_gb300 import CholeskySolverD, MatrixType, workloads
+    torch = cuda
+    n, vals, idx = 4096, *workloads.grid3d_coo(16, 1e-3)
+    s = CholeskySolverD(n, torch.tensor(idx[0], device="cuda"), torch.tensor(idx[1], device="cuda"),
+                        torch.tensor(vals, device="cuda"), MatrixType.COO, refine=True)
+    b = np.random.default_rng(5).standard_normal((n, 4))
+    if where == "one_column":
+        b[17, 2] = np.nan
+    elif where == "all_columns":
+        b[:] = np.nan
+    else:
+        b[5, 0] = np.inf
+    bt = torch.tensor(b, device="cuda")
+    xt = torch.zeros_like(bt)
+    st = s.solve_refined(bt, xt, tol=1e-10, max_iter=3)
+    s.check()
+    assert not st.converged
+    assert not np.isfinite(st.max_rel_residual)
+    assert st.iterations == 3
+    # a finite b on the same solver still converges afterwards
+    b2 = np.random.default_rng(6).standard_normal((n, 4))
+    st2 = s.solve_refined(torch.tensor(b2, device="cuda"), xt, tol=1e-10, max_iter=3)
+    assert st2.converged and st2.max_rel_residual <= 1e-10

@@ -1,7 +1,6 @@
 """GPU test of gbchol_solve_noalloc, the solve entry point for callers that
-cannot allocate GPU memory while solving (graph captures that must not
-allocate, fixed-memory real-time loops, hosts whose allocator owns the
-device). Its work array is a fixed static device array instead of memory
+cannot allocate GPU memory while solving (real-time loops whose device
+memory is fixed up front, hosts whose allocator owns the device). Its work array is a fixed static device array instead of memory
 the solver allocates. Called through the C ABI, two calls in a row, each
 checked against gbchol_solve on the same inputs within the solve tests'
 tolerance (1e-5 relative for FP32, 1e-12 for FP64). This file sorts last so
