@@ -171,6 +171,58 @@ cudaError_t upload_cast(DevBuf<T>& dst, const std::vector<double>& src) {
     return dst.upload(tmp.data(), tmp.size());
 }
 
+// The bulk sweeps' tiles and schedule (FP32 factor, no 32-column partial
+// sums), the tiles expanded on the device from the FP32 panels. Skipped (the
+// solves then use the 32-column sweeps for every RHS count) when the tiles
+// would take more than half of the free device memory.
+int setup_snb(gbchol_solver* h) {
+    const SolvePlan& P = h->plan;
+    h->snb_ready = false;
+    h->snb_lo_tiles.release();
+    h->snb_up_tiles.release();
+    if (!(h->store & GBCHOL_STORE_F32) || P.units.empty() || !P.parts.empty()) return GBCHOL_OK;
+    if (const char* env = std::getenv("GBCHOL_BULK_MIN_RHS")) h->snb_min_rhs = std::atoi(env);
+    SnbUpperPlan B;
+    build_snb_upper(P, B);
+    SnbOptions so;
+    if (const char* env = std::getenv("GBCHOL_BULK_KEEP")) so.keep = std::atoi(env);
+    if (const char* env = std::getenv("GBCHOL_BULK_GROUP")) so.group = std::atoi(env);
+    if (const char* env = std::getenv("GBCHOL_BULK_BLK_NS")) so.blk_ns = std::atoll(env);
+    if (const char* env = std::getenv("GBCHOL_BULK_BASE_NS")) so.base_ns = std::atoll(env);
+    SnbLowerPlan L;
+    build_snb_lower(P, B, so, L);
+    const size_t nlo = P.contribs.size(), nup = B.dep.size();
+    const size_t bytes = (nlo + nup) * 32 * 32 * sizeof(float);
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    if (bytes > free_b / 2) return GBCHOL_OK;
+    CUDA_TRY(h->snb_up_begin.upload(B.begin.data(), B.begin.size()));
+    CUDA_TRY(h->snb_up_dep.upload(B.dep.data(), B.dep.size()));
+    CUDA_TRY(h->snb_up_rows.upload(B.rows.data(), B.rows.size()));
+    CUDA_TRY(h->snb_unit_info.upload(L.unit_info.data(), L.unit_info.size()));
+    CUDA_TRY(h->snb_parts.upload(L.parts.data(), L.parts.size()));
+    CUDA_TRY(h->snb_order_lo.upload(L.order_lo.data(), L.order_lo.size()));
+    CUDA_TRY(h->snb_order_up.upload(L.order_up.data(), L.order_up.size()));
+    h->snb_nparts = (int32_t)L.parts.size();
+    // flags of the bulk partial sums follow the units'
+    if (h->uflags.count < P.units.size() + L.parts.size()) {
+        CUDA_TRY(h->uflags.alloc(P.units.size() + L.parts.size()));
+        CUDA_TRY(cudaMemset(h->uflags.p, 0, sizeof(int32_t) * h->uflags.count));
+    }
+    CUDA_TRY(h->snb_lo_tiles.alloc(std::max<size_t>(1, nlo) * 32 * 32));
+    CUDA_TRY(h->snb_up_tiles.alloc(std::max<size_t>(1, nup) * 32 * 32));
+    DevBuf<int64_t> src;
+    DevBuf<int32_t> ld, nrw;
+    CUDA_TRY(src.upload(B.src.data(), B.src.size()));
+    CUDA_TRY(ld.upload(B.ld.data(), B.ld.size()));
+    CUDA_TRY(nrw.upload(B.nrw.data(), B.nrw.size()));
+    CUDA_TRY(launch_snb_expand_lower(h->contribs.p, (int64_t)nlo, h->pan32.p, h->snb_lo_tiles.p, 0));
+    CUDA_TRY(launch_snb_expand_upper(src.p, ld.p, nrw.p, (int64_t)nup, h->pan32.p, h->snb_up_tiles.p, 0));
+    CUDA_TRY(cudaDeviceSynchronize());
+    h->snb_ready = true;
+    return GBCHOL_OK;
+}
+
 // Builds the solve plan from the factor and the level orders and uploads it.
 int setup_plan(gbchol_solver* h) {
     const Factor& F = h->F;
@@ -228,6 +280,7 @@ int setup_plan(gbchol_solver* h) {
     // unit flags, then partial-sum flags; <= 8 RHS slices
     CUDA_TRY(h->uflags.alloc(std::max<size_t>(1, (P.units.size() + P.parts.size()) * 8)));
     CUDA_TRY(cudaMemset(h->uflags.p, 0, sizeof(int32_t) * h->uflags.count));
+    if (int rc = setup_snb(h)) return rc;
     // row flags: top rows are always "ready" for the row kernels (they are
     // solved by the supernodal kernel in an earlier launch)
     h->flags_init.assign((size_t)n, 0);
@@ -309,9 +362,18 @@ namespace {
 // kernel; `out` is written through perm by both upper kernels.
 }  // namespace
 
+namespace {
+// Solves of this RHS count use the bulk supernodal sweeps.
+bool use_snb(const gbchol_solver* h, int nrhs, bool f32) {
+    return f32 && h->snb_ready && snb_supported(nrhs) && nrhs >= h->snb_min_rhs;
+}
+}  // namespace
+
 size_t gbchol::work_bytes(const gbchol_solver* h, int nrhs, bool f32) {
     const size_t es = f32 ? sizeof(float) : sizeof(double);
     const size_t x = ((size_t)std::max(h->n, 1) * nrhs * es + 255) / 256 * 256;
+    if (use_snb(h, nrhs, f32))  // the bulk sweeps' partial-sum slots
+        return x + (size_t)h->snb_nparts * 32 * nrhs * sizeof(float);
     return x + sn_pbuf_bytes((int)h->plan.parts.size(), nrhs, !f32, false);
 }
 
@@ -353,21 +415,54 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
     sn.sys0.parts = h->parts.p;
     sn.sys0.pbuf = static_cast<unsigned char*>(work) +
                    ((size_t)h->n * nrhs * (f32 ? sizeof(float) : sizeof(double)) + 255) / 256 * 256;
-    sn.sys0.n_units = (int)P.units.size();
-    sn.sys0.nrhs = nrhs;
-    sn.sys0.nslices = sn_slices(nrhs, !f32);
-    sn.nitems = (int)P.unit_order_lo.size() * sn.sys0.nslices;
-    sn.status = h->status.p;
-    sn.skip = skip;
-    sn.order = h->order_lo.p;
-    sn.counters = h->counters.p + 2;
-    sn.epoch = h->dev_epoch.p;
-    CUDA_TRY(launch_sn_sweep(sn, true, io, s));
-    sn.sys0.out = out;
-    sn.nitems = (int)P.units.size() * sn.sys0.nslices;
-    sn.order = h->order_up.p;
-    sn.counters = h->counters.p + 4;
-    CUDA_TRY(launch_sn_sweep(sn, false, io, s));
+    if (use_snb(h, nrhs, f32)) {
+        // 33..128 RHS: the bulk-copy supernodal sweeps (solve_snb.cu)
+        SnbArgs b;
+        b.units = h->units.p;
+        b.contribs = h->contribs.p;
+        b.lo_tiles = h->snb_lo_tiles.p;
+        b.up_tiles = h->snb_up_tiles.p;
+        b.up_begin = h->snb_up_begin.p;
+        b.up_rows = h->snb_up_rows.p;
+        b.up_dep = h->snb_up_dep.p;
+        b.unit_info = h->snb_unit_info.p;
+        b.parts = h->snb_parts.p;
+        b.pbuf = reinterpret_cast<float*>(sn.sys0.pbuf);
+        b.n_units = (int)P.units.size();
+        b.dinv = h->dinv32.p;
+        b.perm = h->perm.p;
+        b.tmp = static_cast<float*>(work);
+        b.uflags = h->uflags.p;
+        b.nrhs = nrhs;
+        b.status = h->status.p;
+        b.skip = skip;
+        b.epoch = h->dev_epoch.p;
+        b.nitems = (int)P.units.size() + h->snb_nparts;
+        b.order = h->snb_order_lo.p;
+        b.counters = h->counters.p + 2;
+        CUDA_TRY(launch_snb_sweep(b, true, io, s));
+        b.out = out;
+        b.nitems = (int)P.units.size();
+        b.order = h->snb_order_up.p;
+        b.counters = h->counters.p + 4;
+        CUDA_TRY(launch_snb_sweep(b, false, io, s));
+    } else {
+        sn.sys0.n_units = (int)P.units.size();
+        sn.sys0.nrhs = nrhs;
+        sn.sys0.nslices = sn_slices(nrhs, !f32);
+        sn.nitems = (int)P.unit_order_lo.size() * sn.sys0.nslices;
+        sn.status = h->status.p;
+        sn.skip = skip;
+        sn.order = h->order_lo.p;
+        sn.counters = h->counters.p + 2;
+        sn.epoch = h->dev_epoch.p;
+        CUDA_TRY(launch_sn_sweep(sn, true, io, s));
+        sn.sys0.out = out;
+        sn.nitems = (int)P.units.size() * sn.sys0.nslices;
+        sn.order = h->order_up.p;
+        sn.counters = h->counters.p + 4;
+        CUDA_TRY(launch_sn_sweep(sn, false, io, s));
+    }
     RowSweepArgs pt = lo;  // top-row terms of the leaf rows: no waits
     pt.sys0.rowptr = h->upt_rowptr.p;
     pt.sys0.cols = h->upt_cols.p;

@@ -412,4 +412,130 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
     }
 }
 
+void build_snb_upper(const SolvePlan& P, SnbUpperPlan& B) {
+    const int32_t nunits = (int32_t)P.units.size();
+    B.begin.assign((size_t)nunits + 1, 0);
+    for (int32_t u = 0; u < nunits; ++u) {
+        const SnUnit& U = P.units[u];
+        const int32_t wj = U.pos0 + U.w;
+        const int32_t nrb = (U.ld - U.sn_w + kChunk - 1) / kChunk;
+        const int32_t nlater = (U.sn_w - wj + kChunk - 1) / kChunk;
+        const int32_t chain = wj < U.sn_w ? 1 : 0;
+        B.begin[u + 1] = B.begin[u] + nrb + nlater - chain;
+    }
+    const size_t nb = (size_t)B.begin[nunits];
+    B.src.resize(nb);
+    B.ld.resize(nb);
+    B.nrw.resize(nb);
+    B.dep.resize(nb);
+    B.rows.assign(nb * kChunk, -1);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int32_t u = 0; u < nunits; ++u) {
+        const SnUnit& U = P.units[u];
+        const int32_t* srows = P.sn_rows.data() + U.rows_off;
+        const int32_t wj = U.pos0 + U.w;
+        const int32_t nrb = (U.ld - U.sn_w + kChunk - 1) / kChunk;
+        const int32_t nlater = (U.sn_w - wj + kChunk - 1) / kChunk;
+        for (int32_t b = 0; b < B.begin[u + 1] - B.begin[u]; ++b) {
+            int32_t p0, nr, dep;
+            if (b < nrb) {  // off-diagonal rows, highest block first
+                p0 = U.sn_w + (nrb - 1 - b) * kChunk;
+                nr = std::min(kChunk, U.ld - p0);
+                dep = P.unit_of_row[srows[p0]];
+            } else {        // later chunks of the supernode, last first
+                const int32_t c = nlater - 1 - (b - nrb);
+                p0 = wj + c * kChunk;
+                nr = std::min(kChunk, U.sn_w - p0);
+                dep = u + 1 + c;
+            }
+            const size_t t = (size_t)B.begin[u] + b;
+            B.src[t] = U.panel_col_off + p0;
+            B.ld[t] = U.ld;
+            B.nrw[t] = nr | (U.w << 16);
+            B.dep[t] = dep;
+            for (int32_t i = 0; i < nr; ++i) B.rows[t * kChunk + i] = srows[p0 + i];
+        }
+    }
+}
+
+void build_snb_lower(const SolvePlan& P, const SnbUpperPlan& B, const SnbOptions& o, SnbLowerPlan& L) {
+    const int32_t nunits = (int32_t)P.units.size();
+    L.unit_info.assign((size_t)nunits * 3, 0);
+    L.parts.clear();
+    for (int32_t u = 0; u < nunits; ++u) {
+        const SnUnit& U = P.units[u];
+        const int32_t chain = U.pos0 > 0 ? 1 : 0;
+        const int32_t nfree = U.contrib_end - U.contrib_begin - chain;
+        int32_t first = U.contrib_begin;
+        const int32_t pb = (int32_t)L.parts.size();
+        if (o.group > 0 && nfree > o.keep + o.group) {
+            const int32_t split = U.contrib_begin + nfree - o.keep;  // the unit keeps [split, end - chain)
+            const int32_t ng = (split - U.contrib_begin + o.group - 1) / o.group;
+            for (int32_t g = 0; g < ng; ++g) {  // equal shares of the split-off blocks
+                SnPartial q{};
+                q.unit = u;
+                q.contrib_begin = U.contrib_begin + (int32_t)((int64_t)(split - U.contrib_begin) * g / ng);
+                q.contrib_end = U.contrib_begin + (int32_t)((int64_t)(split - U.contrib_begin) * (g + 1) / ng);
+                L.parts.push_back(q);
+            }
+            first = split;
+        }
+        L.unit_info[(size_t)u * 3] = first;
+        L.unit_info[(size_t)u * 3 + 1] = pb;
+        L.unit_info[(size_t)u * 3 + 2] = (int32_t)L.parts.size();
+    }
+    // estimated starts (as in build_plan): an item should start when its work
+    // before its last wait is just done as that wait ends; the key is that
+    // start and at least one more than the key of every item it waits on, so
+    // sorting by key is a topological order
+    struct Est {
+        int64_t first = INT64_MAX, last = 0, key_dep = -1;
+        void dep(int64_t fin, int64_t key, int64_t lat) {
+            first = std::min(first, fin + lat);
+            last = std::max(last, fin + lat);
+            key_dep = std::max(key_dep, key);
+        }
+        int64_t done(int64_t nblocks, int64_t base, int64_t blk, int64_t& key) const {
+            const int64_t f = first == INT64_MAX ? 0 : first;
+            key = std::max({f, last - std::max<int64_t>(0, nblocks - 1) * blk, key_dep + 1});
+            return std::max(std::max(key, last) + base + blk, key + base + blk * std::max<int64_t>(1, nblocks));
+        }
+    };
+    const int32_t nparts = (int32_t)L.parts.size();
+    std::vector<int64_t> fin_u((size_t)nunits, 0), key_u((size_t)nunits, 0);
+    std::vector<int64_t> fin_p((size_t)nparts, 0), key_p((size_t)nparts, 0);
+    for (int32_t u = 0; u < nunits; ++u) {  // sources precede their destinations
+        const SnUnit& U = P.units[u];
+        Est eu;
+        for (int32_t q = L.unit_info[(size_t)u * 3 + 1]; q < L.unit_info[(size_t)u * 3 + 2]; ++q) {
+            Est eq;
+            for (int32_t e = L.parts[q].contrib_begin; e < L.parts[q].contrib_end; ++e)
+                eq.dep(fin_u[P.contribs[e].src_unit], key_u[P.contribs[e].src_unit], o.lat_ns);
+            fin_p[q] = eq.done(L.parts[q].contrib_end - L.parts[q].contrib_begin, o.base_ns, o.blk_ns, key_p[q]);
+            eu.dep(fin_p[q], key_p[q], o.lat_ns);
+        }
+        for (int32_t e = L.unit_info[(size_t)u * 3]; e < U.contrib_end; ++e)
+            eu.dep(fin_u[P.contribs[e].src_unit], key_u[P.contribs[e].src_unit], o.lat_ns);
+        fin_u[u] = eu.done(U.contrib_end - L.unit_info[(size_t)u * 3], o.base_ns, o.blk_ns, key_u[u]);
+    }
+    std::vector<int64_t> fin_up((size_t)nunits, 0), key_up((size_t)nunits, 0);
+    for (int32_t u = nunits - 1; u >= 0; --u) {  // the upper sweep waits on later units
+        const SnUnit& U = P.units[u];
+        Est eu;
+        for (int32_t t = B.begin[u]; t < B.begin[u + 1]; ++t) eu.dep(fin_up[B.dep[t]], key_up[B.dep[t]], o.lat_ns);
+        if (U.pos0 + U.w < U.sn_w) eu.dep(fin_up[u + 1], key_up[u + 1], o.lat_ns);  // the chain unit
+        fin_up[u] = eu.done(B.begin[u + 1] - B.begin[u], o.base_ns, o.blk_ns, key_up[u]);
+    }
+    L.order_lo.resize((size_t)nunits + nparts);
+    for (int32_t u = 0; u < nunits; ++u) L.order_lo[u] = u;
+    for (int32_t q = 0; q < nparts; ++q) L.order_lo[nunits + q] = ~q;
+    auto key_lo = [&](int32_t item) { return item >= 0 ? key_u[item] : key_p[~item]; };
+    std::stable_sort(L.order_lo.begin(), L.order_lo.end(),
+                     [&](int32_t a, int32_t b) { return key_lo(a) < key_lo(b); });
+    L.order_up.resize((size_t)nunits);
+    for (int32_t u = 0; u < nunits; ++u) L.order_up[u] = u;
+    std::stable_sort(L.order_up.begin(), L.order_up.end(),
+                     [&](int32_t a, int32_t b) { return key_up[a] < key_up[b]; });
+}
+
 }  // namespace gbchol

@@ -102,6 +102,46 @@ struct PlanOptions {
     int32_t part_group = 0;
 };
 
+// Upper-sweep blocks of the bulk supernodal sweeps, per unit in the order
+// the unit applies them (the supernode's off-diagonal 32-row blocks, highest
+// rows first, then its later chunks but the next, last first): where each
+// block lies in the panels, which work-array rows it multiplies and which
+// unit it waits for.
+struct SnbUpperPlan {
+    std::vector<int32_t> begin;  // per unit: first block (n_units + 1 entries)
+    std::vector<int64_t> src;    // panel offset of (block row 0, unit column 0)
+    std::vector<int32_t> ld;     // leading dimension of that panel
+    std::vector<int32_t> nrw;    // block rows | unit columns << 16
+    std::vector<int32_t> dep;    // unit whose flag the block waits for
+    std::vector<int32_t> rows;   // 32 per block: permuted row of each block row, -1 past the block
+};
+
+void build_snb_upper(const SolvePlan& P, SnbUpperPlan& U);
+
+// Lower-sweep work items of the bulk supernodal sweeps and the ticket order
+// of both bulk sweeps. A unit whose list (without the chain block) is longer
+// than keep + group applies only its last `keep` blocks itself; the earlier
+// ones go to partial sums of about `group` blocks (separate items, started as
+// soon as their sources are done) that the unit adds in a fixed order.
+// Ticket keys come from the start-time estimate of build_plan with costs for
+// one item applying its blocks one after the other (blk_ns each).
+struct SnbOptions {
+    int32_t keep = 16;
+    int32_t group = 0;        // 0: no partial sums
+    int64_t lat_ns = 1000;    // flag latency
+    int64_t base_ns = 3000;   // fixed cost of an item (diagonal solve, chain step)
+    int64_t blk_ns = 500;     // cost of one block
+};
+
+struct SnbLowerPlan {
+    std::vector<int32_t> unit_info;   // per unit: first block it applies itself, first and end partial
+    std::vector<SnPartial> parts;     // partial sums over contribution ranges
+    std::vector<int32_t> order_lo;    // lower-sweep tickets: unit u, or partial p as ~p
+    std::vector<int32_t> order_up;    // upper-sweep tickets: units
+};
+
+void build_snb_lower(const SolvePlan& P, const SnbUpperPlan& B, const SnbOptions& o, SnbLowerPlan& L);
+
 // Builds the plan from a factor and the level orders of L and L^T (rows
 // sorted by (level, row)).
 void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,

@@ -1,0 +1,484 @@
+// Bulk-copy supernodal sweeps for many right-hand sides (sm_103a, FP32).
+//
+// Same work decomposition as solve_sn.cu (units of <= 32 columns of the
+// top-region supernodes, atomic tickets in estimated-start order, epoch-
+// valued unit flags, the chain block folded into the diagonal solve), shaped
+// for 33..128 RHS:
+//
+// * One work item = one unit and every RHS column, so each L block is read
+//   once per solve instead of once per 32-column slice. Long lower-sweep
+//   block lists can be split into partial-sum items (plan.cpp,
+//   build_snb_lower) that the unit adds in a fixed order.
+// * L blocks are pre-expanded 32 x 32 tiles (zero outside the block's rows
+//   and columns): lower sweep, one per contribution block, [source
+//   column][unit row]; upper sweep, one per off-diagonal block of the
+//   unit's supernode, [block row][unit column]. A tile is one 4 KB bulk copy.
+// * A producer warp takes the tickets (running up to one item ahead of the
+//   consumers through two descriptor slots) and streams each item's blocks
+//   through a 4-stage shared-memory ring with cp.async.bulk: per block,
+//   once the source unit's flag is set, the L tile and the block's rows of
+//   the work array, one bulk copy per run of consecutive rows, completing on
+//   the stage's mbarrier. Descriptors and flags are read 32 blocks at a time
+//   (one round trip per window). Eight consumer warps apply each stage
+//   (thread = one RHS column and 16 (or 8) unit rows / columns, 4-row groups
+//   the block lacks skipped; every output has one owner, so there is no
+//   reduction across warps and no CTA-wide barrier per block) and release
+//   it on the stage's second mbarrier.
+// * After the last block: t' = t - sum, x = E t' (E = D^-1 lower, D^-T
+//   upper), then, once the chain unit's flag is set, x -= M x_chain; the x
+//   rows go to the work array (and, upper sweep, through perm to the output)
+//   and one release store publishes the unit.
+// Reference: the same sweeps as kernels/kernels.cu:64-202 (solve_lower /
+// solve_upper), with the per-row flag waits of the reference replaced by one
+// flag per unit.
+//
+// Every wait is bounded (device.cuh, bulk.cuh). Results are deterministic:
+// each output is summed by one thread over the item's blocks in list order.
+#include <cuda_runtime.h>
+
+#include "bulk.cuh"
+#include "device.cuh"
+#include "launch.h"
+#include "solve_snb.h"
+
+namespace gbchol {
+
+namespace {
+
+constexpr int kCW = 8;                    // consumer warps
+constexpr int kThreads = (kCW + 1) * 32;  // + one producer warp
+constexpr int kStages = 4;
+constexpr int kTile = 32 * 32;
+
+template <int SW>
+struct SnbStage {
+    float l[32][32];   // L tile
+    float x[32 * SW];  // the block's rows of the work array, row stride = the RHS count
+};
+
+template <int SW>
+struct SnbSmem {
+    SnbStage<SW> st[kStages];
+    float t[32][SW];   // t' = t - sum of the blocks (right-hand side of the diagonal solve)
+    float e[32][32];   // e[j][i] = E[i][j]
+    float m[32][32];   // m[j][i] = M[i][j] (the chain block folded into the diagonal solve)
+    uint64_t full[kStages], empty[kStages];
+    uint64_t item_full[2], item_empty[2];  // the two item-descriptor slots
+    SnUnit item_unit[2];
+    int item_v[2], item_valid[2];
+    int ext[kStages];        // rows of the stage's x block (lower: source columns, upper: block rows)
+    unsigned mask[kStages];  // unit rows (lower) / columns (upper) the block has
+};
+
+template <typename TO, bool ACCUM>
+struct SnbIO {
+    using tout = TO;
+    static constexpr bool accum = ACCUM;
+};
+
+// Item geometry shared by the producer and the consumers.
+struct SnbItem {
+    bool part, chain;
+    int uidx, tile0, nblk;
+};
+
+template <bool LOWER>
+__device__ __forceinline__ SnbItem snb_item(const SnbArgs& a, int v, const SnUnit& U) {
+    SnbItem it;
+    // a lower-sweep partial sum (item ~p): blocks summed into a slot
+    it.part = LOWER && v < 0;
+    it.uidx = it.part ? a.parts[~v].unit : v;
+    // the chain input: lower, the previous chunk of the supernode (its block
+    // is the last of the list); upper, the next one (not listed)
+    it.chain = !it.part && (LOWER ? U.pos0 > 0 : U.pos0 + U.w < U.sn_w);
+    if (it.part) {
+        it.tile0 = a.parts[~v].contrib_begin;
+        it.nblk = a.parts[~v].contrib_end - it.tile0;
+    } else if (LOWER) {
+        it.tile0 = a.unit_info[(size_t)it.uidx * 3];
+        it.nblk = U.contrib_end - (it.chain ? 1 : 0) - it.tile0;
+    } else {
+        it.tile0 = a.up_begin[it.uidx];
+        it.nblk = a.up_begin[it.uidx + 1] - it.tile0;
+    }
+    return it;
+}
+
+template <class io, bool LOWER, int SW>
+__global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    SnbSmem<SW>& sm = *reinterpret_cast<SnbSmem<SW>*>(smem_raw);
+    if (a.skip && dev::ld_volatile(a.skip)) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // every CTA reads the sweep's epoch before the last CTA out bumps it
+    const int epoch = dev::ld_volatile(a.epoch);
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            bulk::mbar_init(&sm.full[s], 1);
+            bulk::mbar_init(&sm.empty[s], kCW);
+        }
+        for (int s = 0; s < 2; ++s) {
+            bulk::mbar_init(&sm.item_full[s], 1);
+            bulk::mbar_init(&sm.item_empty[s], kCW);
+        }
+        bulk::fence_mbar_init();
+    }
+    __syncthreads();
+    const int nrhs = a.nrhs;
+    if (warp == kCW) {
+        // ---- producer: tickets, then the item's blocks into the stage ring
+        uint32_t gs = 0;  // ring stages used so far
+        for (uint32_t n = 0;; ++n) {
+            const int slot = (int)(n & 1);
+            int tk = 0;
+            if (lane == 0) tk = atomicAdd(a.counters, 1);
+            tk = __shfl_sync(0xffffffffu, tk, 0);
+            const bool valid = tk < a.nitems;
+            const int v = valid ? a.order[tk] : 0;
+            if (lane == 0) {
+                if (n >= 2) bulk::mbar_wait(&sm.item_empty[slot], ((n >> 1) - 1) & 1, a.status);
+                sm.item_valid[slot] = valid ? 1 : 0;
+                if (valid) {
+                    sm.item_v[slot] = v;
+                    sm.item_unit[slot] = a.units[v >= 0 ? v : a.parts[~v].unit];
+                }
+                bulk::mbar_arrive(&sm.item_full[slot]);
+            }
+            if (!valid) break;
+            const SnUnit U = a.units[v >= 0 ? v : a.parts[~v].unit];
+            const SnbItem it = snb_item<LOWER>(a, v, U);
+            const unsigned umask = U.w == 32 ? 0xffffffffu : (1u << U.w) - 1u;
+            // blocks in windows of 32: lane j reads the descriptor of the
+            // window's j-th block and checks its source's flag (one round
+            // trip for the window); the descriptors are broadcast by shuffles
+            for (int w0 = 0; w0 < it.nblk; w0 += 32) {
+                const int cnt = min(32, it.nblk - w0);
+                int src_j = 0, xcol_j = 0, w_j = 0, ready_j = 1;
+                unsigned mask_j = 0;
+                if (lane < cnt) {
+                    const int t = it.tile0 + w0 + lane;
+                    if (LOWER) {
+                        const SnContrib& C = a.contribs[t];
+                        src_j = C.src_unit;
+                        xcol_j = C.xcol;
+                        w_j = C.w;
+                        mask_j = C.rowmask;
+                    } else {
+                        src_j = a.up_dep[t];
+                    }
+                    ready_j = dev::ld_acquire(a.uflags + src_j) >= epoch;
+                }
+                // upper: the rows of the window's first block (later blocks'
+                // rows are read one block ahead)
+                int row_next = LOWER ? -1 : a.up_rows[(size_t)(it.tile0 + w0) * 32 + lane];
+                __syncwarp();  // orders the lanes' flag observations before every lane's copies
+                for (int q = 0; q < cnt; ++q) {
+                    const uint32_t g = gs + (uint32_t)(w0 + q);
+                    const int s = (int)(g % kStages);
+                    const int t = it.tile0 + w0 + q;
+                    const int src = __shfl_sync(0xffffffffu, src_j, q);
+                    const int ready = __shfl_sync(0xffffffffu, ready_j, q);
+                    int row;
+                    unsigned mask;
+                    if (LOWER) {
+                        const int xc = __shfl_sync(0xffffffffu, xcol_j, q), wb = __shfl_sync(0xffffffffu, w_j, q);
+                        row = lane < wb ? xc + lane : -1;
+                        mask = __shfl_sync(0xffffffffu, mask_j, q);
+                    } else {
+                        row = row_next;
+                        if (q + 1 < cnt) row_next = a.up_rows[(size_t)(t + 1) * 32 + lane];
+                        mask = umask;
+                    }
+                    // the block's rows are a prefix of the lanes; runs of
+                    // consecutive work-array rows go in one bulk copy each
+                    const unsigned have = __ballot_sync(0xffffffffu, row >= 0);
+                    const int rows = __popc(have);
+                    const int prev = __shfl_up_sync(0xffffffffu, row, 1);
+                    const bool start = row >= 0 && (lane == 0 || prev != row - 1);
+                    const unsigned later = __ballot_sync(0xffffffffu, start) & ~((2u << lane) - 1u);
+                    const int run = (later ? __ffs(later) - 1 : rows) - lane;  // rows in my run (if start)
+                    if (lane == 0) {
+                        if (g >= kStages) {
+                            const uint32_t par = ((g / kStages) - 1) & 1;
+                            bulk::mbar_wait(&sm.empty[s], par, a.status);
+                            // the stage's previous copies have landed (normally
+                            // long since: its consumers waited for them)
+                            bulk::mbar_wait(&sm.full[s], par, a.status, false);
+                        }
+                        if (!ready) dev::wait_geq(a.uflags + src, epoch, a.status);
+                        sm.ext[s] = rows;
+                        sm.mask[s] = mask;
+                        bulk::mbar_arrive_expect_tx(&sm.full[s], (uint32_t)((kTile + rows * nrhs) * 4));
+                    }
+                    __syncwarp();
+                    // the source rows were published under the flag: order the
+                    // bulk (async-proxy) reads after its acquire
+                    bulk::fence_proxy_async_global();
+                    const float* ltile = (LOWER ? a.lo_tiles : a.up_tiles) + (size_t)t * kTile;
+                    if (lane == 0) bulk::copy_g2s(&sm.st[s].l[0][0], ltile, kTile * 4, &sm.full[s]);
+                    if (start)
+                        bulk::copy_g2s(&sm.st[s].x[lane * nrhs], a.tmp + (size_t)row * nrhs,
+                                       (uint32_t)(run * nrhs) * 4, &sm.full[s]);
+                }
+            }
+            gs += (uint32_t)it.nblk;
+        }
+        // no bulk copy may still be landing when the CTA exits (they complete
+        // by themselves; this matters only after an abandoned wait)
+        if (lane == 0) {
+            for (int s = 0; s < kStages; ++s) {
+                if ((uint32_t)s >= gs) break;
+                const uint32_t last = gs - 1 - (uint32_t)((gs - 1 - (uint32_t)s) % kStages);  // last use of s
+                bulk::mbar_wait(&sm.full[s], (last / kStages) & 1, a.status, false);
+            }
+        }
+    } else {
+        // ---- consumers: thread = one RHS column k and NR unit rows (lower)
+        // / columns (upper) from r0
+        constexpr int G = SW / 32;        // consumer warps across the RHS columns
+        constexpr int NR = 32 * G / kCW;  // rows / columns per consumer thread
+        const int k = 32 * (warp % G) + lane;
+        const int r0 = NR * (warp / G);
+        uint32_t gs = 0;
+        for (uint32_t n = 0;; ++n) {
+            const int slot = (int)(n & 1);
+            bulk::mbar_wait(&sm.item_full[slot], (n >> 1) & 1, a.status);
+            if (!sm.item_valid[slot]) break;
+            const int v = sm.item_v[slot];
+            const SnUnit U = sm.item_unit[slot];
+            __syncwarp();
+            if (lane == 0) bulk::mbar_arrive(&sm.item_empty[slot]);  // the descriptor has been read
+            const SnbItem it = snb_item<LOWER>(a, v, U);
+            const int uidx = it.uidx, w = U.w;
+            // the unit's current right-hand side (my rows, my column)
+            float tv[NR];
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+                const int i = r0 + r;
+                tv[r] = (!it.part && i < w && k < nrhs) ? __ldcg(a.tmp + (size_t)(U.c0 + i) * nrhs + k) : 0.f;
+            }
+            // E and M to shared memory (read after the consumers' barrier
+            // below; the previous item's readers passed its last barrier)
+            if (!it.part) {
+                const float* dv = a.dinv + (size_t)uidx * 3 * kTile;
+                const float* mc = dv + (LOWER ? 1 : 2) * kTile;
+                for (int idx = tid; idx < kTile; idx += kCW * 32) {
+                    // dv[i + 32 j] = D^-1[i][j]
+                    if (LOWER) (&sm.e[0][0])[idx] = dv[idx];
+                    else sm.e[idx & 31][idx >> 5] = dv[idx];
+                    if (it.chain) (&sm.m[0][0])[idx] = mc[idx];
+                }
+            }
+            float acc[NR];
+#pragma unroll
+            for (int r = 0; r < NR; ++r) acc[r] = 0.f;
+            for (int b = 0; b < it.nblk; ++b) {
+                const uint32_t g = gs + (uint32_t)b;
+                const int s = (int)(g % kStages);
+                bulk::mbar_wait(&sm.full[s], (g / kStages) & 1, a.status);
+                const int ext = sm.ext[s];
+                // 4-row groups of my rows (columns) the block has: the others hold zeros
+                const unsigned grp = sm.mask[s] >> r0;
+                const SnbStage<SW>& st = sm.st[s];
+                for (int j = 0; j < ext; ++j) {
+                    const float xv = st.x[j * nrhs + k];
+                    const float4* lr = reinterpret_cast<const float4*>(&st.l[j][r0]);
+#pragma unroll
+                    for (int q = 0; q < NR / 4; ++q) {
+                        if (!((grp >> (4 * q)) & 0xFu)) continue;  // warp-uniform
+                        const float4 lv = lr[q];
+                        acc[4 * q] = fmaf(lv.x, xv, acc[4 * q]);
+                        acc[4 * q + 1] = fmaf(lv.y, xv, acc[4 * q + 1]);
+                        acc[4 * q + 2] = fmaf(lv.z, xv, acc[4 * q + 2]);
+                        acc[4 * q + 3] = fmaf(lv.w, xv, acc[4 * q + 3]);
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) bulk::mbar_arrive(&sm.empty[s]);
+            }
+            gs += (uint32_t)it.nblk;
+            if (it.part) {  // the sum goes to the partial's slot, then its flag
+                float* ps = a.pbuf + (size_t)(~v) * 32 * nrhs;
+                if (k < nrhs) {
+#pragma unroll
+                    for (int r = 0; r < NR; ++r) ps[(r0 + r) * nrhs + k] = acc[r];
+                }
+                bulk::named_sync(1, kCW * 32);
+                if (tid == 0) dev::st_release(a.uflags + a.n_units + ~v, epoch);
+                continue;
+            }
+            if (LOWER) {  // the unit's partial sums, in a fixed order
+                const int pb = a.unit_info[(size_t)uidx * 3 + 1], pe = a.unit_info[(size_t)uidx * 3 + 2];
+                for (int q = pb; q < pe; ++q) {
+                    if (lane == 0) dev::wait_geq(a.uflags + a.n_units + q, epoch, a.status);
+                    __syncwarp();
+                    const float* ps = a.pbuf + (size_t)q * 32 * nrhs;
+                    if (k < nrhs) {
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) acc[r] += __ldcg(ps + (r0 + r) * nrhs + k);
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < NR; ++r) sm.t[r0 + r][k] = tv[r] - acc[r];
+            bulk::named_sync(1, kCW * 32);
+            // x = E t' (my rows, my column)
+            float xv[NR];
+#pragma unroll
+            for (int r = 0; r < NR; ++r) xv[r] = 0.f;
+#pragma unroll 4
+            for (int j = 0; j < 32; ++j) {
+                const float tj = sm.t[j][k];
+                const float4* er = reinterpret_cast<const float4*>(&sm.e[j][r0]);
+#pragma unroll
+                for (int q = 0; q < NR / 4; ++q) {
+                    const float4 ev = er[q];
+                    xv[4 * q] = fmaf(ev.x, tj, xv[4 * q]);
+                    xv[4 * q + 1] = fmaf(ev.y, tj, xv[4 * q + 1]);
+                    xv[4 * q + 2] = fmaf(ev.z, tj, xv[4 * q + 2]);
+                    xv[4 * q + 3] = fmaf(ev.w, tj, xv[4 * q + 3]);
+                }
+            }
+            if (it.chain) {
+                const int cu = LOWER ? uidx - 1 : uidx + 1;                  // chain unit
+                const int crow = LOWER ? U.c0 - 32 : U.c0 + w;               // its first row
+                const int cw = LOWER ? 32 : min(32, U.sn_w - (U.pos0 + w));  // its width
+                if (lane == 0) dev::wait_geq(a.uflags + cu, epoch, a.status);
+                __syncwarp();
+                float xc[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    xc[j] = (j < cw && k < nrhs) ? __ldcg(a.tmp + (size_t)(crow + j) * nrhs + k) : 0.f;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const float4* mr = reinterpret_cast<const float4*>(&sm.m[j][r0]);
+#pragma unroll
+                    for (int q = 0; q < NR / 4; ++q) {
+                        const float4 mv = mr[q];
+                        xv[4 * q] = fmaf(-mv.x, xc[j], xv[4 * q]);
+                        xv[4 * q + 1] = fmaf(-mv.y, xc[j], xv[4 * q + 1]);
+                        xv[4 * q + 2] = fmaf(-mv.z, xc[j], xv[4 * q + 2]);
+                        xv[4 * q + 3] = fmaf(-mv.w, xc[j], xv[4 * q + 3]);
+                    }
+                }
+            }
+            if (k < nrhs) {
+#pragma unroll
+                for (int r = 0; r < NR; ++r) {
+                    const int i = r0 + r;
+                    if (i < w) {
+                        a.tmp[(size_t)(U.c0 + i) * nrhs + k] = xv[r];
+                        if (!LOWER) {
+                            using TO = typename io::tout;
+                            TO* out = static_cast<TO*>(a.out);
+                            const size_t oo = (size_t)a.perm[U.c0 + i] * nrhs + k;
+                            if (io::accum) out[oo] += (TO)xv[r];
+                            else out[oo] = (TO)xv[r];
+                        }
+                    }
+                }
+            }
+            // the barrier orders the consumers' writes before the release
+            bulk::named_sync(1, kCW * 32);
+            if (tid == 0) dev::st_release(a.uflags + uidx, epoch);
+        }
+    }
+    __syncthreads();
+    // the last CTA out resets the ticket and advances the epoch for the next
+    // launch (the launch boundary orders these writes)
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(a.counters + 1, 1) == (int)gridDim.x - 1) {
+            a.counters[0] = 0;
+            a.counters[1] = 0;
+            *a.epoch = epoch + 1;
+        }
+    }
+}
+
+template <class io, bool LOWER, int SW>
+cudaError_t launch_snb(const SnbArgs& a, cudaStream_t stream) {
+    const void* fn = (const void*)snb_sweep_kernel<io, LOWER, SW>;
+    const size_t smem = sizeof(SnbSmem<SW>);
+    int grid = 0;
+    cudaError_t e = coop_grid(fn, kThreads, smem, &grid);  // resident CTAs: a persistent grid
+    if (e != cudaSuccess) return e;
+    if (grid > a.nitems) grid = a.nitems;
+    snb_sweep_kernel<io, LOWER, SW><<<grid, kThreads, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+template <class io>
+cudaError_t launch_snb_io(const SnbArgs& a, bool lower, cudaStream_t stream) {
+    if (snb_width(a.nrhs) == 64)
+        return lower ? launch_snb<io, true, 64>(a, stream) : launch_snb<io, false, 64>(a, stream);
+    return lower ? launch_snb<io, true, 128>(a, stream) : launch_snb<io, false, 128>(a, stream);
+}
+
+// Lower tiles: warp per contribution block, lane = unit row i; tile[j][i] =
+// L[row i, source column j] (the block's rows are the set bits of its row
+// mask, in order).
+__global__ void expand_lower_kernel(const SnContrib* __restrict__ contribs, int64_t n,
+                                    const float* __restrict__ panels, float* __restrict__ tiles) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < n; b += nw) {
+        const SnContrib C = contribs[b];
+        const bool has = (C.rowmask >> lane) & 1u;
+        const int ci = __popc(C.rowmask & ((1u << lane) - 1u));
+        float* out = tiles + b * kTile;
+        for (int j = 0; j < 32; ++j)
+            out[j * 32 + lane] = (has && j < C.w) ? panels[C.panel_off + (int64_t)j * C.ld + ci] : 0.f;
+    }
+}
+
+// Upper tiles: warp per block, lane = block row i; tile[i][c] = L[row i,
+// unit column c] = panels[src + c * ld + i].
+__global__ void expand_upper_kernel(const int64_t* __restrict__ src, const int32_t* __restrict__ ld,
+                                    const int32_t* __restrict__ nrw, int64_t n, const float* __restrict__ panels,
+                                    float* __restrict__ tiles) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < n; b += nw) {
+        const int nr = nrw[b] & 0xffff, w = nrw[b] >> 16;
+        const int64_t s0 = src[b];
+        const int l = ld[b];
+        float* out = tiles + b * kTile;
+        for (int c = 0; c < 32; ++c)
+            out[lane * 32 + c] = (lane < nr && c < w) ? panels[s0 + (int64_t)c * l + lane] : 0.f;
+    }
+}
+
+int expand_grid(int64_t n) {
+    const int64_t blocks = (n * 32 + 255) / 256;
+    return (int)(blocks < 4096 ? (blocks > 0 ? blocks : 1) : 4096);
+}
+
+}  // namespace
+
+cudaError_t launch_snb_sweep(const SnbArgs& a, bool lower, SweepIO io, cudaStream_t stream) {
+    if (a.nitems == 0) return cudaSuccess;
+    if (!snb_supported(a.nrhs)) return cudaErrorInvalidValue;
+    switch (io) {
+        case SweepIO::F32: return launch_snb_io<SnbIO<float, false>>(a, lower, stream);
+        case SweepIO::F32_MIXED: return launch_snb_io<SnbIO<double, false>>(a, lower, stream);
+        case SweepIO::F32_REFINE: return launch_snb_io<SnbIO<double, true>>(a, lower, stream);
+        default: return cudaErrorInvalidValue;  // FP64 solves use solve_sn.cu
+    }
+}
+
+cudaError_t launch_snb_expand_lower(const SnContrib* contribs, int64_t n, const float* panels, float* tiles,
+                                    cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    expand_lower_kernel<<<expand_grid(n), 256, 0, stream>>>(contribs, n, panels, tiles);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_snb_expand_upper(const int64_t* src, const int32_t* ld, const int32_t* nrw, int64_t n,
+                                    const float* panels, float* tiles, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    expand_upper_kernel<<<expand_grid(n), 256, 0, stream>>>(src, ld, nrw, n, panels, tiles);
+    return cudaGetLastError();
+}
+
+}  // namespace gbchol

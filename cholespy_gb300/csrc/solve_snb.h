@@ -1,0 +1,56 @@
+// Launch interface of the bulk-copy supernodal sweeps (solve_snb.cu): the
+// FP32 top-region sweeps for many right-hand sides.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "host/plan.h"
+#include "kernels.h"
+
+namespace gbchol {
+
+struct SnbArgs {
+    const SnUnit* units = nullptr;
+    const SnContrib* contribs = nullptr;
+    const int32_t* order = nullptr;     // tickets: unit u, or (lower sweep) partial sum p as ~p
+    const float* lo_tiles = nullptr;    // per contribution block: 32 x 32, [source column][unit row]
+    const float* up_tiles = nullptr;    // per upper block: 32 x 32, [block row][unit column]
+    const int32_t* up_begin = nullptr;  // per unit: first upper block (n_units + 1 entries)
+    const int32_t* up_rows = nullptr;   // per upper block: 32 work-array rows (-1 past the block)
+    const int32_t* up_dep = nullptr;    // per upper block: the unit whose flag it waits for
+    const int32_t* unit_info = nullptr; // lower: per unit, first block it applies itself, first / end partial
+    const SnPartial* parts = nullptr;   // lower: partial sums over contribution ranges
+    float* pbuf = nullptr;              // lower: partial-sum slots, 32 x nrhs each
+    int n_units = 0;                    // partial p's flag follows the units': n_units + p
+    const float* dinv = nullptr;        // per unit: D^-1, M_lo, M_up (32 x 32, column-major each)
+    const int32_t* perm = nullptr;
+    float* tmp = nullptr;               // n x nrhs work array (permuted space), 16-byte aligned
+    void* out = nullptr;                // upper sweep: the solution, through perm (TOut)
+    int* uflags = nullptr;              // completion flags: units, then partial sums
+    int nrhs = 0;
+    int nitems = 0;                     // lower: n_units + partial sums; upper: n_units
+    int* epoch = nullptr;               // device sweep counter: read at start, +1 by the last CTA out
+    int* status = nullptr;
+    const int* skip = nullptr;
+    int* counters = nullptr;            // [ticket, exited CTAs], zero between launches
+};
+
+// The bulk sweeps take RHS counts above 32 that are multiples of 4 (rows of
+// the work array are copied in 16-byte units); one work item holds every
+// RHS column of its unit.
+inline bool snb_supported(int nrhs) { return nrhs > 32 && nrhs <= 128 && nrhs % 4 == 0; }
+// Shared-memory width of a work item: 64 columns up to 64 RHS, else 128.
+inline int snb_width(int nrhs) { return nrhs <= 64 ? 64 : 128; }
+
+cudaError_t launch_snb_sweep(const SnbArgs& a, bool lower, SweepIO io, cudaStream_t stream);
+
+// Expands the FP32 panels into the sweeps' 32 x 32 tiles (zero outside a
+// block's rows and columns). Lower tiles: one per contribution block.
+// Upper tiles: one per (panel offset, leading dimension, rows | columns << 16).
+cudaError_t launch_snb_expand_lower(const SnContrib* contribs, int64_t n, const float* panels, float* tiles,
+                                    cudaStream_t stream);
+cudaError_t launch_snb_expand_upper(const int64_t* src, const int32_t* ld, const int32_t* nrw, int64_t n,
+                                    const float* panels, float* tiles, cudaStream_t stream);
+
+}  // namespace gbchol

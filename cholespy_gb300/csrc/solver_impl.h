@@ -15,6 +15,7 @@
 #include "kernels.h"
 #include "refine.h"
 #include "solve_sn.h"
+#include "solve_snb.h"
 
 namespace gbchol {
 
@@ -136,6 +137,16 @@ struct gbchol_solver {
     DevBuf<int32_t> unit_of_row;         // unit holding each top row
     DevBuf<float> dinv32;
     DevBuf<double> dinv64;    // inverse diagonal blocks of the units
+    // bulk supernodal sweeps (FP32, 33..128 RHS): expanded 32 x 32 L tiles,
+    // the upper sweep's block lists, the lower sweep's partial sums and both
+    // ticket orders (solve_snb.cu)
+    DevBuf<float> snb_lo_tiles, snb_up_tiles;
+    DevBuf<int32_t> snb_up_begin, snb_up_dep, snb_up_rows;
+    DevBuf<int32_t> snb_unit_info, snb_order_lo, snb_order_up;
+    DevBuf<SnPartial> snb_parts;
+    int32_t snb_nparts = 0;
+    bool snb_ready = false;
+    int32_t snb_min_rhs = 33;  // RHS counts from here on use the bulk sweeps (when supported)
     DevBuf<int32_t> counters; // [ticket, exits] per sweep kernel (5 kernels)
     DevBuf<int32_t> dev_epoch;  // sweep counter of the solve kernels (device-resident)
     std::vector<int32_t> flags_init;  // 0 for leaf rows, INT_MAX for top rows

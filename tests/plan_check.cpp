@@ -333,13 +333,61 @@ bool check_transpose() {
     return ok;
 }
 
+// The bulk sweeps' schedule (build_snb_upper / build_snb_lower): every item
+// waits only on items with earlier tickets, the partial sums of a unit cover
+// the start of its block list exactly (in order, no gaps or overlaps), and the
+// upper blocks of a unit are the blocks of the 32-column sweep in its order.
+int check_snb(const SolvePlan& P, const SnbOptions& o) {
+    int bad = 0;
+    SnbUpperPlan B;
+    build_snb_upper(P, B);
+    SnbLowerPlan L;
+    build_snb_lower(P, B, o, L);
+    const int32_t nu = (int32_t)P.units.size(), np = (int32_t)L.parts.size();
+    if ((int32_t)L.order_lo.size() != nu + np || (int32_t)L.order_up.size() != nu) return 1;
+    std::vector<int32_t> tu((size_t)nu, -1), tp((size_t)np, -1), tup((size_t)nu, -1);
+    for (int32_t t = 0; t < nu + np; ++t) {
+        const int32_t v = L.order_lo[t];
+        if (v >= 0) tu[v] = t;
+        else tp[~v] = t;
+    }
+    for (int32_t t = 0; t < nu; ++t) tup[L.order_up[t]] = t;
+    for (int32_t u = 0; u < nu; ++u) {
+        const SnUnit& U = P.units[u];
+        const int32_t first = L.unit_info[(size_t)u * 3], pb = L.unit_info[(size_t)u * 3 + 1],
+                      pe = L.unit_info[(size_t)u * 3 + 2];
+        int32_t at = U.contrib_begin;
+        for (int32_t q = pb; q < pe; ++q) {
+            bad += L.parts[q].unit != u || L.parts[q].contrib_begin != at ||
+                   L.parts[q].contrib_end <= L.parts[q].contrib_begin;
+            at = L.parts[q].contrib_end;
+            bad += tp[q] < 0 || tp[q] >= tu[u];
+            for (int32_t e = L.parts[q].contrib_begin; e < L.parts[q].contrib_end; ++e)
+                bad += tu[P.contribs[e].src_unit] >= tp[q];
+        }
+        bad += at != first || first > U.contrib_end;
+        for (int32_t e = first; e < U.contrib_end; ++e) bad += tu[P.contribs[e].src_unit] >= tu[u];
+        const int32_t wj = U.pos0 + U.w, nrb = (U.ld - U.sn_w + kChunk - 1) / kChunk;
+        const int32_t nlater = (U.sn_w - wj + kChunk - 1) / kChunk, chain = wj < U.sn_w ? 1 : 0;
+        bad += B.begin[u + 1] - B.begin[u] != nrb + nlater - chain;
+        for (int32_t t = B.begin[u]; t < B.begin[u + 1]; ++t) {
+            bad += tup[B.dep[t]] >= tup[u];
+            const int32_t nr = B.nrw[t] & 0xffff, w = B.nrw[t] >> 16;
+            bad += nr < 1 || nr > kChunk || w != U.w;
+            for (int32_t i = 0; i < kChunk; ++i) bad += (B.rows[(size_t)t * kChunk + i] >= 0) != (i < nr);
+        }
+        if (chain) bad += tup[u + 1] >= tup[u];
+    }
+    return bad;
+}
+
 int main() {
     if (!check_transpose()) return 1;
     struct Case { int dim, k, minw, keep, group; };
     const Case cases[] = {
         {2, 8, 1, 16, 32},  {2, 20, 4, 16, 32}, {2, 20, 8, 2, 3},   {2, 40, 1, 1, 2},
         {3, 8, 1, 2, 3},    {3, 14, 4, 16, 32}, {3, 14, 8, 4, 5},   {3, 18, 8, 16, 32},
-        {3, 18, 8, 0, 0},   {3, 14, 100000, 16, 32},
+        {3, 18, 8, 0, 0},   {3, 14, 100000, 16, 32}, {2, 40, 1, 0, 0}, {3, 14, 4, 0, 0},
     };
     int failed = 0;
     for (const Case& cs : cases) {
@@ -369,6 +417,14 @@ int main() {
         po.part_keep = cs.keep;
         po.part_group = cs.group;
         build_plan(F, lo, up, po, P);
+        if (cs.group == 0) {  // the bulk schedule is built on plans without 32-column partial sums
+            for (const SnbOptions& so : {SnbOptions{}, SnbOptions{2, 3, 1000, 3000, 500}, SnbOptions{0, 1, 10, 10, 10}}) {
+                const int bad = check_snb(P, so);
+                std::printf("%dD k=%d minw=%d bulk keep=%d group=%d: checks failed %d %s\n", cs.dim, cs.k, cs.minw,
+                            so.keep, so.group, bad, bad ? "FAIL" : "ok");
+                failed += bad != 0;
+            }
+        }
         for (int r : {1, 3}) {
             errors = 0;
             const double rel = run_case(F, P, r);

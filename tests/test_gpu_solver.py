@@ -472,3 +472,51 @@ def test_refined_solve_nonfinite_rhs_never_converges(cuda, where):
     b2 = np.random.default_rng(6).standard_normal((n, 4))
     st2 = s.solve_refined(torch.tensor(b2, device="cuda"), xt, tol=1e-10, max_iter=3)
     assert st2.converged and st2.max_rel_residual <= 1e-10
+
+
+@pytest.mark.parametrize("name", ["grid3d_16", "ico4"])
+@pytest.mark.parametrize("group", ["0", "3"])
+def test_bulk_sweeps_match_oracle_and_narrow(cuda, name, group, monkeypatch):
+    """The bulk-copy supernodal sweeps (FP32, 33..128 RHS in multiples of 4:
+    one work item per unit holding every RHS column) against the oracle's
+    FP32/FP64 sweeps and against the 32-column sweeps of a second solver on
+    the same matrix (GBCHOL_BULK_MIN_RHS=129 keeps it on them), both
+    shared-memory widths, with and without lower-sweep partial sums
+    (GBCHOL_BULK_GROUP), plain FP32 and the refined solve's mixed-precision
+    sweeps."""
+    from cholespy_gb300 import CholeskySolverD, CholeskySolverF, MatrixType
+    torch = cuda
+    n, vals, idx = PROBLEMS[name]()
+    monkeypatch.setenv("GBCHOL_BULK_GROUP", group)
+    monkeypatch.setenv("GBCHOL_BULK_KEEP", "2")
+    s_bulk = _make(torch, n, vals, idx, CholeskySolverF)
+    sr = CholeskySolverD(n, torch.tensor(idx[0], device="cuda"), torch.tensor(idx[1], device="cuda"),
+                         torch.tensor(vals, device="cuda"), MatrixType.COO, refine=True)
+    monkeypatch.setenv("GBCHOL_BULK_MIN_RHS", "129")
+    s_narrow = _make(torch, n, vals, idx, CholeskySolverF)
+    perm, colptr, rowidx, lv = s_bulk.factor()
+    for nrhs in (36, 64, 68, 100, 128):
+        b = np.random.default_rng(nrhs).standard_normal((n, nrhs))
+        bt = torch.tensor(b.astype(np.float32), device="cuda")
+        x1, x2 = torch.zeros_like(bt), torch.zeros_like(bt)
+        s_bulk.solve(bt, x1)
+        s_narrow.solve(bt, x2)
+        s_bulk.check()
+        s_narrow.check()
+        x1h, x2h = x1.cpu().numpy().astype(np.float64), x2.cpu().numpy().astype(np.float64)
+        xo64 = oracle.reference_solve(perm, colptr, rowidx, lv, b, np.float64)
+        xo32 = oracle.reference_solve(perm, colptr, rowidx, lv, b.astype(np.float32), np.float32)
+        scale = np.abs(xo64).max()
+        err_b = np.abs(x1h - xo64).max() / scale
+        err_o = np.abs(xo32 - xo64).max() / scale
+        assert err_b <= 4 * err_o + 1e-6, (nrhs, err_b, err_o)
+        assert np.abs(x1h - x2h).max() / scale <= 1e-5
+    # refined solve (FP32 sweeps reading FP64 b, adding into FP64 x)
+    b = np.random.default_rng(7).standard_normal((n, 128))
+    bt = torch.tensor(b, device="cuda")
+    xt = torch.zeros_like(bt)
+    st = sr.solve_refined(bt, xt, tol=1e-10, max_iter=5)
+    assert st.converged
+    A = sym_matrix(n, vals, idx)
+    res = np.linalg.norm(b - A @ xt.cpu().numpy(), axis=0) / np.linalg.norm(b, axis=0)
+    assert res.max() <= 1e-10

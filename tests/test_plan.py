@@ -1,7 +1,8 @@
 """Host-side check of the supernodal solve plan (no GPU): tests/plan_check.cpp
 runs every sweep item in ticket order on the CPU and checks each wait, the
 partial sums of the lower sweep and the solution; it also checks the
-multi-threaded CSC transpose against a serial one for several thread counts."""
+multi-threaded CSC transpose against a serial one for several thread counts,
+and the bulk sweeps' schedule (tickets, partial-sum coverage, upper blocks)."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -20,4 +21,5 @@ def test_plan_schedule_and_solution(tmp_path):
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     p = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
     assert p.returncode == 0, p.stdout[-4000:] + p.stderr[-2000:]
-    assert p.stdout.count(" ok") == 21, p.stdout
+    # 12 plans x 2 RHS counts, the transpose check, 3 plans x 3 bulk schedules
+    assert "FAIL" not in p.stdout and p.stdout.count(" ok") == 34, p.stdout
