@@ -129,8 +129,11 @@ struct SnbOptions {
     int32_t keep = 16;
     int32_t group = 0;        // 0: no partial sums
     int64_t lat_ns = 1000;    // flag latency
-    int64_t base_ns = 3000;   // fixed cost of an item (diagonal solve, chain step)
-    int64_t blk_ns = 500;     // cost of one block
+    int64_t base_ns = 5000;   // fixed cost of an item (diagonal solve, chain step)
+    // cost of one block. Measured at 64^3, 128 RHS (5.99 / 5.87 / 5.79 /
+    // 5.73 / 5.75 ms per solve for 2.5 / 4 / 6 / 9 / 15 us): a long list is
+    // best started as soon as its first source is done, ahead of the estimate.
+    int64_t blk_ns = 9000;
 };
 
 struct SnbLowerPlan {

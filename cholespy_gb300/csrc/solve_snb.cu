@@ -12,7 +12,8 @@
 // * L blocks are pre-expanded 32 x 32 tiles (zero outside the block's rows
 //   and columns): lower sweep, one per contribution block, [source
 //   column][unit row]; upper sweep, one per off-diagonal block of the
-//   unit's supernode, [block row][unit column]. A tile is one 4 KB bulk copy.
+//   unit's supernode, [block row][unit column]. The rows of a tile that the
+//   block has (its source columns / block rows) are one bulk copy.
 // * A producer warp takes the tickets (running up to one item ahead of the
 //   consumers through two descriptor slots) and streams each item's blocks
 //   through a 4-stage shared-memory ring with cp.async.bulk: per block,
@@ -208,14 +209,15 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                         if (!ready) dev::wait_geq(a.uflags + src, epoch, a.status);
                         sm.ext[s] = rows;
                         sm.mask[s] = mask;
-                        bulk::mbar_arrive_expect_tx(&sm.full[s], (uint32_t)((kTile + rows * nrhs) * 4));
+                        bulk::mbar_arrive_expect_tx(&sm.full[s], (uint32_t)(rows * (32 + nrhs) * 4));
                     }
                     __syncwarp();
                     // the source rows were published under the flag: order the
                     // bulk (async-proxy) reads after its acquire
                     bulk::fence_proxy_async_global();
                     const float* ltile = (LOWER ? a.lo_tiles : a.up_tiles) + (size_t)t * kTile;
-                    if (lane == 0) bulk::copy_g2s(&sm.st[s].l[0][0], ltile, kTile * 4, &sm.full[s]);
+                    // the tile's first `rows` rows: the rest is zero and unread
+                    if (lane == 0) bulk::copy_g2s(&sm.st[s].l[0][0], ltile, (uint32_t)rows * 32 * 4, &sm.full[s]);
                     if (start)
                         bulk::copy_g2s(&sm.st[s].x[lane * nrhs], a.tmp + (size_t)row * nrhs,
                                        (uint32_t)(run * nrhs) * 4, &sm.full[s]);
@@ -280,7 +282,28 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                 // 4-row groups of my rows (columns) the block has: the others hold zeros
                 const unsigned grp = sm.mask[s] >> r0;
                 const SnbStage<SW>& st = sm.st[s];
-                for (int j = 0; j < ext; ++j) {
+                int j = 0;
+                // four block rows at a time: their loads go out together
+                for (; j + 4 <= ext; j += 4) {
+                    float xj[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) xj[u] = st.x[(j + u) * nrhs + k];
+#pragma unroll
+                    for (int q = 0; q < NR / 4; ++q) {
+                        if (!((grp >> (4 * q)) & 0xFu)) continue;  // warp-uniform
+                        float4 lv[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) lv[u] = reinterpret_cast<const float4*>(&st.l[j + u][r0])[q];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            acc[4 * q] = fmaf(lv[u].x, xj[u], acc[4 * q]);
+                            acc[4 * q + 1] = fmaf(lv[u].y, xj[u], acc[4 * q + 1]);
+                            acc[4 * q + 2] = fmaf(lv[u].z, xj[u], acc[4 * q + 2]);
+                            acc[4 * q + 3] = fmaf(lv[u].w, xj[u], acc[4 * q + 3]);
+                        }
+                    }
+                }
+                for (; j < ext; ++j) {
                     const float xv = st.x[j * nrhs + k];
                     const float4* lr = reinterpret_cast<const float4*>(&st.l[j][r0]);
 #pragma unroll
