@@ -182,6 +182,7 @@ int setup_snb(gbchol_solver* h) {
     h->snb_up_tiles.release();
     if (!(h->store & GBCHOL_STORE_F32) || P.units.empty() || !P.parts.empty()) return GBCHOL_OK;
     if (const char* env = std::getenv("GBCHOL_BULK_MIN_RHS")) h->snb_min_rhs = std::atoi(env);
+    if (const char* env = std::getenv("GBCHOL_BULK_TC")) h->snb_tc = std::atoi(env) != 0;
     SnbUpperPlan B;
     build_snb_upper(P, B);
     SnbOptions so;
@@ -434,6 +435,7 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
         b.tmp = static_cast<float*>(work);
         b.uflags = h->uflags.p;
         b.nrhs = nrhs;
+        b.tensor_cores = h->snb_tc ? 1 : 0;
         b.status = h->status.p;
         b.skip = skip;
         b.epoch = h->dev_epoch.p;

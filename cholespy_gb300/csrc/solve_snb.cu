@@ -41,6 +41,7 @@
 #include "device.cuh"
 #include "launch.h"
 #include "solve_snb.h"
+#include "tcgen05.cuh"
 
 namespace gbchol {
 
@@ -48,8 +49,13 @@ namespace {
 
 constexpr int kCW = 8;                    // consumer warps
 constexpr int kThreads = (kCW + 1) * 32;  // + one producer warp
-constexpr int kStages = 4;
 constexpr int kTile = 32 * 32;
+// Ring stages: 4 for the CUDA-core consumers, 2 with the tensor-core
+// operand buffers (two CTAs per SM either way).
+template <bool TC>
+struct SnbRing {
+    static constexpr int S = TC ? 2 : 4;
+};
 
 template <int SW>
 struct SnbStage {
@@ -57,8 +63,25 @@ struct SnbStage {
     float x[32 * SW];  // the block's rows of the work array, row stride = the RHS count
 };
 
-template <int SW>
+// Tensor-core operands of one block (canonical K-major layout, tcgen05.cuh):
+// A = the block's work-array rows transposed (128 RHS columns x 32), B = the
+// L tile (32 unit rows / columns x 32), each split into TF32 high and low
+// parts.
+template <bool TC>
+struct SnbTc {};
+template <>
+struct SnbTc<true> {
+    __align__(1024) float a_hi[128 * 32];
+    __align__(1024) float a_lo[128 * 32];
+    __align__(1024) float b_hi[32 * 32];
+    __align__(1024) float b_lo[32 * 32];
+    uint64_t mma_done;  // one phase per block: its MMAs have completed
+    uint32_t tmem;      // accumulator: 128 lanes x 32 columns
+};
+
+template <int SW, bool TC>
 struct SnbSmem {
+    static constexpr int kStages = SnbRing<TC>::S;
     SnbStage<SW> st[kStages];
     float t[32][SW];   // t' = t - sum of the blocks (right-hand side of the diagonal solve)
     float e[32][32];   // e[j][i] = E[i][j]
@@ -69,6 +92,7 @@ struct SnbSmem {
     int item_v[2], item_valid[2];
     int ext[kStages];        // rows of the stage's x block (lower: source columns, upper: block rows)
     unsigned mask[kStages];  // unit rows (lower) / columns (upper) the block has
+    SnbTc<TC> tc;
 };
 
 template <typename TO, bool ACCUM>
@@ -105,10 +129,72 @@ __device__ __forceinline__ SnbItem snb_item(const SnbArgs& a, int v, const SnUni
     return it;
 }
 
-template <class io, bool LOWER, int SW>
+// The consumers' conversion of one landed stage into the tensor-core
+// operands: A(k, j) = x[j][k] (RHS column k, block row j), B(n, j) =
+// tile[j][n], each value v as hi = tf32(v), lo = tf32(v - hi); zero past the
+// block's `ext` rows and the RHS count. Thread t: A for RHS column t % 128
+// and row groups t / 128 + 2q; B for unit row / column t % 32 and row group t / 32.
+template <int SW>
+__device__ __forceinline__ void snb_split(const SnbStage<SW>& st, SnbTc<true>& tb, int ext, int nrhs, int tid) {
+    const int ka = tid & 127;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int jg = (tid >> 7) + 2 * q;  // rows 4 jg .. 4 jg + 3
+        float4 hi, lo;
+        float* h = &hi.x;
+        float* l = &lo.x;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = 4 * jg + u;
+            const float v = (j < ext && ka < nrhs) ? st.x[j * nrhs + ka] : 0.f;
+            h[u] = tc::to_tf32(v);
+            l[u] = tc::to_tf32(v - h[u]);
+        }
+        const int off = (ka >> 3) * 256 + jg * 32 + (ka & 7) * 4;  // floats: SBO 1024 B, LBO 128 B
+        *reinterpret_cast<float4*>(&tb.a_hi[off]) = hi;
+        *reinterpret_cast<float4*>(&tb.a_lo[off]) = lo;
+    }
+    {
+        const int nb = tid & 31, jg = tid >> 5;
+        float4 hi, lo;
+        float* h = &hi.x;
+        float* l = &lo.x;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = 4 * jg + u;
+            const float v = j < ext ? st.l[j][nb] : 0.f;
+            h[u] = tc::to_tf32(v);
+            l[u] = tc::to_tf32(v - h[u]);
+        }
+        const int off = (nb >> 3) * 256 + jg * 32 + (nb & 7) * 4;
+        *reinterpret_cast<float4*>(&tb.b_hi[off]) = hi;
+        *reinterpret_cast<float4*>(&tb.b_lo[off]) = lo;
+    }
+}
+
+// One block on the tensor cores (one thread): D += A_lo B_hi + A_hi B_lo +
+// A_hi B_hi over K = 32 in steps of 8 (3 x 4 MMAs of 128 x 32 x 8).
+__device__ __forceinline__ void snb_mma(SnbTc<true>& tb, bool first) {
+    constexpr uint32_t idesc = tc::idesc_tf32(128, 32);
+    const float* as[3] = {tb.a_lo, tb.a_hi, tb.a_hi};
+    const float* bs[3] = {tb.b_hi, tb.b_lo, tb.b_hi};
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+            const uint64_t ad = tc::smem_desc(as[p] + ks * 64, 128, 1024);
+            const uint64_t bd = tc::smem_desc(bs[p] + ks * 64, 128, 1024);
+            tc::mma_tf32(tb.tmem, ad, bd, idesc, (first && p == 0 && ks == 0) ? 0u : 1u);
+        }
+    }
+    tc::commit(&tb.mma_done);
+}
+
+template <class io, bool LOWER, int SW, bool TC>
 __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    SnbSmem<SW>& sm = *reinterpret_cast<SnbSmem<SW>*>(smem_raw);
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    SnbSmem<SW, TC>& sm = *reinterpret_cast<SnbSmem<SW, TC>*>(smem_raw);
+    constexpr int kStages = SnbRing<TC>::S;
     if (a.skip && dev::ld_volatile(a.skip)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // every CTA reads the sweep's epoch before the last CTA out bumps it
@@ -122,9 +208,15 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             bulk::mbar_init(&sm.item_full[s], 1);
             bulk::mbar_init(&sm.item_empty[s], kCW);
         }
+        if constexpr (TC) bulk::mbar_init(&sm.tc.mma_done, 1);
         bulk::fence_mbar_init();
     }
+    if constexpr (TC) {
+        if (warp == 0) tc::alloc(&sm.tc.tmem, 32);
+        tc::fence_before_sync();
+    }
     __syncthreads();
+    if constexpr (TC) tc::fence_after_sync();
     const int nrhs = a.nrhs;
     if (warp == kCW) {
         // ---- producer: tickets, then the item's blocks into the stage ring
@@ -237,7 +329,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
     } else {
         // ---- consumers: thread = one RHS column k and NR unit rows (lower)
         // / columns (upper) from r0
-        constexpr int G = SW / 32;        // consumer warps across the RHS columns
+        constexpr int G = TC ? 4 : SW / 32;  // consumer warps across the RHS columns (TC: 128 accumulator lanes)
         constexpr int NR = 32 * G / kCW;  // rows / columns per consumer thread
         const int k = 32 * (warp % G) + lane;
         const int r0 = NR * (warp / G);
@@ -245,6 +337,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
         for (uint32_t n = 0;; ++n) {
             const int slot = (int)(n & 1);
             bulk::mbar_wait(&sm.item_full[slot], (n >> 1) & 1, a.status);
+            static_assert(!TC || (SW == 128 && 32 * 4 / kCW == 16), "tensor-core mapping: 128 lanes x 16 columns");
             if (!sm.item_valid[slot]) break;
             const int v = sm.item_v[slot];
             const SnUnit U = sm.item_unit[slot];
@@ -278,6 +371,20 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                 const uint32_t g = gs + (uint32_t)b;
                 const int s = (int)(g % kStages);
                 bulk::mbar_wait(&sm.full[s], (g / kStages) & 1, a.status);
+                if constexpr (TC) {
+                    // the previous block's MMAs have read the operand buffers
+                    if (g > 0) bulk::mbar_wait(&sm.tc.mma_done, (g - 1) & 1, a.status);
+                    snb_split<SW>(sm.st[s], sm.tc, sm.ext[s], nrhs, tid);
+                    tc::fence_proxy_async_smem();
+                    __syncwarp();
+                    if (lane == 0) bulk::mbar_arrive(&sm.empty[s]);  // the stage is free again
+                    bulk::named_sync(1, kCW * 32);
+                    if (tid == 0) {
+                        tc::fence_after_sync();
+                        snb_mma(sm.tc, b == 0);
+                    }
+                    continue;
+                }
                 const int ext = sm.ext[s];
                 // 4-row groups of my rows (columns) the block has: the others hold zeros
                 const unsigned grp = sm.mask[s] >> r0;
@@ -320,6 +427,14 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                 if (lane == 0) bulk::mbar_arrive(&sm.empty[s]);
             }
             gs += (uint32_t)it.nblk;
+            if constexpr (TC) {
+                if (it.nblk > 0) {  // the accumulator: my 16 columns of lane k
+                    bulk::mbar_wait(&sm.tc.mma_done, (gs - 1) & 1, a.status);
+                    tc::fence_after_sync();
+                    tc::ld16(sm.tc.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)r0, acc);
+                    tc::fence_before_sync();  // ordered before the next item's MMAs (barriers below)
+                }
+            }
             if (it.part) {  // the sum goes to the partial's slot, then its flag
                 float* ps = a.pbuf + (size_t)(~v) * 32 * nrhs;
                 if (k < nrhs) {
@@ -405,8 +520,18 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             bulk::named_sync(1, kCW * 32);
             if (tid == 0) dev::st_release(a.uflags + uidx, epoch);
         }
+        if constexpr (TC) {
+            // every MMA has completed before the accumulator is freed (the
+            // consumers waited for each item's last one; this matters only
+            // after an abandoned wait)
+            if (tid == 0 && gs > 0) bulk::mbar_wait(&sm.tc.mma_done, (gs - 1) & 1, a.status, false);
+        }
     }
     __syncthreads();
+    if constexpr (TC) {
+        tc::fence_after_sync();
+        if (warp == 0) tc::dealloc(sm.tc.tmem, 32);
+    }
     // the last CTA out resets the ticket and advances the epoch for the next
     // launch (the launch boundary orders these writes)
     if (tid == 0) {
@@ -419,23 +544,25 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
     }
 }
 
-template <class io, bool LOWER, int SW>
+template <class io, bool LOWER, int SW, bool TC>
 cudaError_t launch_snb(const SnbArgs& a, cudaStream_t stream) {
-    const void* fn = (const void*)snb_sweep_kernel<io, LOWER, SW>;
-    const size_t smem = sizeof(SnbSmem<SW>);
+    const void* fn = (const void*)snb_sweep_kernel<io, LOWER, SW, TC>;
+    const size_t smem = sizeof(SnbSmem<SW, TC>);
     int grid = 0;
     cudaError_t e = coop_grid(fn, kThreads, smem, &grid);  // resident CTAs: a persistent grid
     if (e != cudaSuccess) return e;
     if (grid > a.nitems) grid = a.nitems;
-    snb_sweep_kernel<io, LOWER, SW><<<grid, kThreads, smem, stream>>>(a);
+    snb_sweep_kernel<io, LOWER, SW, TC><<<grid, kThreads, smem, stream>>>(a);
     return cudaGetLastError();
 }
 
 template <class io>
 cudaError_t launch_snb_io(const SnbArgs& a, bool lower, cudaStream_t stream) {
+    if (a.tensor_cores)
+        return lower ? launch_snb<io, true, 128, true>(a, stream) : launch_snb<io, false, 128, true>(a, stream);
     if (snb_width(a.nrhs) == 64)
-        return lower ? launch_snb<io, true, 64>(a, stream) : launch_snb<io, false, 64>(a, stream);
-    return lower ? launch_snb<io, true, 128>(a, stream) : launch_snb<io, false, 128>(a, stream);
+        return lower ? launch_snb<io, true, 64, false>(a, stream) : launch_snb<io, false, 64, false>(a, stream);
+    return lower ? launch_snb<io, true, 128, false>(a, stream) : launch_snb<io, false, 128, false>(a, stream);
 }
 
 // Lower tiles: warp per contribution block, lane = unit row i; tile[j][i] =

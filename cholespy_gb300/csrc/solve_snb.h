@@ -34,6 +34,7 @@ struct SnbArgs {
     int* status = nullptr;
     const int* skip = nullptr;
     int* counters = nullptr;            // [ticket, exited CTAs], zero between launches
+    int tensor_cores = 0;               // 1: block products on the tensor cores (3 x TF32 split)
 };
 
 // The bulk sweeps take RHS counts above 32 that are multiples of 4 (rows of

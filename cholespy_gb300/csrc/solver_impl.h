@@ -147,6 +147,7 @@ struct gbchol_solver {
     int32_t snb_nparts = 0;
     bool snb_ready = false;
     int32_t snb_min_rhs = 33;  // RHS counts from here on use the bulk sweeps (when supported)
+    bool snb_tc = false;       // bulk sweeps: block products on the tensor cores
     DevBuf<int32_t> counters; // [ticket, exits] per sweep kernel (5 kernels)
     DevBuf<int32_t> dev_epoch;  // sweep counter of the solve kernels (device-resident)
     std::vector<int32_t> flags_init;  // 0 for leaf rows, INT_MAX for top rows

@@ -476,7 +476,8 @@ def test_refined_solve_nonfinite_rhs_never_converges(cuda, where):
 
 @pytest.mark.parametrize("name", ["grid3d_16", "ico4"])
 @pytest.mark.parametrize("group", ["0", "3"])
-def test_bulk_sweeps_match_oracle_and_narrow(cuda, name, group, monkeypatch):
+@pytest.mark.parametrize("tensor_cores", ["0", "1"])
+def test_bulk_sweeps_match_oracle_and_narrow(cuda, name, group, tensor_cores, monkeypatch):
     """The bulk-copy supernodal sweeps (FP32, 33..128 RHS in multiples of 4:
     one work item per unit holding every RHS column) against the oracle's
     FP32/FP64 sweeps and against the 32-column sweeps of a second solver on
@@ -489,6 +490,7 @@ def test_bulk_sweeps_match_oracle_and_narrow(cuda, name, group, monkeypatch):
     n, vals, idx = PROBLEMS[name]()
     monkeypatch.setenv("GBCHOL_BULK_GROUP", group)
     monkeypatch.setenv("GBCHOL_BULK_KEEP", "2")
+    monkeypatch.setenv("GBCHOL_BULK_TC", tensor_cores)
     s_bulk = _make(torch, n, vals, idx, CholeskySolverF)
     sr = CholeskySolverD(n, torch.tensor(idx[0], device="cuda"), torch.tensor(idx[1], device="cuda"),
                          torch.tensor(vals, device="cuda"), MatrixType.COO, refine=True)
@@ -509,6 +511,7 @@ def test_bulk_sweeps_match_oracle_and_narrow(cuda, name, group, monkeypatch):
         scale = np.abs(xo64).max()
         err_b = np.abs(x1h - xo64).max() / scale
         err_o = np.abs(xo32 - xo64).max() / scale
+        print(f"TCERR tc={tensor_cores} {name} nrhs={nrhs} err_bulk={err_b:.3e} err_oracle32={err_o:.3e}")
         assert err_b <= 4 * err_o + 1e-6, (nrhs, err_b, err_o)
         assert np.abs(x1h - x2h).max() / scale <= 1e-5
     # refined solve (FP32 sweeps reading FP64 b, adding into FP64 x)
