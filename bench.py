@@ -65,17 +65,38 @@ def parse_args():
 
 # ------------------------------------------------------------- helpers ----
 
-# DRAM bytes (read + write) of one FP32 solve, summed over its 5 sweep
+# DRAM bytes (read + write) of one FP32 solve, summed over its sweep
 # launches, from one ncu capture of `bench.py --workload solve` at the same
 # size (dram__bytes_read.sum + dram__bytes_write.sum; the per-kernel table
-# and the command are kept with the ncu summaries). Keyed by (k, nrhs).
-MEASURED_SOLVE_TRAFFIC_F32 = {(64, 128): 1922223616}
+# and the command are kept with the ncu summaries). Keyed by the solve plan's
+# signature (n, nnz(L), top-region units, contribution blocks, RHS count,
+# supernodal kernel): a plan or kernel that changed since the capture finds
+# no entry and reports null instead of a stale figure.
+MEASURED_SOLVE_TRAFFIC_F32 = {}
 
 
-def measured_traffic(args, f32=True):
+def plan_signature(info, nrhs):
+    kernel = "bulk" if (32 < nrhs <= 128 and nrhs % 4 == 0) else "sliced"
+    return (int(info.n), int(info.nnz_l), int(info.top_units), int(info.top_blocks), int(nrhs), kernel)
+
+
+def measured_traffic(info, nrhs, f32=True):
     if not f32:
         return None
-    return MEASURED_SOLVE_TRAFFIC_F32.get((args.k, args.nrhs))
+    return MEASURED_SOLVE_TRAFFIC_F32.get(plan_signature(info, nrhs))
+
+
+def cpu_rate(solve, rhs_per_call, min_seconds=10.0, min_calls=3):
+    """RHS-solves/s of a host solve: one untimed warm-up call, then calls
+    until at least min_seconds and min_calls have passed (a bounded sample)."""
+    solve()
+    calls, t0 = 0, time.perf_counter()
+    while True:
+        solve()
+        calls += 1
+        dt = time.perf_counter() - t0
+        if calls >= min_calls and dt >= min_seconds:
+            return rhs_per_call * calls / dt, calls, dt
 
 
 _FMA_PEAKS = {}
@@ -399,14 +420,15 @@ def run_ours(args, world, rank, local):
         cores = os.cpu_count() or 1
         sample = max(1, min(args.cpu_sample_rhs, args.nrhs))
         bs = np.ascontiguousarray(b[:, :sample])
-        c0 = time.perf_counter()
-        oracle.cpu_solve(perm, Lp, Li, Lx, bs, threads=cores)
-        cdt = time.perf_counter() - c0
-        cpu = {"value": sample / cdt, "unit": "RHS-solves/s", "cores": cores, "kind": "port",
-               "sample": f"{sample} of {args.nrhs} RHS columns, one FP64 solve "
-                         "(cholmod_solve semantics) on the same factor, RHS split over threads"}
+        rate, calls, cdt = cpu_rate(lambda: oracle.cpu_solve(perm, Lp, Li, Lx, bs, threads=cores), sample)
+        cpu = {"value": rate, "unit": "RHS-solves/s", "cores": cores, "kind": "port",
+               "sample": f"{sample} of {args.nrhs} RHS columns per call, FP64 solve (cholmod_solve "
+                         f"semantics) on the same factor, RHS split over threads; 1 warm-up + {calls} "
+                         f"timed calls, {cdt:.1f} s"}
 
-    lps = info.launches_per_solve
+    # the bulk supernodal sweeps (33..128 RHS, multiples of 4) add one launch:
+    # the scatter of the top rows' solution
+    lps = info.launches_per_solve + (1 if (32 < args.nrhs <= 128 and args.nrhs % 4 == 0) else 0)
     launches = lps + (args.max_iter + 1) + args.max_iter * lps
     line = {
         "metric": HEADLINE_METRIC,
@@ -428,7 +450,8 @@ def run_ours(args, world, rank, local):
                        "compute": compute_roofline(torch, n, info.nnz_l, args.nrhs, t_64 / args.steps, True)},
         "roofline": {"kernel": "triangular sweeps (FP32 solve, lower+upper)", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": measured_traffic(args),
+                     "frac": achieved / peak, "traffic": measured_traffic(info, args.nrhs),
+                     "plan_signature": list(plan_signature(info, args.nrhs)),
                      "algorithmic_bytes": bytes32, "ms_per_solve": 1e3 * t_32,
                      "compute": compute_roofline(torch, n, info.nnz_l, args.nrhs, t_32, False)},
         "e2e": {"value": e2e_value, "unit": "RHS-solves/s",
@@ -473,9 +496,9 @@ def _cpu_sample(perm, Lp, Li, Lx, b, nrhs_sample):
     import oracle
     cores = os.cpu_count() or 1
     bs = np.ascontiguousarray(b[:, :nrhs_sample])
-    c0 = time.perf_counter()
-    oracle.cpu_solve(perm, Lp, Li, Lx, bs, threads=cores)
-    return bs.shape[1] / (time.perf_counter() - c0), cores
+    rate, _, _ = cpu_rate(lambda: oracle.cpu_solve(perm, Lp, Li, Lx, bs, threads=cores), bs.shape[1],
+                          min_seconds=5.0)
+    return rate, cores
 
 
 def run_batch(args, world, rank, local):
@@ -726,7 +749,7 @@ def run_solve(args, world, rank, local):
                  roofline={"kernel": "triangular sweeps (lower+upper)", "bound": "hbm",
                            "achieved": byts / (t / args.steps) / 1e9, "peak": peak, "peak_kind": kind,
                            "unit": "GB/s", "frac": byts / (t / args.steps) / 1e9 / peak,
-                           "traffic": measured_traffic(args, not args.fp64),
+                           "traffic": measured_traffic(info, args.nrhs, not args.fp64),
                            "compute": compute_roofline(torch, n, info.nnz_l, args.nrhs, t / args.steps,
                                                        args.fp64),
                            "algorithmic_bytes": byts},

@@ -443,11 +443,13 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
         b.order = h->snb_order_lo.p;
         b.counters = h->counters.p + 2;
         CUDA_TRY(launch_snb_sweep(b, true, io, s));
-        b.out = out;
+        b.out = nullptr;  // the top rows' output is scattered afterwards, off the chain
         b.nitems = (int)P.units.size();
         b.order = h->snb_order_up.p;
         b.counters = h->counters.p + 4;
         CUDA_TRY(launch_snb_sweep(b, false, io, s));
+        b.out = out;
+        CUDA_TRY(launch_snb_scatter(b, (int)P.units.size(), io, s));
     } else {
         sn.sys0.n_units = (int)P.units.size();
         sn.sys0.nrhs = nrhs;

@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(kThreads) residual_kernel(ResidualArgs a) {
                 const double r = bv - acc[q];
                 a.r[o] = r;
                 rn[q] = fma(r, r, rn[q]);
-                bn[q] = fma(bv, bv, bn[q]);
+                if (a.first) bn[q] = fma(bv, bv, bn[q]);  // ||b|| once per refined solve
             }
         }
     }

@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                     const int i = r0 + r;
                     if (i < w) {
                         a.tmp[(size_t)(U.c0 + i) * nrhs + k] = xv[r];
-                        if (!LOWER) {
+                        if (!LOWER && a.out) {
                             using TO = typename io::tout;
                             TO* out = static_cast<TO*>(a.out);
                             const size_t oo = (size_t)a.perm[U.c0 + i] * nrhs + k;
@@ -599,6 +599,31 @@ __global__ void expand_upper_kernel(const int64_t* __restrict__ src, const int32
     }
 }
 
+// The top rows' part of the solution, out[perm[row]] = (or +=) tmp[row],
+// after the upper sweep (one CTA per unit, coalesced along each row).
+template <class io>
+__global__ void __launch_bounds__(256) scatter_kernel(const SnUnit* __restrict__ units, const int32_t* __restrict__ perm,
+                                                      const float* __restrict__ tmp, void* out_, int nrhs,
+                                                      const int* skip) {
+    if (skip && dev::ld_volatile(skip)) return;
+    using TO = typename io::tout;
+    TO* out = static_cast<TO*>(out_);
+    const SnUnit U = units[blockIdx.x];
+    for (int idx = threadIdx.x; idx < U.w * nrhs; idx += blockDim.x) {
+        const int i = idx / nrhs, k = idx - i * nrhs;
+        const size_t oo = (size_t)perm[U.c0 + i] * nrhs + k;
+        const TO v = (TO)tmp[(size_t)(U.c0 + i) * nrhs + k];
+        if (io::accum) out[oo] += v;
+        else out[oo] = v;
+    }
+}
+
+template <class io>
+cudaError_t launch_scatter_io(const SnbArgs& a, int nunits, cudaStream_t stream) {
+    scatter_kernel<io><<<nunits, 256, 0, stream>>>(a.units, a.perm, a.tmp, a.out, a.nrhs, a.skip);
+    return cudaGetLastError();
+}
+
 int expand_grid(int64_t n) {
     const int64_t blocks = (n * 32 + 255) / 256;
     return (int)(blocks < 4096 ? (blocks > 0 ? blocks : 1) : 4096);
@@ -614,6 +639,16 @@ cudaError_t launch_snb_sweep(const SnbArgs& a, bool lower, SweepIO io, cudaStrea
         case SweepIO::F32_MIXED: return launch_snb_io<SnbIO<double, false>>(a, lower, stream);
         case SweepIO::F32_REFINE: return launch_snb_io<SnbIO<double, true>>(a, lower, stream);
         default: return cudaErrorInvalidValue;  // FP64 solves use solve_sn.cu
+    }
+}
+
+cudaError_t launch_snb_scatter(const SnbArgs& a, int nunits, SweepIO io, cudaStream_t stream) {
+    if (nunits == 0) return cudaSuccess;
+    switch (io) {
+        case SweepIO::F32: return launch_scatter_io<SnbIO<float, false>>(a, nunits, stream);
+        case SweepIO::F32_MIXED: return launch_scatter_io<SnbIO<double, false>>(a, nunits, stream);
+        case SweepIO::F32_REFINE: return launch_scatter_io<SnbIO<double, true>>(a, nunits, stream);
+        default: return cudaErrorInvalidValue;
     }
 }
 

@@ -44,7 +44,11 @@ inline bool snb_supported(int nrhs) { return nrhs > 32 && nrhs <= 128 && nrhs % 
 // Shared-memory width of a work item: 64 columns up to 64 RHS, else 128.
 inline int snb_width(int nrhs) { return nrhs <= 64 ? 64 : 128; }
 
+// The upper sweep writes the output only when a.out is set; otherwise this
+// kernel writes the top rows' solution afterwards (out[perm[row]] = or +=
+// tmp[row]), off the sweep's dependency chain.
 cudaError_t launch_snb_sweep(const SnbArgs& a, bool lower, SweepIO io, cudaStream_t stream);
+cudaError_t launch_snb_scatter(const SnbArgs& a, int nunits, SweepIO io, cudaStream_t stream);
 
 // Expands the FP32 panels into the sweeps' 32 x 32 tiles (zero outside a
 // block's rows and columns). Lower tiles: one per contribution block.
