@@ -190,6 +190,9 @@ int setup_snb(gbchol_solver* h) {
     if (const char* env = std::getenv("GBCHOL_BULK_GROUP")) so.group = std::atoi(env);
     if (const char* env = std::getenv("GBCHOL_BULK_BLK_NS")) so.blk_ns = std::atoll(env);
     if (const char* env = std::getenv("GBCHOL_BULK_BASE_NS")) so.base_ns = std::atoll(env);
+    so.max_cols = snb_group_cols(h->snb_tc);
+    if (const char* env = std::getenv("GBCHOL_BULK_GROUP_COLS"))
+        so.max_cols = std::min(so.max_cols, std::max(32, std::atoi(env)));
     SnbLowerPlan L;
     build_snb_lower(P, B, so, L);
     const size_t nlo = P.contribs.size(), nup = B.dep.size();
@@ -201,6 +204,7 @@ int setup_snb(gbchol_solver* h) {
     CUDA_TRY(h->snb_up_dep.upload(B.dep.data(), B.dep.size()));
     CUDA_TRY(h->snb_up_rows.upload(B.rows.data(), B.rows.size()));
     CUDA_TRY(h->snb_unit_info.upload(L.unit_info.data(), L.unit_info.size()));
+    CUDA_TRY(h->snb_groups.upload(L.groups.data(), L.groups.size()));
     CUDA_TRY(h->snb_parts.upload(L.parts.data(), L.parts.size()));
     CUDA_TRY(h->snb_order_lo.upload(L.order_lo.data(), L.order_lo.size()));
     CUDA_TRY(h->snb_order_up.upload(L.order_up.data(), L.order_up.size()));
@@ -426,6 +430,7 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
         b.up_begin = h->snb_up_begin.p;
         b.up_rows = h->snb_up_rows.p;
         b.up_dep = h->snb_up_dep.p;
+        b.groups = h->snb_groups.p;
         b.unit_info = h->snb_unit_info.p;
         b.parts = h->snb_parts.p;
         b.pbuf = reinterpret_cast<float*>(sn.sys0.pbuf);

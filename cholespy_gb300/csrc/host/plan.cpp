@@ -460,29 +460,49 @@ void build_snb_upper(const SolvePlan& P, SnbUpperPlan& B) {
 
 void build_snb_lower(const SolvePlan& P, const SnbUpperPlan& B, const SnbOptions& o, SnbLowerPlan& L) {
     const int32_t nunits = (int32_t)P.units.size();
-    L.unit_info.assign((size_t)nunits * 3, 0);
+    L.unit_info.assign((size_t)nunits * 4, 0);
     L.parts.clear();
+    L.groups.clear();
     for (int32_t u = 0; u < nunits; ++u) {
         const SnUnit& U = P.units[u];
         const int32_t chain = U.pos0 > 0 ? 1 : 0;
-        const int32_t nfree = U.contrib_end - U.contrib_begin - chain;
-        int32_t first = U.contrib_begin;
+        const int32_t end = U.contrib_end - chain;
+        const int32_t g0 = (int32_t)L.groups.size();
+        const int32_t own_c0 = U.c0 - U.pos0;  // first column of the unit's supernode
+        for (int32_t e = U.contrib_begin; e < end;) {
+            const SnContrib& C = P.contribs[e];
+            SnbGroup g{e, C.w, C.src_unit, C.xcol, C.rowmask};
+            int32_t f = e + 1;
+            const bool own = C.xcol >= own_c0 && C.xcol < U.c0;
+            while (!own && f < end && P.contribs[f - 1].w == kChunk && P.contribs[f].rowmask == C.rowmask &&
+                   P.contribs[f].src_unit == P.contribs[f - 1].src_unit + 1 &&
+                   P.contribs[f].xcol == P.contribs[f - 1].xcol + kChunk && g.cols + P.contribs[f].w <= o.max_cols) {
+                g.cols += P.contribs[f].w;
+                g.src_unit = P.contribs[f].src_unit;
+                ++f;
+            }
+            L.groups.push_back(g);
+            e = f;
+        }
+        const int32_t ng_u = (int32_t)L.groups.size() - g0;
+        int32_t first = g0;
         const int32_t pb = (int32_t)L.parts.size();
-        if (o.group > 0 && nfree > o.keep + o.group) {
-            const int32_t split = U.contrib_begin + nfree - o.keep;  // the unit keeps [split, end - chain)
-            const int32_t ng = (split - U.contrib_begin + o.group - 1) / o.group;
-            for (int32_t g = 0; g < ng; ++g) {  // equal shares of the split-off blocks
-                SnPartial q{};
-                q.unit = u;
-                q.contrib_begin = U.contrib_begin + (int32_t)((int64_t)(split - U.contrib_begin) * g / ng);
-                q.contrib_end = U.contrib_begin + (int32_t)((int64_t)(split - U.contrib_begin) * (g + 1) / ng);
-                L.parts.push_back(q);
+        if (o.group > 0 && ng_u > o.keep + o.group) {
+            const int32_t split = g0 + ng_u - o.keep;  // the unit keeps groups [split, end)
+            const int32_t np = (split - g0 + o.group - 1) / o.group;
+            for (int32_t q = 0; q < np; ++q) {  // equal shares of the split-off groups
+                SnPartial pp{};
+                pp.unit = u;
+                pp.contrib_begin = g0 + (int32_t)((int64_t)(split - g0) * q / np);
+                pp.contrib_end = g0 + (int32_t)((int64_t)(split - g0) * (q + 1) / np);
+                L.parts.push_back(pp);
             }
             first = split;
         }
-        L.unit_info[(size_t)u * 3] = first;
-        L.unit_info[(size_t)u * 3 + 1] = pb;
-        L.unit_info[(size_t)u * 3 + 2] = (int32_t)L.parts.size();
+        L.unit_info[(size_t)u * 4] = first;
+        L.unit_info[(size_t)u * 4 + 1] = (int32_t)L.groups.size();
+        L.unit_info[(size_t)u * 4 + 2] = pb;
+        L.unit_info[(size_t)u * 4 + 3] = (int32_t)L.parts.size();
     }
     // estimated starts (as in build_plan): an item should start when its work
     // before its last wait is just done as that wait ends; the key is that
@@ -507,16 +527,17 @@ void build_snb_lower(const SolvePlan& P, const SnbUpperPlan& B, const SnbOptions
     for (int32_t u = 0; u < nunits; ++u) {  // sources precede their destinations
         const SnUnit& U = P.units[u];
         Est eu;
-        for (int32_t q = L.unit_info[(size_t)u * 3 + 1]; q < L.unit_info[(size_t)u * 3 + 2]; ++q) {
+        for (int32_t q = L.unit_info[(size_t)u * 4 + 2]; q < L.unit_info[(size_t)u * 4 + 3]; ++q) {
             Est eq;
             for (int32_t e = L.parts[q].contrib_begin; e < L.parts[q].contrib_end; ++e)
-                eq.dep(fin_u[P.contribs[e].src_unit], key_u[P.contribs[e].src_unit], o.lat_ns);
+                eq.dep(fin_u[L.groups[e].src_unit], key_u[L.groups[e].src_unit], o.lat_ns);
             fin_p[q] = eq.done(L.parts[q].contrib_end - L.parts[q].contrib_begin, o.base_ns, o.blk_ns, key_p[q]);
             eu.dep(fin_p[q], key_p[q], o.lat_ns);
         }
-        for (int32_t e = L.unit_info[(size_t)u * 3]; e < U.contrib_end; ++e)
-            eu.dep(fin_u[P.contribs[e].src_unit], key_u[P.contribs[e].src_unit], o.lat_ns);
-        fin_u[u] = eu.done(U.contrib_end - L.unit_info[(size_t)u * 3], o.base_ns, o.blk_ns, key_u[u]);
+        const int32_t gf = L.unit_info[(size_t)u * 4], ge = L.unit_info[(size_t)u * 4 + 1];
+        for (int32_t e = gf; e < ge; ++e) eu.dep(fin_u[L.groups[e].src_unit], key_u[L.groups[e].src_unit], o.lat_ns);
+        if (U.pos0 > 0) eu.dep(fin_u[u - 1], key_u[u - 1], o.lat_ns);  // the chain unit
+        fin_u[u] = eu.done(ge - gf + (U.pos0 > 0 ? 1 : 0), o.base_ns, o.blk_ns, key_u[u]);
     }
     std::vector<int64_t> fin_up((size_t)nunits, 0), key_up((size_t)nunits, 0);
     for (int32_t u = nunits - 1; u >= 0; --u) {  // the upper sweep waits on later units

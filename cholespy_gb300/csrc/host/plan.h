@@ -118,16 +118,31 @@ struct SnbUpperPlan {
 
 void build_snb_upper(const SolvePlan& P, SnbUpperPlan& U);
 
-// Lower-sweep work items of the bulk supernodal sweeps and the ticket order
-// of both bulk sweeps. A unit whose list (without the chain block) is longer
-// than keep + group applies only its last `keep` blocks itself; the earlier
-// ones go to partial sums of about `group` blocks (separate items, started as
-// soon as their sources are done) that the unit adds in a fixed order.
-// Ticket keys come from the start-time estimate of build_plan with costs for
-// one item applying its blocks one after the other (blk_ns each).
+// Lower-sweep work of the bulk supernodal sweeps and the ticket order of
+// both bulk sweeps. A unit's contribution list (without the chain block) is
+// cut into groups: consecutive blocks from consecutive chunks of one other
+// supernode (same rows of the unit, contiguous source columns and L tiles)
+// form one group of up to max_cols source columns, applied as one block and
+// waiting only for the flag of its last chunk (the chunks of a supernode
+// finish in order); blocks from earlier chunks of the unit's own supernode
+// stay single. A unit with more than keep + group groups applies only its
+// last `keep` groups itself; the earlier ones go to partial sums of about
+// `group` groups (separate items, started as soon as their sources are done)
+// that the unit adds in a fixed order. Ticket keys come from the start-time
+// estimate of build_plan with costs for one item applying its groups one
+// after the other (blk_ns each).
+struct SnbGroup {
+    int32_t first;     // first contribution block (its L tile starts the group's tile rows)
+    int32_t cols;      // source columns (tile rows) of the group
+    int32_t src_unit;  // unit of the group's last chunk
+    int32_t xcol;      // first source column
+    uint32_t rowmask;  // the unit rows the group has
+};
+
 struct SnbOptions {
     int32_t keep = 16;
     int32_t group = 0;        // 0: no partial sums
+    int32_t max_cols = 64;    // source columns per group (32: no merging)
     int64_t lat_ns = 1000;    // flag latency
     int64_t base_ns = 5000;   // fixed cost of an item (diagonal solve, chain step)
     // cost of one block. Measured at 64^3, 128 RHS (5.99 / 5.87 / 5.79 /
@@ -137,8 +152,10 @@ struct SnbOptions {
 };
 
 struct SnbLowerPlan {
-    std::vector<int32_t> unit_info;   // per unit: first block it applies itself, first and end partial
-    std::vector<SnPartial> parts;     // partial sums over contribution ranges
+    std::vector<SnbGroup> groups;     // per unit in list order (chain block excluded)
+    std::vector<int32_t> unit_info;   // per unit: first group it applies itself, end of its groups,
+                                      // first and end partial sum
+    std::vector<SnPartial> parts;     // partial sums over group ranges (contrib_begin/end = groups)
     std::vector<int32_t> order_lo;    // lower-sweep tickets: unit u, or partial p as ~p
     std::vector<int32_t> order_up;    // upper-sweep tickets: units
 };

@@ -50,17 +50,20 @@ namespace {
 constexpr int kCW = 8;                    // consumer warps
 constexpr int kThreads = (kCW + 1) * 32;  // + one producer warp
 constexpr int kTile = 32 * 32;
-// Ring stages: 4 for the CUDA-core consumers, 2 with the tensor-core
-// operand buffers (two CTAs per SM either way).
-template <bool TC>
+// Ring geometry: KB block rows per stage (lower sweep with CUDA-core
+// consumers: groups of up to 64 source columns; otherwise 32) and S stages:
+// 4 of 32 rows, or 2 of 64 rows or with the tensor-core operand buffers (two
+// CTAs per SM in every case).
+template <bool LOWER, bool TC>
 struct SnbRing {
-    static constexpr int S = TC ? 2 : 4;
+    static constexpr int KB = (LOWER && !TC) ? 64 : 32;
+    static constexpr int S = (TC || KB == 64) ? 2 : 4;
 };
 
-template <int SW>
+template <int SW, int KB>
 struct SnbStage {
-    float l[32][32];   // L tile
-    float x[32 * SW];  // the block's rows of the work array, row stride = the RHS count
+    float l[KB][32];   // L tile rows (lower: source columns; upper: block rows)
+    float x[KB * SW];  // the block's rows of the work array, row stride = the RHS count
 };
 
 // Tensor-core operands of one block (canonical K-major layout, tcgen05.cuh):
@@ -79,10 +82,10 @@ struct SnbTc<true> {
     uint32_t tmem;      // accumulator: 128 lanes x 32 columns
 };
 
-template <int SW, bool TC>
+template <int SW, bool LOWER, bool TC>
 struct SnbSmem {
-    static constexpr int kStages = SnbRing<TC>::S;
-    SnbStage<SW> st[kStages];
+    static constexpr int kStages = SnbRing<LOWER, TC>::S;
+    SnbStage<SW, SnbRing<LOWER, TC>::KB> st[kStages];
     float t[32][SW];   // t' = t - sum of the blocks (right-hand side of the diagonal solve)
     float e[32][32];   // e[j][i] = E[i][j]
     float m[32][32];   // m[j][i] = M[i][j] (the chain block folded into the diagonal solve)
@@ -120,8 +123,8 @@ __device__ __forceinline__ SnbItem snb_item(const SnbArgs& a, int v, const SnUni
         it.tile0 = a.parts[~v].contrib_begin;
         it.nblk = a.parts[~v].contrib_end - it.tile0;
     } else if (LOWER) {
-        it.tile0 = a.unit_info[(size_t)it.uidx * 3];
-        it.nblk = U.contrib_end - (it.chain ? 1 : 0) - it.tile0;
+        it.tile0 = a.unit_info[(size_t)it.uidx * 4];
+        it.nblk = a.unit_info[(size_t)it.uidx * 4 + 1] - it.tile0;
     } else {
         it.tile0 = a.up_begin[it.uidx];
         it.nblk = a.up_begin[it.uidx + 1] - it.tile0;
@@ -135,7 +138,7 @@ __device__ __forceinline__ SnbItem snb_item(const SnbArgs& a, int v, const SnUni
 // block's `ext` rows and the RHS count. Thread t: A for RHS column t % 128
 // and row groups t / 128 + 2q; B for unit row / column t % 32 and row group t / 32.
 template <int SW>
-__device__ __forceinline__ void snb_split(const SnbStage<SW>& st, SnbTc<true>& tb, int ext, int nrhs, int tid) {
+__device__ __forceinline__ void snb_split(const SnbStage<SW, 32>& st, SnbTc<true>& tb, int ext, int nrhs, int tid) {
     const int ka = tid & 127;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -193,8 +196,8 @@ __device__ __forceinline__ void snb_mma(SnbTc<true>& tb, bool first) {
 template <class io, bool LOWER, int SW, bool TC>
 __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    SnbSmem<SW, TC>& sm = *reinterpret_cast<SnbSmem<SW, TC>*>(smem_raw);
-    constexpr int kStages = SnbRing<TC>::S;
+    SnbSmem<SW, LOWER, TC>& sm = *reinterpret_cast<SnbSmem<SW, LOWER, TC>*>(smem_raw);
+    constexpr int kStages = SnbRing<LOWER, TC>::S;
     if (a.skip && dev::ld_volatile(a.skip)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // every CTA reads the sweep's epoch before the last CTA out bumps it
@@ -246,16 +249,17 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             // trip for the window); the descriptors are broadcast by shuffles
             for (int w0 = 0; w0 < it.nblk; w0 += 32) {
                 const int cnt = min(32, it.nblk - w0);
-                int src_j = 0, xcol_j = 0, w_j = 0, ready_j = 1;
+                int src_j = 0, xcol_j = 0, w_j = 0, first_j = 0, ready_j = 1;
                 unsigned mask_j = 0;
                 if (lane < cnt) {
                     const int t = it.tile0 + w0 + lane;
                     if (LOWER) {
-                        const SnContrib& C = a.contribs[t];
-                        src_j = C.src_unit;
-                        xcol_j = C.xcol;
-                        w_j = C.w;
-                        mask_j = C.rowmask;
+                        const SnbGroup& G = a.groups[t];
+                        src_j = G.src_unit;
+                        xcol_j = G.xcol;
+                        w_j = G.cols;
+                        first_j = G.first;
+                        mask_j = G.rowmask;
                     } else {
                         src_j = a.up_dep[t];
                     }
@@ -271,25 +275,35 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                     const int t = it.tile0 + w0 + q;
                     const int src = __shfl_sync(0xffffffffu, src_j, q);
                     const int ready = __shfl_sync(0xffffffffu, ready_j, q);
-                    int row;
+                    int row, rows_l = 0, tile = t;
                     unsigned mask;
                     if (LOWER) {
-                        const int xc = __shfl_sync(0xffffffffu, xcol_j, q), wb = __shfl_sync(0xffffffffu, w_j, q);
-                        row = lane < wb ? xc + lane : -1;
+                        // a group: contiguous work-array rows and tile rows, one copy each
+                        row = __shfl_sync(0xffffffffu, xcol_j, q);
+                        rows_l = __shfl_sync(0xffffffffu, w_j, q);
+                        tile = __shfl_sync(0xffffffffu, first_j, q);
                         mask = __shfl_sync(0xffffffffu, mask_j, q);
                     } else {
                         row = row_next;
                         if (q + 1 < cnt) row_next = a.up_rows[(size_t)(t + 1) * 32 + lane];
                         mask = umask;
                     }
-                    // the block's rows are a prefix of the lanes; runs of
+                    // upper: the block's rows are a prefix of the lanes; runs of
                     // consecutive work-array rows go in one bulk copy each
-                    const unsigned have = __ballot_sync(0xffffffffu, row >= 0);
-                    const int rows = __popc(have);
-                    const int prev = __shfl_up_sync(0xffffffffu, row, 1);
-                    const bool start = row >= 0 && (lane == 0 || prev != row - 1);
-                    const unsigned later = __ballot_sync(0xffffffffu, start) & ~((2u << lane) - 1u);
-                    const int run = (later ? __ffs(later) - 1 : rows) - lane;  // rows in my run (if start)
+                    int rows, run = 0;
+                    bool start;
+                    if (LOWER) {
+                        rows = rows_l;
+                        start = lane == 0;
+                        run = rows;
+                    } else {
+                        const unsigned have = __ballot_sync(0xffffffffu, row >= 0);
+                        rows = __popc(have);
+                        const int prev = __shfl_up_sync(0xffffffffu, row, 1);
+                        start = row >= 0 && (lane == 0 || prev != row - 1);
+                        const unsigned later = __ballot_sync(0xffffffffu, start) & ~((2u << lane) - 1u);
+                        run = (later ? __ffs(later) - 1 : rows) - lane;  // rows in my run (if start)
+                    }
                     if (lane == 0) {
                         if (g >= kStages) {
                             const uint32_t par = ((g / kStages) - 1) & 1;
@@ -307,11 +321,11 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                     // the source rows were published under the flag: order the
                     // bulk (async-proxy) reads after its acquire
                     bulk::fence_proxy_async_global();
-                    const float* ltile = (LOWER ? a.lo_tiles : a.up_tiles) + (size_t)t * kTile;
+                    const float* ltile = (LOWER ? a.lo_tiles : a.up_tiles) + (size_t)tile * kTile;
                     // the tile's first `rows` rows: the rest is zero and unread
                     if (lane == 0) bulk::copy_g2s(&sm.st[s].l[0][0], ltile, (uint32_t)rows * 32 * 4, &sm.full[s]);
                     if (start)
-                        bulk::copy_g2s(&sm.st[s].x[lane * nrhs], a.tmp + (size_t)row * nrhs,
+                        bulk::copy_g2s(&sm.st[s].x[(LOWER ? 0 : lane) * nrhs], a.tmp + (size_t)row * nrhs,
                                        (uint32_t)(run * nrhs) * 4, &sm.full[s]);
                 }
             }
@@ -388,7 +402,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                 const int ext = sm.ext[s];
                 // 4-row groups of my rows (columns) the block has: the others hold zeros
                 const unsigned grp = sm.mask[s] >> r0;
-                const SnbStage<SW>& st = sm.st[s];
+                const auto& st = sm.st[s];
                 int j = 0;
                 // four block rows at a time: their loads go out together
                 for (; j + 4 <= ext; j += 4) {
@@ -446,7 +460,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                 continue;
             }
             if (LOWER) {  // the unit's partial sums, in a fixed order
-                const int pb = a.unit_info[(size_t)uidx * 3 + 1], pe = a.unit_info[(size_t)uidx * 3 + 2];
+                const int pb = a.unit_info[(size_t)uidx * 4 + 2], pe = a.unit_info[(size_t)uidx * 4 + 3];
                 for (int q = pb; q < pe; ++q) {
                     if (lane == 0) dev::wait_geq(a.uflags + a.n_units + q, epoch, a.status);
                     __syncwarp();
@@ -547,7 +561,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
 template <class io, bool LOWER, int SW, bool TC>
 cudaError_t launch_snb(const SnbArgs& a, cudaStream_t stream) {
     const void* fn = (const void*)snb_sweep_kernel<io, LOWER, SW, TC>;
-    const size_t smem = sizeof(SnbSmem<SW, TC>);
+    const size_t smem = sizeof(SnbSmem<SW, LOWER, TC>);
     int grid = 0;
     cudaError_t e = coop_grid(fn, kThreads, smem, &grid);  // resident CTAs: a persistent grid
     if (e != cudaSuccess) return e;

@@ -15,12 +15,14 @@ struct SnbArgs {
     const SnContrib* contribs = nullptr;
     const int32_t* order = nullptr;     // tickets: unit u, or (lower sweep) partial sum p as ~p
     const float* lo_tiles = nullptr;    // per contribution block: 32 x 32, [source column][unit row]
+                                        // (a group's tiles are consecutive: its rows are contiguous)
     const float* up_tiles = nullptr;    // per upper block: 32 x 32, [block row][unit column]
     const int32_t* up_begin = nullptr;  // per unit: first upper block (n_units + 1 entries)
     const int32_t* up_rows = nullptr;   // per upper block: 32 work-array rows (-1 past the block)
     const int32_t* up_dep = nullptr;    // per upper block: the unit whose flag it waits for
-    const int32_t* unit_info = nullptr; // lower: per unit, first block it applies itself, first / end partial
-    const SnPartial* parts = nullptr;   // lower: partial sums over contribution ranges
+    const SnbGroup* groups = nullptr;   // lower: merged contribution blocks, per unit in list order
+    const int32_t* unit_info = nullptr; // lower: per unit, first own group, end of groups, first / end partial
+    const SnPartial* parts = nullptr;   // lower: partial sums over group ranges
     float* pbuf = nullptr;              // lower: partial-sum slots, 32 x nrhs each
     int n_units = 0;                    // partial p's flag follows the units': n_units + p
     const float* dinv = nullptr;        // per unit: D^-1, M_lo, M_up (32 x 32, column-major each)
@@ -43,6 +45,9 @@ struct SnbArgs {
 inline bool snb_supported(int nrhs) { return nrhs > 32 && nrhs <= 128 && nrhs % 4 == 0; }
 // Shared-memory width of a work item: 64 columns up to 64 RHS, else 128.
 inline int snb_width(int nrhs) { return nrhs <= 64 ? 64 : 128; }
+// Source columns per lower-sweep group: 64 with the CUDA-core consumers, 32
+// with the tensor-core ones.
+inline int snb_group_cols(bool tensor_cores) { return tensor_cores ? 32 : 64; }
 
 // The upper sweep writes the output only when a.out is set; otherwise this
 // kernel writes the top rows' solution afterwards (out[perm[row]] = or +=

@@ -144,6 +144,7 @@ struct gbchol_solver {
     DevBuf<int32_t> snb_up_begin, snb_up_dep, snb_up_rows;
     DevBuf<int32_t> snb_unit_info, snb_order_lo, snb_order_up;
     DevBuf<SnPartial> snb_parts;
+    DevBuf<SnbGroup> snb_groups;
     int32_t snb_nparts = 0;
     bool snb_ready = false;
     int32_t snb_min_rhs = 33;  // RHS counts from here on use the bulk sweeps (when supported)

@@ -334,9 +334,13 @@ bool check_transpose() {
 }
 
 // The bulk sweeps' schedule (build_snb_upper / build_snb_lower): every item
-// waits only on items with earlier tickets, the partial sums of a unit cover
-// the start of its block list exactly (in order, no gaps or overlaps), and the
-// upper blocks of a unit are the blocks of the 32-column sweep in its order.
+// waits only on items with earlier tickets; a unit's groups are its
+// contribution list without the chain block, in order, each a run of
+// consecutive blocks from consecutive full chunks of one supernode (same row
+// mask, contiguous source columns, so contiguous L tiles), waiting on the
+// unit of its last chunk, and no larger than max_cols; its partial sums
+// cover the start of its groups exactly; the upper blocks of a unit are the
+// blocks of the 32-column sweep in its order.
 int check_snb(const SolvePlan& P, const SnbOptions& o) {
     int bad = 0;
     SnbUpperPlan B;
@@ -352,32 +356,54 @@ int check_snb(const SolvePlan& P, const SnbOptions& o) {
         else tp[~v] = t;
     }
     for (int32_t t = 0; t < nu; ++t) tup[L.order_up[t]] = t;
+    int32_t gat = 0;
     for (int32_t u = 0; u < nu; ++u) {
         const SnUnit& U = P.units[u];
-        const int32_t first = L.unit_info[(size_t)u * 3], pb = L.unit_info[(size_t)u * 3 + 1],
-                      pe = L.unit_info[(size_t)u * 3 + 2];
-        int32_t at = U.contrib_begin;
+        const int32_t first = L.unit_info[(size_t)u * 4], gend = L.unit_info[(size_t)u * 4 + 1],
+                      pb = L.unit_info[(size_t)u * 4 + 2], pe = L.unit_info[(size_t)u * 4 + 3];
+        const int32_t chain = U.pos0 > 0 ? 1 : 0;
+        // groups cover [contrib_begin, contrib_end - chain) in order
+        int32_t e = U.contrib_begin;
+        for (int32_t g = gat; g < gend; ++g) {
+            const SnbGroup& G = L.groups[g];
+            bad += G.first != e;
+            int32_t cols = 0, f = e;
+            while (cols < G.cols && f < U.contrib_end - chain) {
+                const SnContrib& C = P.contribs[f];
+                bad += C.rowmask != G.rowmask || C.xcol != G.xcol + cols;
+                if (cols + C.w < G.cols) bad += C.w != kChunk;
+                cols += C.w;
+                ++f;
+            }
+            bad += cols != G.cols || G.cols > std::max(o.max_cols, kChunk) || P.contribs[f - 1].src_unit != G.src_unit;
+            bad += tu[G.src_unit] < 0 || tu[G.src_unit] >= tu[u];
+            e = f;
+        }
+        bad += e != U.contrib_end - chain;
+        if (chain) bad += tu[u - 1] >= tu[u];
+        int32_t at = gat;
         for (int32_t q = pb; q < pe; ++q) {
             bad += L.parts[q].unit != u || L.parts[q].contrib_begin != at ||
                    L.parts[q].contrib_end <= L.parts[q].contrib_begin;
             at = L.parts[q].contrib_end;
             bad += tp[q] < 0 || tp[q] >= tu[u];
-            for (int32_t e = L.parts[q].contrib_begin; e < L.parts[q].contrib_end; ++e)
-                bad += tu[P.contribs[e].src_unit] >= tp[q];
+            for (int32_t g = L.parts[q].contrib_begin; g < L.parts[q].contrib_end; ++g)
+                bad += tu[L.groups[g].src_unit] >= tp[q];
         }
-        bad += at != first || first > U.contrib_end;
-        for (int32_t e = first; e < U.contrib_end; ++e) bad += tu[P.contribs[e].src_unit] >= tu[u];
+        bad += at != first || first > gend;
+        gat = gend;
         const int32_t wj = U.pos0 + U.w, nrb = (U.ld - U.sn_w + kChunk - 1) / kChunk;
-        const int32_t nlater = (U.sn_w - wj + kChunk - 1) / kChunk, chain = wj < U.sn_w ? 1 : 0;
-        bad += B.begin[u + 1] - B.begin[u] != nrb + nlater - chain;
+        const int32_t nlater = (U.sn_w - wj + kChunk - 1) / kChunk, uchain = wj < U.sn_w ? 1 : 0;
+        bad += B.begin[u + 1] - B.begin[u] != nrb + nlater - uchain;
         for (int32_t t = B.begin[u]; t < B.begin[u + 1]; ++t) {
             bad += tup[B.dep[t]] >= tup[u];
             const int32_t nr = B.nrw[t] & 0xffff, w = B.nrw[t] >> 16;
             bad += nr < 1 || nr > kChunk || w != U.w;
             for (int32_t i = 0; i < kChunk; ++i) bad += (B.rows[(size_t)t * kChunk + i] >= 0) != (i < nr);
         }
-        if (chain) bad += tup[u + 1] >= tup[u];
+        if (uchain) bad += tup[u + 1] >= tup[u];
     }
+    bad += gat != (int32_t)L.groups.size();
     return bad;
 }
 
@@ -418,7 +444,7 @@ int main() {
         po.part_group = cs.group;
         build_plan(F, lo, up, po, P);
         if (cs.group == 0) {  // the bulk schedule is built on plans without 32-column partial sums
-            for (const SnbOptions& so : {SnbOptions{}, SnbOptions{2, 3, 1000, 3000, 500}, SnbOptions{0, 1, 10, 10, 10}}) {
+            for (const SnbOptions& so : {SnbOptions{}, SnbOptions{2, 3, 32, 1000, 3000, 500}, SnbOptions{0, 1, 128, 10, 10, 10}}) {
                 const int bad = check_snb(P, so);
                 std::printf("%dD k=%d minw=%d bulk keep=%d group=%d: checks failed %d %s\n", cs.dim, cs.k, cs.minw,
                             so.keep, so.group, bad, bad ? "FAIL" : "ok");
