@@ -65,6 +65,7 @@ def _declare(lib):
         "gbchol_refactorize": (C.c_int, [P, I64, P, P, P, I32]),
         "gbchol_factor_refactorize": (C.c_int, [P, I64, P, P, P, I32, I32]),
         "gbchol_autotune": (C.c_int, [P, I32, I32, P, I32, I32, C.POINTER(I32)]),
+        "gbchol_autotune_sweeps": (C.c_int, [P, I32, I32, I32, C.POINTER(I32)]),
         "gbchol_factorize": (C.c_int, [I32, I64, P, P, P, I32, I32, C.POINTER(P)]),
         "gbchol_factor_info": (C.c_int, [P, C.POINTER(I32), C.POINTER(I64), C.POINTER(I32),
                                          C.POINTER(D)]),

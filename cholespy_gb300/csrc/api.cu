@@ -190,7 +190,7 @@ int setup_snb(gbchol_solver* h) {
     if (const char* env = std::getenv("GBCHOL_BULK_GROUP")) so.group = std::atoi(env);
     if (const char* env = std::getenv("GBCHOL_BULK_BLK_NS")) so.blk_ns = std::atoll(env);
     if (const char* env = std::getenv("GBCHOL_BULK_BASE_NS")) so.base_ns = std::atoll(env);
-    so.max_cols = snb_group_cols(h->snb_tc);
+    so.max_cols = snb_group_cols(h->snb_tc || h->snb_tc_groups);
     if (const char* env = std::getenv("GBCHOL_BULK_GROUP_COLS"))
         so.max_cols = std::min(so.max_cols, std::max(32, std::atoi(env)));
     SnbLowerPlan L;
@@ -209,6 +209,7 @@ int setup_snb(gbchol_solver* h) {
     CUDA_TRY(h->snb_order_lo.upload(L.order_lo.data(), L.order_lo.size()));
     CUDA_TRY(h->snb_order_up.upload(L.order_up.data(), L.order_up.size()));
     h->snb_nparts = (int32_t)L.parts.size();
+    h->snb_group_cols = so.max_cols;
     // flags of the bulk partial sums follow the units'
     if (h->uflags.count < P.units.size() + L.parts.size()) {
         CUDA_TRY(h->uflags.alloc(P.units.size() + L.parts.size()));
@@ -368,10 +369,17 @@ namespace {
 }  // namespace
 
 namespace {
-// Solves of this RHS count use the bulk supernodal sweeps.
-bool use_snb(const gbchol_solver* h, int nrhs, bool f32) {
-    return f32 && h->snb_ready && snb_supported(nrhs) && nrhs >= h->snb_min_rhs;
+// Supernodal kernel of a solve: 0 the 32-column sweeps, 1 the bulk sweeps,
+// 2 the bulk sweeps on the tensor cores (tiles built for groups of <= 32
+// columns). An autotuned choice for this RHS count wins over the defaults.
+int sn_kind(const gbchol_solver* h, int nrhs, bool f32) {
+    if (!f32 || !h->snb_ready || !snb_supported(nrhs)) return 0;
+    const auto& t = h->tuned[nrhs];
+    if (t.valid) return (t.sn == 2 && h->snb_group_cols > 32) ? 1 : t.sn;
+    if (nrhs < h->snb_min_rhs) return 0;
+    return (h->snb_tc && h->snb_group_cols <= 32) ? 2 : 1;
 }
+bool use_snb(const gbchol_solver* h, int nrhs, bool f32) { return sn_kind(h, nrhs, f32) != 0; }
 }  // namespace
 
 size_t gbchol::work_bytes(const gbchol_solver* h, int nrhs, bool f32) {
@@ -403,8 +411,10 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
     lo.status = h->status.p;
     lo.skip = skip;
     lo.counters = h->counters.p;
-    lo.chunk = row_chunk();
+    const auto& tune = h->tuned[nrhs];
+    lo.chunk = tune.valid ? tune.chunk : row_chunk();
     lo.max_nrhs = nrhs;
+    lo.rhs_split = tune.valid ? tune.rhs_split : 0;
     lo.epoch = h->dev_epoch.p;
     CUDA_TRY(launch_row_sweep(lo, true, io, s));
     SnSweepArgs sn;
@@ -440,7 +450,7 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
         b.tmp = static_cast<float*>(work);
         b.uflags = h->uflags.p;
         b.nrhs = nrhs;
-        b.tensor_cores = h->snb_tc ? 1 : 0;
+        b.tensor_cores = sn_kind(h, nrhs, f32) == 2 ? 1 : 0;
         b.status = h->status.p;
         b.skip = skip;
         b.epoch = h->dev_epoch.p;
@@ -798,6 +808,83 @@ int gbchol_autotune(gbchol_handle h, int32_t precision, int32_t nrhs, const int3
     if (rc == GBCHOL_OK && best != h->plan_opt.min_top_width)
         rc = gbchol_replan(h, best, keep.part_keep, keep.part_group);
     if (rc == GBCHOL_OK && chosen) *chosen = best;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    return rc;
+}
+
+int gbchol_autotune_sweeps(gbchol_handle h, int32_t precision, int32_t nrhs, int32_t reps, int32_t* choice) {
+    if (!h) return fail(GBCHOL_EINVAL, "Null handle.");
+    if (int rc = check_rhs(nrhs)) return rc;
+    if (precision != 0 && precision != 1) return fail(GBCHOL_EINVAL, "precision must be 0 or 1.");
+    const bool f32 = precision == 0;
+    if (!(h->store & (f32 ? GBCHOL_STORE_F32 : GBCHOL_STORE_F64)))
+        return fail(GBCHOL_ESTATE, f32 ? "This solver keeps no FP32 factor." : "This solver keeps no FP64 factor.");
+    if (reps < 1 || reps > 100) return fail(GBCHOL_EINVAL, "reps must be in [1, 100].");
+    if (h->n == 0) {
+        if (choice) *choice = 0;
+        return GBCHOL_OK;
+    }
+    DeviceGuard g(h->device);
+    // the tensor-core variant needs lower groups of <= 32 columns: rebuild
+    // the bulk tiles for it first (the other variants run on them too)
+    const bool bulk_ok = f32 && h->snb_ready && snb_supported(nrhs);
+    if (bulk_ok && h->snb_group_cols > 32) {
+        h->snb_tc_groups = true;
+        CUDA_TRY(cudaDeviceSynchronize());
+        if (int rc = setup_snb(h)) return rc;
+    }
+    const size_t bytes = (size_t)h->n * nrhs * (f32 ? sizeof(float) : sizeof(double));
+    DevBuf<unsigned char> b, x;
+    CUDA_TRY(b.alloc(bytes));
+    CUDA_TRY(x.alloc(bytes));
+    CUDA_TRY(cudaMemset(b.p, 0, bytes));
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    int rc = GBCHOL_OK;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        rc = fail(GBCHOL_ECUDA, "cudaEventCreate failed.");
+    const SweepIO io = f32 ? SweepIO::F32 : SweepIO::F64;
+    gbchol_solver::SweepTune best;
+    float best_ms = 0.f;
+    const int sn_max = bulk_ok ? 2 : 0;
+    for (int sn = 0; sn <= sn_max && rc == GBCHOL_OK; ++sn)
+        for (int split = 0; split <= (nrhs <= 8 ? 1 : 0) && rc == GBCHOL_OK; ++split)
+            for (int chunk : {1, 2, 4}) {
+                if (rc != GBCHOL_OK) break;
+                gbchol_solver::SweepTune t;
+                t.valid = 1;
+                t.sn = (int8_t)sn;
+                t.rhs_split = (int8_t)split;
+                t.chunk = (int8_t)chunk;
+                h->tuned[nrhs] = t;
+                if ((rc = ensure_tmp(h, work_bytes(h, nrhs, f32)))) break;
+                for (int w = 0; w < 2 && rc == GBCHOL_OK; ++w) rc = run_sweeps(h, f32, io, nrhs, b.p, x.p, nullptr, s);
+                if (rc) break;
+                cudaEventRecord(e0, s);
+                for (int r = 0; r < reps && rc == GBCHOL_OK; ++r)
+                    rc = run_sweeps(h, f32, io, nrhs, b.p, x.p, nullptr, s);
+                cudaEventRecord(e1, s);
+                if (rc) break;
+                if (cudaEventSynchronize(e1) != cudaSuccess) {
+                    rc = fail(GBCHOL_ECUDA, "autotune: timing failed.");
+                    break;
+                }
+                h->last_stream = s;
+                if ((rc = gbchol_check(h))) break;
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (!best.valid || ms < best_ms) {
+                    best = t;
+                    best_ms = ms;
+                }
+            }
+    h->last_stream = nullptr;
+    h->tuned[nrhs] = rc == GBCHOL_OK ? best : gbchol_solver::SweepTune{};
+    if (rc == GBCHOL_OK && choice) *choice = best.sn | (best.rhs_split << 4) | (best.chunk << 8);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     cudaStreamSynchronize(s);

@@ -59,6 +59,7 @@ struct RowSweepArgs {
     int* counters = nullptr;      // [ticket, exited warps], zero between launches
     int chunk = 1;                // consecutive tasks taken per ticket
     int max_nrhs = 0;             // largest nrhs over the systems (kernel variant choice)
+    int rhs_split = 0;            // 1: lanes over the RHS columns even for <= 8 RHS (autotuned)
     int batched_variant = 0;      // 1: one variant for every nrhs (per-system dispatch)
 };
 

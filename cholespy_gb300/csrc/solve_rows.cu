@@ -292,6 +292,7 @@ cudaError_t launch_io(const RowSweepArgs& a, cudaStream_t stream) {
     const void* fn;
     const int r = a.max_nrhs;
     if (a.batched_variant) fn = (const void*)row_sweep_kernel<io, LOWER, 0>;
+    else if (a.rhs_split && r <= 16) fn = (const void*)row_sweep_kernel<io, LOWER, 16>;
     else if (r <= 1) fn = (const void*)row_sweep_kernel<io, LOWER, 1>;
     else if (r <= 2) fn = (const void*)row_sweep_kernel<io, LOWER, 2>;
     else if (r <= 4) fn = (const void*)row_sweep_kernel<io, LOWER, 4>;

@@ -149,6 +149,15 @@ struct gbchol_solver {
     bool snb_ready = false;
     int32_t snb_min_rhs = 33;  // RHS counts from here on use the bulk sweeps (when supported)
     bool snb_tc = false;       // bulk sweeps: block products on the tensor cores
+    bool snb_tc_groups = false;  // build the lower groups for the tensor cores (<= 32 columns)
+    int32_t snb_group_cols = 0;  // source columns per lower group the tiles were built for
+    // per RHS count, the sweep variant chosen by gbchol_autotune_sweeps:
+    // supernodal kernel (0 sliced, 1 bulk, 2 bulk on the tensor cores), row
+    // sweeps with lanes over the RHS, rows per ticket; valid = 0: defaults
+    struct SweepTune {
+        int8_t valid = 0, sn = 0, rhs_split = 0, chunk = 1;
+    };
+    SweepTune tuned[GBCHOL_MAX_RHS + 1];
     DevBuf<int32_t> counters; // [ticket, exits] per sweep kernel (5 kernels)
     DevBuf<int32_t> dev_epoch;  // sweep counter of the solve kernels (device-resident)
     std::vector<int32_t> flags_init;  // 0 for leaf rows, INT_MAX for top rows

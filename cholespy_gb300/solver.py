@@ -375,6 +375,25 @@ class _CholeskySolver:
                                               C.byref(chosen)))
         return int(chosen.value)
 
+    def autotune_sweeps(self, n_rhs, precision=None, reps=3):
+        """Time the sweep variants for `n_rhs` RHS on the current plan and keep
+        the fastest for later solves of that RHS count (gbchol_autotune_sweeps):
+        the top-region kernel ("sliced": 32-column RHS slices, "bulk": one work
+        item per unit for every RHS column, "bulk_tc": the same on the tensor
+        cores), the row sweeps' lane mode (lanes over the RHS for <= 8 RHS) and
+        the rows per row-sweep ticket. Returns the choice as a dict. No
+        counterpart in the reference."""
+        self._gpu_only("autotune_sweeps")
+        if precision is None:
+            prec = 0 if (self._precision == 0 or self._refine) else 1
+        else:
+            prec = 0 if precision == "float" else 1
+        choice = C.c_int32(0)
+        _ffi.check(_ffi.lib().gbchol_autotune_sweeps(self._h, prec, int(n_rhs), int(reps), C.byref(choice)))
+        v = int(choice.value)
+        return {"kernel": ("sliced", "bulk", "bulk_tc")[v & 15], "rhs_split": bool((v >> 4) & 15),
+                "rows_per_ticket": v >> 8}
+
     def info(self) -> SolverInfo:
         self._gpu_only("info")
         inf = _ffi.Info()

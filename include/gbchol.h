@@ -294,6 +294,22 @@ int gbchol_autotune(gbchol_handle h, int32_t precision, int32_t nrhs, const int3
                     int32_t reps, int32_t* chosen);
 
 /*
+ * Times the sweep variants on this solver's current plan for `nrhs` RHS of
+ * the given precision (`reps` timed solves each, after two untimed ones)
+ * and keeps the fastest for later solves of that RHS count: the
+ * top-region kernel (0: 32-column RHS slices, 1: one work item per unit for
+ * every RHS column, CUDA cores, 2: the same on the tensor cores; 1 and 2
+ * only for FP32 and 33..128 RHS in multiples of 4), for <= 8 RHS whether
+ * the row sweeps put their lanes over the RHS columns instead of the
+ * nonzeros (threads per column), and the rows each row-sweep ticket takes
+ * (1, 2 or 4: how many consecutive level-ordered rows are merged into one
+ * task). *choice = kernel | rhs_split << 4 | rows_per_ticket << 8.
+ * Allocates scratch and synchronises. No counterpart in the reference (its
+ * launch shape is fixed, src/cholesky_solver.cpp:378-413).
+ */
+int gbchol_autotune_sweeps(gbchol_handle h, int32_t precision, int32_t nrhs, int32_t reps, int32_t* choice);
+
+/*
  * Numeric refactorisation of a solver: new values of the same sparsity
  * pattern (same n and input format as at creation). Keeps the ordering, the
  * symbolic factor and the level analysis; recomputes the numeric factor on the

@@ -523,3 +523,27 @@ def test_bulk_sweeps_match_oracle_and_narrow(cuda, name, group, tensor_cores, mo
     A = sym_matrix(n, vals, idx)
     res = np.linalg.norm(b - A @ xt.cpu().numpy(), axis=0) / np.linalg.norm(b, axis=0)
     assert res.max() <= 1e-10
+
+
+@pytest.mark.parametrize("nrhs", [4, 64])
+def test_autotune_sweeps(cuda, nrhs):
+    """gbchol_autotune_sweeps times every sweep variant for an RHS count
+    (top-region kernel, row-sweep lane mode, rows per ticket), keeps the
+    fastest, and solves with it afterwards: results still match the oracle
+    (FP32 within 1e-5 relative to max |x|)."""
+    from cholespy_gb300 import CholeskySolverF
+    torch = cuda
+    n, vals, idx = PROBLEMS["grid3d_16"]()
+    s = _make(torch, n, vals, idx, CholeskySolverF)
+    choice = s.autotune_sweeps(nrhs, reps=2)
+    assert choice["kernel"] in (("sliced", "bulk", "bulk_tc") if nrhs > 32 else ("sliced",))
+    assert choice["rows_per_ticket"] in (1, 2, 4)
+    assert choice["rhs_split"] in ((False, True) if nrhs <= 8 else (False,))
+    perm, colptr, rowidx, lv = s.factor()
+    b = np.random.default_rng(nrhs).standard_normal((n, nrhs)).astype(np.float32)
+    bt = torch.tensor(b, device="cuda")
+    xt = torch.zeros_like(bt)
+    s.solve(bt, xt)
+    s.check()
+    xo = oracle.reference_solve(perm, colptr, rowidx, lv, b, np.float32)
+    assert np.abs(xt.cpu().numpy() - xo).max() / np.abs(xo).max() <= 1e-5
