@@ -52,6 +52,7 @@ def _declare(lib):
         "gbchol_last_error": (C.c_char_p, []),
         "gbchol_version": (C.c_char_p, []),
         "gbchol_create": (C.c_int, [I32, I64, P, P, P, I32, I32, C.POINTER(P)]),
+        "gbchol_create_device": (C.c_int, [I32, I64, P, P, P, I32, I32, C.POINTER(P)]),
         "gbchol_create_from_factor": (C.c_int, [I32, P, P, P, P, I32, C.POINTER(P)]),
         "gbchol_destroy": (C.c_int, [P]),
         "gbchol_solve": (C.c_int, [P, I32, I32, P, P, P]),

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "grad.h"
+#include "prep.h"
 #include "solver_impl.h"
 
 using namespace gbchol;
@@ -525,6 +526,20 @@ const char* gbchol_last_error(void) { return g_last_error.c_str(); }
 
 const char* gbchol_version(void) { return "gbchol 0.1.0 (sm_103a)"; }
 
+}  // extern "C"
+
+namespace {
+
+// The rest of construction once the input is a sorted, duplicate-summed CSC
+// (host arrays ii / jj: the input's index arrays, recorded for the cached
+// refactorisation).
+int create_from_csc(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t* jj, int32_t matrix_type,
+                    int32_t store, Csc& A, gbchol_handle* out);
+
+}  // namespace
+
+extern "C" {
+
 int gbchol_create(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t* jj,
                   const double* x, int32_t matrix_type, int32_t store, gbchol_handle* out) {
     if (!out) return fail(GBCHOL_EINVAL, "out must not be NULL.");
@@ -533,14 +548,70 @@ int gbchol_create(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t*
     if (n_rows < 0) return fail(GBCHOL_EINVAL, "The number of rows must be non-negative.");
     if (nnz > 0 && (!ii || !jj || !x)) return fail(GBCHOL_EINVAL, "Null input array.");
     if (matrix_type != GBCHOL_COO && !ii) return fail(GBCHOL_EINVAL, "Null pointer array.");
+    std::string err;
+    Csc A;
+    Status st = build_csc(n_rows, nnz, ii, jj, x, matrix_type, A, err);
+    if (st != ST_OK) return fail(GBCHOL_EINVAL, err);
+    return create_from_csc(n_rows, nnz, ii, jj, matrix_type, store, A, out);
+}
+
+int gbchol_create_device(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t* jj, const double* x,
+                         int32_t matrix_type, int32_t store, gbchol_handle* out) {
+    if (!out) return fail(GBCHOL_EINVAL, "out must not be NULL.");
+    *out = nullptr;
+    if (int rc = check_store(store)) return rc;
+    if (n_rows < 0) return fail(GBCHOL_EINVAL, "The number of rows must be non-negative.");
+    if (nnz < 0 || nnz >= (int64_t)INT32_MAX) return fail(GBCHOL_EINVAL, "Number of nonzero entries out of range.");
+    if (nnz > 0 && (!ii || !jj || !x)) return fail(GBCHOL_EINVAL, "Null input array.");
+    if (matrix_type != GBCHOL_COO && matrix_type != GBCHOL_CSR && matrix_type != GBCHOL_CSC)
+        return fail(GBCHOL_EINVAL, "Unknown matrix type.");
+    if (matrix_type != GBCHOL_COO && !ii) return fail(GBCHOL_EINVAL, "Null pointer array.");
+    // the index arrays on the host: the pointer array's check, and the record
+    // of the input pattern for the cached refactorisation
+    const size_t nii = matrix_type == GBCHOL_COO ? (size_t)nnz : (size_t)n_rows + 1;
+    std::vector<int32_t> hi(nii), hj((size_t)nnz);
+    if (nii) CUDA_TRY(cudaMemcpy(hi.data(), ii, nii * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (nnz) CUDA_TRY(cudaMemcpy(hj.data(), jj, (size_t)nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (matrix_type != GBCHOL_COO) {
+        const std::string what = matrix_type == GBCHOL_CSR ? "Sparse CSR matrix" : "Sparse CSC matrix";
+        bool ok = hi[0] == 0 && (int64_t)hi[n_rows] == nnz;
+        for (int32_t k = 0; ok && k < n_rows; ++k) ok = hi[k + 1] >= hi[k];
+        if (!ok) return fail(GBCHOL_EINVAL, what + ": Invalid pointer array.");
+    }
+    DeviceCsc D;
+    int bad = 0;
+    CUDA_TRY(device_csc(n_rows, nnz, ii, jj, x, matrix_type, D, &bad, nullptr));
+    if (bad)
+        return fail(GBCHOL_EINVAL, matrix_type == GBCHOL_COO   ? "Sparse COO matrix: index out of range."
+                                   : matrix_type == GBCHOL_CSR ? "Sparse CSR matrix: index out of range."
+                                                                : "Sparse CSC matrix: index out of range.");
+    Csc A;
+    A.n = n_rows;
+    A.colptr.resize((size_t)n_rows + 1);
+    A.rowidx.resize((size_t)D.nnz);
+    A.vals.resize((size_t)D.nnz);
+    cudaError_t e = cudaMemcpy(A.colptr.data(), D.colptr, A.colptr.size() * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && D.nnz)
+        e = cudaMemcpy(A.rowidx.data(), D.rowidx, A.rowidx.size() * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && D.nnz)
+        e = cudaMemcpy(A.vals.data(), D.vals, A.vals.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    D.release();
+    CUDA_TRY(e);
+    return create_from_csc(n_rows, nnz, hi.data(), hj.data(), matrix_type, store, A, out);
+}
+
+}  // extern "C"
+
+namespace {
+
+int create_from_csc(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t* jj, int32_t matrix_type,
+                    int32_t store, Csc& A, gbchol_handle* out) {
     std::unique_ptr<gbchol_solver> h(new (std::nothrow) gbchol_solver());
     if (!h) return fail(GBCHOL_ENOMEM, "Out of host memory.");
     h->n = n_rows;
     h->store = store;
     std::string err;
-    Csc A;
-    Status st = build_csc(n_rows, nnz, ii, jj, x, matrix_type, A, err);
-    if (st != ST_OK) return fail(GBCHOL_EINVAL, err);
+    Status st = ST_OK;
     auto t0 = std::chrono::steady_clock::now();
     FactorOptions opt;
     st = factorize(A, opt, h->F, err);
@@ -560,10 +631,6 @@ int gbchol_create(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t*
     *out = h.release();
     return GBCHOL_OK;
 }
-
-}  // extern "C"
-
-namespace {
 
 // Numeric factor of new values on the same pattern: the old ordering is
 // given to the factorisation, and the resulting pattern must be the old one.

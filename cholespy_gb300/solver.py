@@ -22,6 +22,7 @@ from __future__ import annotations
 import ctypes as C
 import enum
 import math
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -153,6 +154,21 @@ def _host_vector(a, dtype, name):
     return np.ascontiguousarray(arr, dtype=dtype)
 
 
+def _device_vector(a, dtype, device, name):
+    """1-D contiguous CUDA tensor of `dtype` on `device` from a CUDA array (the
+    reference's constructor takes int32 indices and float64 values)."""
+    torch = _torch()
+    t = _as_torch(a).detach()
+    if t.dim() != 1:
+        raise ValueError(f"{name} must be a 1-D array.")
+    if dtype == torch.int32:
+        if t.is_floating_point() or t.is_complex() or t.dtype == torch.bool:
+            raise TypeError(f"{name} must be an integer array.")
+        if t.numel() and t.dtype != torch.int32 and (int(t.min()) < -2**31 or int(t.max()) > 2**31 - 1):
+            raise ValueError(f"{name}: index does not fit in int32.")
+    return t.to(device=torch.device("cuda", device), dtype=dtype).contiguous()
+
+
 def _ptr(arr: np.ndarray):
     return C.c_void_p(arr.ctypes.data) if arr.size else C.c_void_p(0)
 
@@ -188,14 +204,26 @@ class _CholeskySolver:
         store = _ffi.STORE_F32 if self._precision == 0 else _ffi.STORE_F64
         if self._refine:
             store = _ffi.STORE_F32 | _ffi.STORE_F64 | _ffi.STORE_A64
-        hi = _host_vector(ii, np.int32, "ii")
-        hj = _host_vector(jj, np.int32, "jj")
-        hx = _host_vector(x, np.float64, "x")
         torch = _torch()
         h = C.c_void_p()
-        with torch.cuda.device(device):
-            st = lib.gbchol_create(n_rows, int(nx), _ptr(hi), _ptr(hj), _ptr(hx), int(type),
-                                   store, C.byref(h))
+        if os.environ.get("GBCHOL_HOST_PREP") == "1":  # the host conversion (gbchol_create)
+            hi = _host_vector(ii, np.int32, "ii")
+            hj = _host_vector(jj, np.int32, "jj")
+            hx = _host_vector(x, np.float64, "x")
+            with torch.cuda.device(device):
+                st = lib.gbchol_create(n_rows, int(nx), _ptr(hi), _ptr(hj), _ptr(hx), int(type),
+                                       store, C.byref(h))
+        else:
+            # the input conversion on the GPU (gbchol_create_device)
+            with torch.cuda.device(device):
+                di = _device_vector(ii, torch.int32, device, "ii")
+                dj = _device_vector(jj, torch.int32, device, "jj")
+                dx = _device_vector(x, torch.float64, device, "x")
+                torch.cuda.current_stream(device).synchronize()
+                st = lib.gbchol_create_device(n_rows, int(nx), C.c_void_p(di.data_ptr() if di.numel() else 0),
+                                              C.c_void_p(dj.data_ptr() if dj.numel() else 0),
+                                              C.c_void_p(dx.data_ptr() if dx.numel() else 0), int(type), store,
+                                              C.byref(h))
         _ffi.check(st)
         self._h = h
         self._n = n_rows

@@ -74,6 +74,18 @@ int gbchol_create(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t*
                   const double* x, int32_t matrix_type, int32_t store, gbchol_handle* out);
 
 /*
+ * gbchol_create for inputs that already live on the current CUDA device
+ * (ii, jj, x device pointers, same meaning as gbchol_create): the COO / CSR /
+ * CSC -> sorted, duplicate-summed CSC conversion runs on the GPU (equal, bit
+ * for bit, to gbchol_create's host conversion), then the CSC goes to the host
+ * for the factorisation. The reference instead copies device inputs to the
+ * host and converts them there (src/main.cpp:47-67,
+ * src/cholesky_solver.cpp:8-149).
+ */
+int gbchol_create_device(int32_t n_rows, int64_t nnz, const int32_t* ii, const int32_t* jj, const double* x,
+                         int32_t matrix_type, int32_t store, gbchol_handle* out);
+
+/*
  * Analyse an existing factor (the hot-path boundary proper): perm[k] is the
  * original row at position k (CHOLMOD Perm), L is given in CSC with sorted
  * rows and the diagonal first in each column (cholmod_factor_to_sparse,
