@@ -230,6 +230,19 @@ int setup_snb(gbchol_solver* h) {
     return GBCHOL_OK;
 }
 
+// Uploads FP64 values and/or their FP32 copy: with both, the FP64 array goes
+// up once and is cast on the device (the FP32 result equals the host cast).
+cudaError_t upload_values(DevBuf<float>& d32, DevBuf<double>& d64, const std::vector<double>& src, bool f32,
+                          bool f64) {
+    if (!f64) return f32 ? upload_cast(d32, src) : cudaSuccess;
+    cudaError_t e = d64.upload(src.data(), src.size());
+    if (e != cudaSuccess || !f32) return e;
+    e = d32.alloc(src.size());
+    if (e != cudaSuccess) return e;
+    e = cast_to_f32(d64.p, d32.p, (int64_t)src.size(), nullptr);
+    return e != cudaSuccess ? e : cudaDeviceSynchronize();
+}
+
 // Builds the solve plan from the factor and the level orders and uploads it.
 int setup_plan(gbchol_solver* h) {
     const Factor& F = h->F;
@@ -245,18 +258,15 @@ int setup_plan(gbchol_solver* h) {
     CUDA_TRY(h->lo_rowptr.upload(P.lo_rowptr.data(), P.lo_rowptr.size()));
     CUDA_TRY(h->lo_cols.upload(P.lo_cols.data(), P.lo_cols.size()));
     CUDA_TRY(h->lo_tasks.upload(P.lo_tasks.data(), P.lo_tasks.size()));
-    if (f32) CUDA_TRY(upload_cast(h->lo_v32, P.lo_vals));
-    if (f64) CUDA_TRY(h->lo_v64.upload(P.lo_vals.data(), P.lo_vals.size()));
+    CUDA_TRY(upload_values(h->lo_v32, h->lo_v64, P.lo_vals, f32, f64));
     // upper leaf sweep: top-row part (partial pass) and diagonal + leaf part
     CUDA_TRY(h->upt_rowptr.upload(P.upt_rowptr.data(), P.upt_rowptr.size()));
     CUDA_TRY(h->upt_cols.upload(P.upt_cols.data(), P.upt_cols.size()));
     CUDA_TRY(h->upt_tasks.upload(P.upt_tasks.data(), P.upt_tasks.size()));
-    if (f32) CUDA_TRY(upload_cast(h->upt_v32, P.upt_vals));
-    if (f64) CUDA_TRY(h->upt_v64.upload(P.upt_vals.data(), P.upt_vals.size()));
+    CUDA_TRY(upload_values(h->upt_v32, h->upt_v64, P.upt_vals, f32, f64));
     CUDA_TRY(h->up_rowptr.upload(P.upl_rowptr.data(), P.upl_rowptr.size()));
     CUDA_TRY(h->up_cols.upload(P.upl_cols.data(), P.upl_cols.size()));
-    if (f32) CUDA_TRY(upload_cast(h->up_v32, P.upl_vals));
-    if (f64) CUDA_TRY(h->up_v64.upload(P.upl_vals.data(), P.upl_vals.size()));
+    CUDA_TRY(upload_values(h->up_v32, h->up_v64, P.upl_vals, f32, f64));
     P.upt_vals.clear();
     P.upt_vals.shrink_to_fit();
     P.upl_vals.clear();
@@ -264,14 +274,12 @@ int setup_plan(gbchol_solver* h) {
     CUDA_TRY(h->up_tasks.upload(P.up_tasks.data(), P.up_tasks.size()));
     // top region
     CUDA_TRY(h->sn_rows.upload(P.sn_rows.data(), P.sn_rows.size()));
-    if (f32) CUDA_TRY(upload_cast(h->pan32, P.panels));
-    if (f64) CUDA_TRY(h->pan64.upload(P.panels.data(), P.panels.size()));
+    CUDA_TRY(upload_values(h->pan32, h->pan64, P.panels, f32, f64));
     CUDA_TRY(h->units.upload(P.units.data(), P.units.size()));
     CUDA_TRY(h->order_lo.upload(P.unit_order_lo.data(), P.unit_order_lo.size()));
     CUDA_TRY(h->unit_of_row.upload(P.unit_of_row.data(), P.unit_of_row.size()));
     CUDA_TRY(h->order_up.upload(P.unit_order_up.data(), P.unit_order_up.size()));
-    if (f32) CUDA_TRY(upload_cast(h->dinv32, P.dinv));
-    if (f64) CUDA_TRY(h->dinv64.upload(P.dinv.data(), P.dinv.size()));
+    CUDA_TRY(upload_values(h->dinv32, h->dinv64, P.dinv, f32, f64));
     P.dinv.clear();
     P.dinv.shrink_to_fit();
     CUDA_TRY(h->counters.alloc(10));

@@ -176,6 +176,11 @@ __global__ void merge_kernel(int32_t n, const int32_t* __restrict__ ptr, const i
     }
 }
 
+__global__ void cast_kernel(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) dst[k] = (float)src[k];
+}
+
 int grid_for(int64_t items) {
     const int64_t b = (items + kT - 1) / kT;
     return (int)(b < 4096 ? (b > 0 ? b : 1) : 4096);
@@ -246,6 +251,12 @@ cudaError_t device_csc(int32_t n, int64_t nnz, const int32_t* ii, const int32_t*
     cleanup();
     out.n = n;
     return cudaSuccess;
+}
+
+cudaError_t cast_to_f32(const double* src, float* dst, int64_t n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    cast_kernel<<<grid_for(n), kT, 0, s>>>(src, dst, n);
+    return cudaGetLastError();
 }
 
 void DeviceCsc::release() {

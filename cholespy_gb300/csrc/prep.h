@@ -24,4 +24,7 @@ struct DeviceCsc {
 cudaError_t device_csc(int32_t n, int64_t nnz, const int32_t* ii, const int32_t* jj, const double* x, int32_t fmt,
                        DeviceCsc& out, int* bad_index, cudaStream_t s);
 
+// dst[k] = (float)src[k] (round to nearest even, as the host cast), device arrays.
+cudaError_t cast_to_f32(const double* src, float* dst, int64_t n, cudaStream_t s);
+
 }  // namespace gbchol

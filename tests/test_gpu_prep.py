@@ -103,3 +103,26 @@ def test_device_prep_errors(cuda):
     with pytest.raises(ValueError, match="Sparse CSR matrix: Invalid pointer array."):
         CholeskySolverF(n, torch.tensor(ptr, device="cuda"), torch.tensor(jj[order], device="cuda"),
                         torch.tensor(x[order], device="cuda"), MatrixType.CSR)
+
+
+def test_device_cast_matches_host_cast(cuda):
+    """A solver keeping both factors casts its FP32 copy on the device; an
+    FP32-only solver casts on the host. Same factor and plan, so their FP32
+    solves agree bit for bit."""
+    from cholespy_gb300 import CholeskySolverD, CholeskySolverF, MatrixType, _ffi
+    torch = cuda
+    n, (ii, jj, x), _ = _inputs("grid3d_16")
+    args = (torch.tensor(ii, device="cuda"), torch.tensor(jj, device="cuda"), torch.tensor(x, device="cuda"),
+            MatrixType.COO)
+    sf = CholeskySolverF(n, *args)
+    sd = CholeskySolverD(n, *args, refine=True)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for nrhs in (1, 8, 64, 128):
+        b = torch.randn(n, nrhs, device="cuda", dtype=torch.float32)
+        x1, x2 = torch.zeros_like(b), torch.zeros_like(b)
+        _ffi.check(_ffi.lib().gbchol_solve(sf.handle, 0, nrhs, C.c_void_p(b.data_ptr()), C.c_void_p(x1.data_ptr()),
+                                           stream))
+        _ffi.check(_ffi.lib().gbchol_solve(sd.handle, 0, nrhs, C.c_void_p(b.data_ptr()), C.c_void_p(x2.data_ptr()),
+                                           stream))
+        torch.cuda.synchronize()
+        assert torch.equal(x1, x2)
