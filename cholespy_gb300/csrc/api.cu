@@ -192,6 +192,7 @@ int setup_snb(gbchol_solver* h) {
     if (const char* env = std::getenv("GBCHOL_BULK_BLK_NS")) so.blk_ns = std::atoll(env);
     if (const char* env = std::getenv("GBCHOL_BULK_BASE_NS")) so.base_ns = std::atoll(env);
     so.max_cols = snb_group_cols(h->snb_tc || h->snb_tc_groups);
+    if (const char* env = std::getenv("GBCHOL_BULK_ORDER")) so.order_by_finish = std::atoi(env) != 0;
     if (const char* env = std::getenv("GBCHOL_BULK_GROUP_COLS"))
         so.max_cols = std::min(so.max_cols, std::max(32, std::atoi(env)));
     SnbLowerPlan L;

@@ -463,7 +463,26 @@ void build_snb_lower(const SolvePlan& P, const SnbUpperPlan& B, const SnbOptions
     L.unit_info.assign((size_t)nunits * 4, 0);
     L.parts.clear();
     L.groups.clear();
-    for (int32_t u = 0; u < nunits; ++u) {
+    // estimated starts (as in build_plan): an item should start when its work
+    // before its last wait is just done as that wait ends; the key is that
+    // start and at least one more than the key of every item it waits on, so
+    // sorting by key is a topological order
+    struct Est {
+        int64_t first = INT64_MAX, last = 0, key_dep = -1;
+        void dep(int64_t fin, int64_t key, int64_t lat) {
+            first = std::min(first, fin + lat);
+            last = std::max(last, fin + lat);
+            key_dep = std::max(key_dep, key);
+        }
+        int64_t done(int64_t nblocks, int64_t base, int64_t blk, int64_t& key) const {
+            const int64_t f = first == INT64_MAX ? 0 : first;
+            key = std::max({f, last - std::max<int64_t>(0, nblocks - 1) * blk, key_dep + 1});
+            return std::max(std::max(key, last) + base + blk, key + base + blk * std::max<int64_t>(1, nblocks));
+        }
+    };
+    std::vector<int64_t> fin_u((size_t)nunits, 0), key_u((size_t)nunits, 0);
+    std::vector<int64_t> fin_p, key_p;
+    for (int32_t u = 0; u < nunits; ++u) {  // sources precede their destinations
         const SnUnit& U = P.units[u];
         const int32_t chain = U.pos0 > 0 ? 1 : 0;
         const int32_t end = U.contrib_end - chain;
@@ -484,6 +503,13 @@ void build_snb_lower(const SolvePlan& P, const SnbUpperPlan& B, const SnbOptions
             L.groups.push_back(g);
             e = f;
         }
+        // the unit applies its groups in the order their sources are
+        // estimated to finish (source order otherwise: the subtrees of a
+        // separator run side by side, so their blocks would wait for each other)
+        if (o.order_by_finish)
+            std::stable_sort(L.groups.begin() + g0, L.groups.end(), [&](const SnbGroup& x, const SnbGroup& y) {
+                return fin_u[x.src_unit] < fin_u[y.src_unit];
+            });
         const int32_t ng_u = (int32_t)L.groups.size() - g0;
         int32_t first = g0;
         const int32_t pb = (int32_t)L.parts.size();
@@ -499,46 +525,27 @@ void build_snb_lower(const SolvePlan& P, const SnbUpperPlan& B, const SnbOptions
             }
             first = split;
         }
+        const int32_t pe = (int32_t)L.parts.size();
         L.unit_info[(size_t)u * 4] = first;
         L.unit_info[(size_t)u * 4 + 1] = (int32_t)L.groups.size();
         L.unit_info[(size_t)u * 4 + 2] = pb;
-        L.unit_info[(size_t)u * 4 + 3] = (int32_t)L.parts.size();
-    }
-    // estimated starts (as in build_plan): an item should start when its work
-    // before its last wait is just done as that wait ends; the key is that
-    // start and at least one more than the key of every item it waits on, so
-    // sorting by key is a topological order
-    struct Est {
-        int64_t first = INT64_MAX, last = 0, key_dep = -1;
-        void dep(int64_t fin, int64_t key, int64_t lat) {
-            first = std::min(first, fin + lat);
-            last = std::max(last, fin + lat);
-            key_dep = std::max(key_dep, key);
-        }
-        int64_t done(int64_t nblocks, int64_t base, int64_t blk, int64_t& key) const {
-            const int64_t f = first == INT64_MAX ? 0 : first;
-            key = std::max({f, last - std::max<int64_t>(0, nblocks - 1) * blk, key_dep + 1});
-            return std::max(std::max(key, last) + base + blk, key + base + blk * std::max<int64_t>(1, nblocks));
-        }
-    };
-    const int32_t nparts = (int32_t)L.parts.size();
-    std::vector<int64_t> fin_u((size_t)nunits, 0), key_u((size_t)nunits, 0);
-    std::vector<int64_t> fin_p((size_t)nparts, 0), key_p((size_t)nparts, 0);
-    for (int32_t u = 0; u < nunits; ++u) {  // sources precede their destinations
-        const SnUnit& U = P.units[u];
+        L.unit_info[(size_t)u * 4 + 3] = pe;
+        fin_p.resize((size_t)pe);
+        key_p.resize((size_t)pe);
         Est eu;
-        for (int32_t q = L.unit_info[(size_t)u * 4 + 2]; q < L.unit_info[(size_t)u * 4 + 3]; ++q) {
+        for (int32_t q = pb; q < pe; ++q) {
             Est eq;
             for (int32_t e = L.parts[q].contrib_begin; e < L.parts[q].contrib_end; ++e)
                 eq.dep(fin_u[L.groups[e].src_unit], key_u[L.groups[e].src_unit], o.lat_ns);
             fin_p[q] = eq.done(L.parts[q].contrib_end - L.parts[q].contrib_begin, o.base_ns, o.blk_ns, key_p[q]);
             eu.dep(fin_p[q], key_p[q], o.lat_ns);
         }
-        const int32_t gf = L.unit_info[(size_t)u * 4], ge = L.unit_info[(size_t)u * 4 + 1];
-        for (int32_t e = gf; e < ge; ++e) eu.dep(fin_u[L.groups[e].src_unit], key_u[L.groups[e].src_unit], o.lat_ns);
-        if (U.pos0 > 0) eu.dep(fin_u[u - 1], key_u[u - 1], o.lat_ns);  // the chain unit
-        fin_u[u] = eu.done(ge - gf + (U.pos0 > 0 ? 1 : 0), o.base_ns, o.blk_ns, key_u[u]);
+        const int32_t ge = (int32_t)L.groups.size();
+        for (int32_t e = first; e < ge; ++e) eu.dep(fin_u[L.groups[e].src_unit], key_u[L.groups[e].src_unit], o.lat_ns);
+        if (chain) eu.dep(fin_u[u - 1], key_u[u - 1], o.lat_ns);  // the chain unit
+        fin_u[u] = eu.done(ge - first + chain, o.base_ns, o.blk_ns, key_u[u]);
     }
+    const int32_t nparts = (int32_t)L.parts.size();
     std::vector<int64_t> fin_up((size_t)nunits, 0), key_up((size_t)nunits, 0);
     for (int32_t u = nunits - 1; u >= 0; --u) {  // the upper sweep waits on later units
         const SnUnit& U = P.units[u];

@@ -143,6 +143,7 @@ struct SnbOptions {
     int32_t keep = 16;
     int32_t group = 0;        // 0: no partial sums
     int32_t max_cols = 64;    // source columns per group (32: no merging)
+    bool order_by_finish = true;  // a unit's groups in estimated source-finish order (else source order)
     int64_t lat_ns = 1000;    // flag latency
     int64_t base_ns = 5000;   // fixed cost of an item (diagonal solve, chain step)
     // cost of one block. Measured at 64^3, 128 RHS (5.99 / 5.87 / 5.79 /

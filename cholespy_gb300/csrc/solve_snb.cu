@@ -341,17 +341,20 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             }
         }
     } else {
-        // ---- consumers: thread = one RHS column k and NR unit rows (lower)
-        // / columns (upper) from r0
-        constexpr int G = TC ? 4 : SW / 32;  // consumer warps across the RHS columns (TC: 128 accumulator lanes)
-        constexpr int NR = 32 * G / kCW;  // rows / columns per consumer thread
-        const int k = 32 * (warp % G) + lane;
-        const int r0 = NR * (warp / G);
+        // ---- consumers: thread = 4 consecutive RHS columns (k4 .. k4 + 3)
+        // x RR unit rows (lower) / columns (upper); warp w owns rows 4w ..
+        // 4w + 3 (with 64 columns, the warp's two half-warps take two rows
+        // each), so a warp skips a block without rows in its group whole
+        constexpr int KG = SW / 4;        // RHS groups of 4: 32 or 16
+        constexpr int RR = KG / 8;        // rows per thread: 4 or 2
+        const int kg = lane % KG;
+        const int k4 = 4 * kg;
+        const int r0 = 4 * warp + (lane / KG) * RR;
+        const bool kin = k4 < nrhs;       // nrhs is a multiple of 4: all four columns or none
         uint32_t gs = 0;
         for (uint32_t n = 0;; ++n) {
             const int slot = (int)(n & 1);
             bulk::mbar_wait(&sm.item_full[slot], (n >> 1) & 1, a.status);
-            static_assert(!TC || (SW == 128 && 32 * 4 / kCW == 16), "tensor-core mapping: 128 lanes x 16 columns");
             if (!sm.item_valid[slot]) break;
             const int v = sm.item_v[slot];
             const SnUnit U = sm.item_unit[slot];
@@ -359,12 +362,14 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             if (lane == 0) bulk::mbar_arrive(&sm.item_empty[slot]);  // the descriptor has been read
             const SnbItem it = snb_item<LOWER>(a, v, U);
             const int uidx = it.uidx, w = U.w;
-            // the unit's current right-hand side (my rows, my column)
-            float tv[NR];
+            // the unit's current right-hand side (my rows, my columns)
+            float4 tv[RR];
 #pragma unroll
-            for (int r = 0; r < NR; ++r) {
+            for (int r = 0; r < RR; ++r) {
                 const int i = r0 + r;
-                tv[r] = (!it.part && i < w && k < nrhs) ? __ldcg(a.tmp + (size_t)(U.c0 + i) * nrhs + k) : 0.f;
+                tv[r] = (!it.part && i < w && kin)
+                            ? __ldcg(reinterpret_cast<const float4*>(a.tmp + (size_t)(U.c0 + i) * nrhs + k4))
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
             }
             // E and M to shared memory (read after the consumers' barrier
             // below; the previous item's readers passed its last barrier)
@@ -378,9 +383,9 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                     if (it.chain) (&sm.m[0][0])[idx] = mc[idx];
                 }
             }
-            float acc[NR];
+            float4 acc[RR];
 #pragma unroll
-            for (int r = 0; r < NR; ++r) acc[r] = 0.f;
+            for (int r = 0; r < RR; ++r) acc[r] = make_float4(0.f, 0.f, 0.f, 0.f);
             for (int b = 0; b < it.nblk; ++b) {
                 const uint32_t g = gs + (uint32_t)b;
                 const int s = (int)(g % kStages);
@@ -400,60 +405,62 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                     continue;
                 }
                 const int ext = sm.ext[s];
-                // 4-row groups of my rows (columns) the block has: the others hold zeros
-                const unsigned grp = sm.mask[s] >> r0;
+                // the warp's 4 rows (columns): a block without any is skipped
+                const bool mine = ((sm.mask[s] >> (4 * warp)) & 0xFu) != 0 && kin;
                 const auto& st = sm.st[s];
-                int j = 0;
-                // four block rows at a time: their loads go out together
-                for (; j + 4 <= ext; j += 4) {
-                    float xj[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) xj[u] = st.x[(j + u) * nrhs + k];
-#pragma unroll
-                    for (int q = 0; q < NR / 4; ++q) {
-                        if (!((grp >> (4 * q)) & 0xFu)) continue;  // warp-uniform
-                        float4 lv[4];
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) lv[u] = reinterpret_cast<const float4*>(&st.l[j + u][r0])[q];
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            acc[4 * q] = fmaf(lv[u].x, xj[u], acc[4 * q]);
-                            acc[4 * q + 1] = fmaf(lv[u].y, xj[u], acc[4 * q + 1]);
-                            acc[4 * q + 2] = fmaf(lv[u].z, xj[u], acc[4 * q + 2]);
-                            acc[4 * q + 3] = fmaf(lv[u].w, xj[u], acc[4 * q + 3]);
+                if (mine) {
+                    auto step = [&](int j) {
+                        const float4 xv = *reinterpret_cast<const float4*>(&st.x[j * nrhs + k4]);
+                        float lr[RR];
+                        if constexpr (RR == 4) {
+                            const float4 l4 = *reinterpret_cast<const float4*>(&st.l[j][r0]);
+                            lr[0] = l4.x; lr[1] = l4.y; lr[2] = l4.z; lr[3] = l4.w;
+                        } else {
+                            const float2 l2 = *reinterpret_cast<const float2*>(&st.l[j][r0]);
+                            lr[0] = l2.x; lr[1] = l2.y;
                         }
-                    }
-                }
-                for (; j < ext; ++j) {
-                    const float xv = st.x[j * nrhs + k];
-                    const float4* lr = reinterpret_cast<const float4*>(&st.l[j][r0]);
 #pragma unroll
-                    for (int q = 0; q < NR / 4; ++q) {
-                        if (!((grp >> (4 * q)) & 0xFu)) continue;  // warp-uniform
-                        const float4 lv = lr[q];
-                        acc[4 * q] = fmaf(lv.x, xv, acc[4 * q]);
-                        acc[4 * q + 1] = fmaf(lv.y, xv, acc[4 * q + 1]);
-                        acc[4 * q + 2] = fmaf(lv.z, xv, acc[4 * q + 2]);
-                        acc[4 * q + 3] = fmaf(lv.w, xv, acc[4 * q + 3]);
+                        for (int r = 0; r < RR; ++r) {
+                            acc[r].x = fmaf(lr[r], xv.x, acc[r].x);
+                            acc[r].y = fmaf(lr[r], xv.y, acc[r].y);
+                            acc[r].z = fmaf(lr[r], xv.z, acc[r].z);
+                            acc[r].w = fmaf(lr[r], xv.w, acc[r].w);
+                        }
+                    };
+                    int j = 0;
+                    for (; j + 4 <= ext; j += 4) {
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) step(j + u);
                     }
+                    for (; j < ext; ++j) step(j);
                 }
                 __syncwarp();
                 if (lane == 0) bulk::mbar_arrive(&sm.empty[s]);
             }
             gs += (uint32_t)it.nblk;
             if constexpr (TC) {
-                if (it.nblk > 0) {  // the accumulator: my 16 columns of lane k
+                // the accumulator (lane = RHS column, 16 columns = unit rows
+                // per warp) goes through shared memory into this mapping
+                if (it.nblk > 0) {
                     bulk::mbar_wait(&sm.tc.mma_done, (gs - 1) & 1, a.status);
                     tc::fence_after_sync();
-                    tc::ld16(sm.tc.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)r0, acc);
+                    float t16[16];
+                    const int kk = 32 * (warp & 3) + lane, rr0 = 16 * (warp >> 2);
+                    tc::ld16(sm.tc.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)rr0, t16);
                     tc::fence_before_sync();  // ordered before the next item's MMAs (barriers below)
+#pragma unroll
+                    for (int r = 0; r < 16; ++r) sm.t[rr0 + r][kk] = t16[r];
+                    bulk::named_sync(1, kCW * 32);
+#pragma unroll
+                    for (int r = 0; r < RR; ++r) acc[r] = *reinterpret_cast<const float4*>(&sm.t[r0 + r][k4]);
+                    bulk::named_sync(1, kCW * 32);
                 }
             }
             if (it.part) {  // the sum goes to the partial's slot, then its flag
                 float* ps = a.pbuf + (size_t)(~v) * 32 * nrhs;
-                if (k < nrhs) {
+                if (kin) {
 #pragma unroll
-                    for (int r = 0; r < NR; ++r) ps[(r0 + r) * nrhs + k] = acc[r];
+                    for (int r = 0; r < RR; ++r) *reinterpret_cast<float4*>(ps + (r0 + r) * nrhs + k4) = acc[r];
                 }
                 bulk::named_sync(1, kCW * 32);
                 if (tid == 0) dev::st_release(a.uflags + a.n_units + ~v, epoch);
@@ -465,30 +472,34 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                     if (lane == 0) dev::wait_geq(a.uflags + a.n_units + q, epoch, a.status);
                     __syncwarp();
                     const float* ps = a.pbuf + (size_t)q * 32 * nrhs;
-                    if (k < nrhs) {
+                    if (kin) {
 #pragma unroll
-                        for (int r = 0; r < NR; ++r) acc[r] += __ldcg(ps + (r0 + r) * nrhs + k);
+                        for (int r = 0; r < RR; ++r) {
+                            const float4 p4 = __ldcg(reinterpret_cast<const float4*>(ps + (r0 + r) * nrhs + k4));
+                            acc[r].x += p4.x; acc[r].y += p4.y; acc[r].z += p4.z; acc[r].w += p4.w;
+                        }
                     }
                 }
             }
 #pragma unroll
-            for (int r = 0; r < NR; ++r) sm.t[r0 + r][k] = tv[r] - acc[r];
+            for (int r = 0; r < RR; ++r)
+                *reinterpret_cast<float4*>(&sm.t[r0 + r][k4 < SW ? k4 : 0]) =
+                    make_float4(tv[r].x - acc[r].x, tv[r].y - acc[r].y, tv[r].z - acc[r].z, tv[r].w - acc[r].w);
             bulk::named_sync(1, kCW * 32);
-            // x = E t' (my rows, my column)
-            float xv[NR];
+            // x = E t' (my rows, my columns)
+            float4 xv[RR];
 #pragma unroll
-            for (int r = 0; r < NR; ++r) xv[r] = 0.f;
+            for (int r = 0; r < RR; ++r) xv[r] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 4
             for (int j = 0; j < 32; ++j) {
-                const float tj = sm.t[j][k];
-                const float4* er = reinterpret_cast<const float4*>(&sm.e[j][r0]);
+                const float4 tj = *reinterpret_cast<const float4*>(&sm.t[j][k4 < SW ? k4 : 0]);
 #pragma unroll
-                for (int q = 0; q < NR / 4; ++q) {
-                    const float4 ev = er[q];
-                    xv[4 * q] = fmaf(ev.x, tj, xv[4 * q]);
-                    xv[4 * q + 1] = fmaf(ev.y, tj, xv[4 * q + 1]);
-                    xv[4 * q + 2] = fmaf(ev.z, tj, xv[4 * q + 2]);
-                    xv[4 * q + 3] = fmaf(ev.w, tj, xv[4 * q + 3]);
+                for (int r = 0; r < RR; ++r) {
+                    const float ev = sm.e[j][r0 + r];
+                    xv[r].x = fmaf(ev, tj.x, xv[r].x);
+                    xv[r].y = fmaf(ev, tj.y, xv[r].y);
+                    xv[r].z = fmaf(ev, tj.z, xv[r].z);
+                    xv[r].w = fmaf(ev, tj.w, xv[r].w);
                 }
             }
             if (it.chain) {
@@ -497,37 +508,34 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                 const int cw = LOWER ? 32 : min(32, U.sn_w - (U.pos0 + w));  // its width
                 if (lane == 0) dev::wait_geq(a.uflags + cu, epoch, a.status);
                 __syncwarp();
-                float xc[32];
+                if (kin) {
 #pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    xc[j] = (j < cw && k < nrhs) ? __ldcg(a.tmp + (size_t)(crow + j) * nrhs + k) : 0.f;
+                    for (int j0 = 0; j0 < 32; j0 += 8) {
+                        float4 xc[8];
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const float4* mr = reinterpret_cast<const float4*>(&sm.m[j][r0]);
+                        for (int u = 0; u < 8; ++u)
+                            xc[u] = (j0 + u < cw) ? __ldcg(reinterpret_cast<const float4*>(
+                                                        a.tmp + (size_t)(crow + j0 + u) * nrhs + k4))
+                                                  : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-                    for (int q = 0; q < NR / 4; ++q) {
-                        const float4 mv = mr[q];
-                        xv[4 * q] = fmaf(-mv.x, xc[j], xv[4 * q]);
-                        xv[4 * q + 1] = fmaf(-mv.y, xc[j], xv[4 * q + 1]);
-                        xv[4 * q + 2] = fmaf(-mv.z, xc[j], xv[4 * q + 2]);
-                        xv[4 * q + 3] = fmaf(-mv.w, xc[j], xv[4 * q + 3]);
+                        for (int u = 0; u < 8; ++u) {
+#pragma unroll
+                            for (int r = 0; r < RR; ++r) {
+                                const float mv = sm.m[j0 + u][r0 + r];
+                                xv[r].x = fmaf(-mv, xc[u].x, xv[r].x);
+                                xv[r].y = fmaf(-mv, xc[u].y, xv[r].y);
+                                xv[r].z = fmaf(-mv, xc[u].z, xv[r].z);
+                                xv[r].w = fmaf(-mv, xc[u].w, xv[r].w);
+                            }
+                        }
                     }
                 }
             }
-            if (k < nrhs) {
+            if (kin) {
 #pragma unroll
-                for (int r = 0; r < NR; ++r) {
+                for (int r = 0; r < RR; ++r) {
                     const int i = r0 + r;
-                    if (i < w) {
-                        a.tmp[(size_t)(U.c0 + i) * nrhs + k] = xv[r];
-                        if (!LOWER && a.out) {
-                            using TO = typename io::tout;
-                            TO* out = static_cast<TO*>(a.out);
-                            const size_t oo = (size_t)a.perm[U.c0 + i] * nrhs + k;
-                            if (io::accum) out[oo] += (TO)xv[r];
-                            else out[oo] = (TO)xv[r];
-                        }
-                    }
+                    if (i < w) *reinterpret_cast<float4*>(a.tmp + (size_t)(U.c0 + i) * nrhs + k4) = xv[r];
                 }
             }
             // the barrier orders the consumers' writes before the release

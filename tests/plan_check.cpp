@@ -362,24 +362,24 @@ int check_snb(const SolvePlan& P, const SnbOptions& o) {
         const int32_t first = L.unit_info[(size_t)u * 4], gend = L.unit_info[(size_t)u * 4 + 1],
                       pb = L.unit_info[(size_t)u * 4 + 2], pe = L.unit_info[(size_t)u * 4 + 3];
         const int32_t chain = U.pos0 > 0 ? 1 : 0;
-        // groups cover [contrib_begin, contrib_end - chain) in order
-        int32_t e = U.contrib_begin;
+        // the groups cover [contrib_begin, contrib_end - chain) exactly once
+        // (in any order: a unit applies them by estimated source finish)
+        std::vector<char> seen((size_t)(U.contrib_end - U.contrib_begin), 0);
         for (int32_t g = gat; g < gend; ++g) {
             const SnbGroup& G = L.groups[g];
-            bad += G.first != e;
-            int32_t cols = 0, f = e;
-            while (cols < G.cols && f < U.contrib_end - chain) {
+            int32_t cols = 0, f = G.first;
+            bad += G.first < U.contrib_begin || G.first >= U.contrib_end - chain;
+            while (cols < G.cols && f >= U.contrib_begin && f < U.contrib_end - chain) {
                 const SnContrib& C = P.contribs[f];
-                bad += C.rowmask != G.rowmask || C.xcol != G.xcol + cols;
+                bad += C.rowmask != G.rowmask || C.xcol != G.xcol + cols || seen[f - U.contrib_begin]++ != 0;
                 if (cols + C.w < G.cols) bad += C.w != kChunk;
                 cols += C.w;
                 ++f;
             }
             bad += cols != G.cols || G.cols > std::max(o.max_cols, kChunk) || P.contribs[f - 1].src_unit != G.src_unit;
             bad += tu[G.src_unit] < 0 || tu[G.src_unit] >= tu[u];
-            e = f;
         }
-        bad += e != U.contrib_end - chain;
+        for (int32_t e = U.contrib_begin; e < U.contrib_end - chain; ++e) bad += seen[e - U.contrib_begin] != 1;
         if (chain) bad += tu[u - 1] >= tu[u];
         int32_t at = gat;
         for (int32_t q = pb; q < pe; ++q) {
@@ -444,7 +444,7 @@ int main() {
         po.part_group = cs.group;
         build_plan(F, lo, up, po, P);
         if (cs.group == 0) {  // the bulk schedule is built on plans without 32-column partial sums
-            for (const SnbOptions& so : {SnbOptions{}, SnbOptions{2, 3, 32, 1000, 3000, 500}, SnbOptions{0, 1, 128, 10, 10, 10}}) {
+            for (const SnbOptions& so : {SnbOptions{}, SnbOptions{2, 3, 32, false, 1000, 3000, 500}, SnbOptions{0, 1, 128, true, 10, 10, 10}}) {
                 const int bad = check_snb(P, so);
                 std::printf("%dD k=%d minw=%d bulk keep=%d group=%d: checks failed %d %s\n", cs.dim, cs.k, cs.minw,
                             so.keep, so.group, bad, bad ? "FAIL" : "ok");
