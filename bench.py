@@ -76,7 +76,7 @@ MEASURED_SOLVE_TRAFFIC_F32 = {}
 
 
 def plan_signature(info, nrhs):
-    kernel = "bulk" if (32 < nrhs <= 128 and nrhs % 4 == 0) else "sliced"
+    kernel = "bulk" if (12 <= nrhs <= 128 and nrhs % 4 == 0) else "sliced"
     return (int(info.n), int(info.nnz_l), int(info.top_units), int(info.top_blocks), int(nrhs), kernel)
 
 
@@ -426,9 +426,9 @@ def run_ours(args, world, rank, local):
                          f"semantics) on the same factor, RHS split over threads; 1 warm-up + {calls} "
                          f"timed calls, {cdt:.1f} s"}
 
-    # the bulk supernodal sweeps (33..128 RHS, multiples of 4) add one launch:
+    # the bulk supernodal sweeps (12..128 RHS, multiples of 4) add one launch:
     # the scatter of the top rows' solution
-    lps = info.launches_per_solve + (1 if (32 < args.nrhs <= 128 and args.nrhs % 4 == 0) else 0)
+    lps = info.launches_per_solve + (1 if (12 <= args.nrhs <= 128 and args.nrhs % 4 == 0) else 0)
     launches = lps + (args.max_iter + 1) + args.max_iter * lps
     line = {
         "metric": HEADLINE_METRIC,

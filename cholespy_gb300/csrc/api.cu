@@ -441,7 +441,7 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
     sn.sys0.pbuf = static_cast<unsigned char*>(work) +
                    ((size_t)h->n * nrhs * (f32 ? sizeof(float) : sizeof(double)) + 255) / 256 * 256;
     if (use_snb(h, nrhs, f32)) {
-        // 33..128 RHS: the bulk-copy supernodal sweeps (solve_snb.cu)
+        // 12..128 RHS (multiples of 4): the bulk-copy supernodal sweeps (solve_snb.cu)
         SnbArgs b;
         b.units = h->units.p;
         b.contribs = h->contribs.p;

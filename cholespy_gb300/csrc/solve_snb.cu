@@ -3,7 +3,7 @@
 // Same work decomposition as solve_sn.cu (units of <= 32 columns of the
 // top-region supernodes, atomic tickets in estimated-start order, epoch-
 // valued unit flags, the chain block folded into the diagonal solve), shaped
-// for 33..128 RHS:
+// for 12..128 RHS (multiples of 4):
 //
 // * One work item = one unit and every RHS column, so each L block is read
 //   once per solve instead of once per 32-column slice. Long lower-sweep
@@ -103,6 +103,21 @@ struct SnbIO {
     using tout = TO;
     static constexpr bool accum = ACCUM;
 };
+
+// RR consecutive floats of shared memory (16-, 8- or 4-byte aligned by the
+// consumers' row mapping), in one load.
+template <int RR>
+__device__ __forceinline__ void load_rows(const float* p, float (&v)[RR]) {
+    if constexpr (RR == 4) {
+        const float4 q = *reinterpret_cast<const float4*>(p);
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else if constexpr (RR == 2) {
+        const float2 q = *reinterpret_cast<const float2*>(p);
+        v[0] = q.x; v[1] = q.y;
+    } else {
+        v[0] = p[0];
+    }
+}
 
 // Item geometry shared by the producer and the consumers.
 struct SnbItem {
@@ -343,10 +358,10 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
     } else {
         // ---- consumers: thread = 4 consecutive RHS columns (k4 .. k4 + 3)
         // x RR unit rows (lower) / columns (upper); warp w owns rows 4w ..
-        // 4w + 3 (with 64 columns, the warp's two half-warps take two rows
-        // each), so a warp skips a block without rows in its group whole
-        constexpr int KG = SW / 4;        // RHS groups of 4: 32 or 16
-        constexpr int RR = KG / 8;        // rows per thread: 4 or 2
+        // 4w + 3 (with 64 / 32 columns, the warp's 2 / 4 lane groups take
+        // 2 / 1 rows each), so a warp skips a block without rows in its group
+        constexpr int KG = SW / 4;        // RHS groups of 4: 32, 16 or 8
+        constexpr int RR = KG / 8;        // rows per thread: 4, 2 or 1
         const int kg = lane % KG;
         const int k4 = 4 * kg;
         const int r0 = 4 * warp + (lane / KG) * RR;
@@ -412,13 +427,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                     auto step = [&](int j) {
                         const float4 xv = *reinterpret_cast<const float4*>(&st.x[j * nrhs + k4]);
                         float lr[RR];
-                        if constexpr (RR == 4) {
-                            const float4 l4 = *reinterpret_cast<const float4*>(&st.l[j][r0]);
-                            lr[0] = l4.x; lr[1] = l4.y; lr[2] = l4.z; lr[3] = l4.w;
-                        } else {
-                            const float2 l2 = *reinterpret_cast<const float2*>(&st.l[j][r0]);
-                            lr[0] = l2.x; lr[1] = l2.y;
-                        }
+                        load_rows<RR>(&st.l[j][r0], lr);
 #pragma unroll
                         for (int r = 0; r < RR; ++r) {
                             acc[r].x = fmaf(lr[r], xv.x, acc[r].x);
@@ -493,9 +502,11 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
 #pragma unroll 4
             for (int j = 0; j < 32; ++j) {
                 const float4 tj = *reinterpret_cast<const float4*>(&sm.t[j][k4 < SW ? k4 : 0]);
+                float ev4[RR];
+                load_rows<RR>(&sm.e[j][r0], ev4);
 #pragma unroll
                 for (int r = 0; r < RR; ++r) {
-                    const float ev = sm.e[j][r0 + r];
+                    const float ev = ev4[r];
                     xv[r].x = fmaf(ev, tj.x, xv[r].x);
                     xv[r].y = fmaf(ev, tj.y, xv[r].y);
                     xv[r].z = fmaf(ev, tj.z, xv[r].z);
@@ -519,9 +530,11 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                                                   : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
                         for (int u = 0; u < 8; ++u) {
+                            float mv4[RR];
+                            load_rows<RR>(&sm.m[j0 + u][r0], mv4);
 #pragma unroll
                             for (int r = 0; r < RR; ++r) {
-                                const float mv = sm.m[j0 + u][r0 + r];
+                                const float mv = mv4[r];
                                 xv[r].x = fmaf(-mv, xc[u].x, xv[r].x);
                                 xv[r].y = fmaf(-mv, xc[u].y, xv[r].y);
                                 xv[r].z = fmaf(-mv, xc[u].z, xv[r].z);
@@ -582,6 +595,8 @@ template <class io>
 cudaError_t launch_snb_io(const SnbArgs& a, bool lower, cudaStream_t stream) {
     if (a.tensor_cores)
         return lower ? launch_snb<io, true, 128, true>(a, stream) : launch_snb<io, false, 128, true>(a, stream);
+    if (snb_width(a.nrhs) == 32)
+        return lower ? launch_snb<io, true, 32, false>(a, stream) : launch_snb<io, false, 32, false>(a, stream);
     if (snb_width(a.nrhs) == 64)
         return lower ? launch_snb<io, true, 64, false>(a, stream) : launch_snb<io, false, 64, false>(a, stream);
     return lower ? launch_snb<io, true, 128, false>(a, stream) : launch_snb<io, false, 128, false>(a, stream);

@@ -39,12 +39,12 @@ struct SnbArgs {
     int tensor_cores = 0;               // 1: block products on the tensor cores (3 x TF32 split)
 };
 
-// The bulk sweeps take RHS counts above 32 that are multiples of 4 (rows of
-// the work array are copied in 16-byte units); one work item holds every
+// The bulk sweeps take RHS counts that are multiples of 4 (rows of the work
+// array are copied in 16-byte units) up to 128; one work item holds every
 // RHS column of its unit.
-inline bool snb_supported(int nrhs) { return nrhs > 32 && nrhs <= 128 && nrhs % 4 == 0; }
-// Shared-memory width of a work item: 64 columns up to 64 RHS, else 128.
-inline int snb_width(int nrhs) { return nrhs <= 64 ? 64 : 128; }
+inline bool snb_supported(int nrhs) { return nrhs >= 4 && nrhs <= 128 && nrhs % 4 == 0; }
+// Shared-memory width of a work item: 32, 64 or 128 columns.
+inline int snb_width(int nrhs) { return nrhs <= 32 ? 32 : (nrhs <= 64 ? 64 : 128); }
 // Source columns per lower-sweep group: 64 with the CUDA-core consumers, 32
 // with the tensor-core ones.
 inline int snb_group_cols(bool tensor_cores) { return tensor_cores ? 32 : 64; }

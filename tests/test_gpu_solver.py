@@ -478,7 +478,7 @@ def test_refined_solve_nonfinite_rhs_never_converges(cuda, where):
 @pytest.mark.parametrize("group", ["0", "3"])
 @pytest.mark.parametrize("tensor_cores", ["0", "1"])
 def test_bulk_sweeps_match_oracle_and_narrow(cuda, name, group, tensor_cores, monkeypatch):
-    """The bulk-copy supernodal sweeps (FP32, 33..128 RHS in multiples of 4:
+    """The bulk-copy supernodal sweeps (FP32, 4..128 RHS in multiples of 4:
     one work item per unit holding every RHS column) against the oracle's
     FP32/FP64 sweeps and against the 32-column sweeps of a second solver on
     the same matrix (GBCHOL_BULK_MIN_RHS=129 keeps it on them), both
@@ -491,13 +491,14 @@ def test_bulk_sweeps_match_oracle_and_narrow(cuda, name, group, tensor_cores, mo
     monkeypatch.setenv("GBCHOL_BULK_GROUP", group)
     monkeypatch.setenv("GBCHOL_BULK_KEEP", "2")
     monkeypatch.setenv("GBCHOL_BULK_TC", tensor_cores)
+    monkeypatch.setenv("GBCHOL_BULK_MIN_RHS", "4")
     s_bulk = _make(torch, n, vals, idx, CholeskySolverF)
     sr = CholeskySolverD(n, torch.tensor(idx[0], device="cuda"), torch.tensor(idx[1], device="cuda"),
                          torch.tensor(vals, device="cuda"), MatrixType.COO, refine=True)
     monkeypatch.setenv("GBCHOL_BULK_MIN_RHS", "129")
     s_narrow = _make(torch, n, vals, idx, CholeskySolverF)
     perm, colptr, rowidx, lv = s_bulk.factor()
-    for nrhs in (36, 64, 68, 100, 128):
+    for nrhs in (4, 12, 32, 36, 64, 68, 100, 128):
         b = np.random.default_rng(nrhs).standard_normal((n, nrhs))
         bt = torch.tensor(b.astype(np.float32), device="cuda")
         x1, x2 = torch.zeros_like(bt), torch.zeros_like(bt)
@@ -536,7 +537,7 @@ def test_autotune_sweeps(cuda, nrhs):
     n, vals, idx = PROBLEMS["grid3d_16"]()
     s = _make(torch, n, vals, idx, CholeskySolverF)
     choice = s.autotune_sweeps(nrhs, reps=2)
-    assert choice["kernel"] in (("sliced", "bulk", "bulk_tc") if nrhs > 32 else ("sliced",))
+    assert choice["kernel"] in ("sliced", "bulk", "bulk_tc")
     assert choice["rows_per_ticket"] in (1, 2, 4)
     assert choice["rhs_split"] in ((False, True) if nrhs <= 8 else (False,))
     perm, colptr, rowidx, lv = s.factor()
