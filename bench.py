@@ -72,7 +72,11 @@ def parse_args():
 # signature (n, nnz(L), top-region units, contribution blocks, RHS count,
 # supernodal kernel): a plan or kernel that changed since the capture finds
 # no entry and reports null instead of a stale figure.
-MEASURED_SOLVE_TRAFFIC_F32 = {}
+MEASURED_SOLVE_TRAFFIC_F32 = {
+    # 64^3 Poisson, 128 RHS, bulk supernodal sweeps: 6 launches
+    # (profiles/sweeps_poisson64_nrhs128_dram.md)
+    (262144, 91560819, 5874, 281246, 128, "bulk"): 2315037696,
+}
 
 
 def plan_signature(info, nrhs):
