@@ -74,10 +74,12 @@ template <bool TC>
 struct SnbTc {};
 template <>
 struct SnbTc<true> {
-    __align__(1024) float a_hi[128 * 32];
-    __align__(1024) float a_lo[128 * 32];
-    __align__(1024) float b_hi[32 * 32];
-    __align__(1024) float b_lo[32 * 32];
+    // 128-byte alignment (the descriptors need 16): coarser padding would
+    // push the CTA past two per SM
+    __align__(128) float a_hi[128 * 32];
+    __align__(128) float a_lo[128 * 32];
+    __align__(128) float b_hi[32 * 32];
+    __align__(128) float b_lo[32 * 32];
     uint64_t mma_done;  // one phase per block: its MMAs have completed
     uint32_t tmem;      // accumulator: 128 lanes x 32 columns
 };
@@ -210,7 +212,7 @@ __device__ __forceinline__ void snb_mma(SnbTc<true>& tb, bool first) {
 
 template <class io, bool LOWER, int SW, bool TC>
 __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     SnbSmem<SW, LOWER, TC>& sm = *reinterpret_cast<SnbSmem<SW, LOWER, TC>*>(smem_raw);
     constexpr int kStages = SnbRing<LOWER, TC>::S;
     if (a.skip && dev::ld_volatile(a.skip)) return;
