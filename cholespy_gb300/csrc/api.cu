@@ -184,9 +184,10 @@ int setup_snb(gbchol_solver* h) {
     if (!(h->store & GBCHOL_STORE_F32) || P.units.empty() || !P.parts.empty()) return GBCHOL_OK;
     if (const char* env = std::getenv("GBCHOL_BULK_MIN_RHS")) h->snb_min_rhs = std::atoi(env);
     if (const char* env = std::getenv("GBCHOL_BULK_TC")) h->snb_tc = std::atoi(env) != 0;
+    SnbOptions so;
+    if (const char* env = std::getenv("GBCHOL_BULK_FOLD")) so.fold = std::atoi(env);
     SnbUpperPlan B;
     build_snb_upper(P, B);
-    SnbOptions so;
     if (const char* env = std::getenv("GBCHOL_BULK_KEEP")) so.keep = std::atoi(env);
     if (const char* env = std::getenv("GBCHOL_BULK_GROUP")) so.group = std::atoi(env);
     if (const char* env = std::getenv("GBCHOL_BULK_BLK_NS")) so.blk_ns = std::atoll(env);
@@ -212,6 +213,10 @@ int setup_snb(gbchol_solver* h) {
     CUDA_TRY(h->snb_order_up.upload(L.order_up.data(), L.order_up.size()));
     h->snb_nparts = (int32_t)L.parts.size();
     h->snb_group_cols = so.max_cols;
+    h->snb_fold = so.fold;
+    // the folded tiles depend only on the factor: a rebuild for other group
+    // widths (after the host copy was dropped) keeps the uploaded ones
+    if (!P.fold2.empty()) CUDA_TRY(upload_cast(h->snb_fold2, P.fold2));
     // flags of the bulk partial sums follow the units'
     if (h->uflags.count < P.units.size() + L.parts.size()) {
         CUDA_TRY(h->uflags.alloc(P.units.size() + L.parts.size()));
@@ -297,6 +302,8 @@ int setup_plan(gbchol_solver* h) {
     CUDA_TRY(h->uflags.alloc(std::max<size_t>(1, (P.units.size() + P.parts.size()) * 8)));
     CUDA_TRY(cudaMemset(h->uflags.p, 0, sizeof(int32_t) * h->uflags.count));
     if (int rc = setup_snb(h)) return rc;
+    P.fold2.clear();
+    P.fold2.shrink_to_fit();
     // row flags: top rows are always "ready" for the row kernels (they are
     // solved by the supernodal kernel in an earlier launch)
     h->flags_init.assign((size_t)n, 0);
@@ -456,6 +463,8 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
         b.pbuf = reinterpret_cast<float*>(sn.sys0.pbuf);
         b.n_units = (int)P.units.size();
         b.dinv = h->dinv32.p;
+        b.fold2 = h->snb_fold2.p;
+        b.fold = h->snb_fold;
         b.perm = h->perm.p;
         b.tmp = static_cast<float*>(work);
         b.uflags = h->uflags.p;

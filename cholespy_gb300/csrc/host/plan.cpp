@@ -194,8 +194,14 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
     //           on the sweep's dependency chain folded into the diagonal
     //           solve, x = D^{-1} t' - M x_chain, so that after the chain
     //           wait a unit does one 32x32 product and no reduction.
+    // The bulk sweeps fold one more block of the unit's own supernode (FP64
+    // products like the above):
+    //   M2_lo = D^{-1} L[unit, chunk two before] and
+    //   M2_up = D^{-T} L[chunk two after, unit]^T.
     constexpr size_t kMat = (size_t)kChunk * kChunk;
     P.dinv.assign((size_t)nunits * 3 * kMat, 0.0);
+    P.fold2.assign((size_t)nunits * 2 * kMat, 0.0);
+#pragma omp parallel for schedule(dynamic, 16)
     for (int32_t u = 0; u < nunits; ++u) {
         const SnUnit& U = P.units[u];
         const double* D = P.panels.data() + U.panel_col_off + U.pos0;  // D(i,j) = D[i + j*ld]
@@ -226,6 +232,26 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
                     double v = 0.0;
                     for (int32_t m = i; m < U.w; ++m) v += X[m + i * kChunk] * Ln[j + (size_t)m * U.ld];
                     Mup[i + j * kChunk] = v;
+                }
+        }
+        double* F2 = P.fold2.data() + (size_t)u * 2 * kMat;
+        if (snb_fold2_lo(U)) {  // chunk two before: 32 columns, 64 to 33 panel columns before the unit's
+            const double* Lp = P.panels.data() + U.panel_col_off - (int64_t)2 * kChunk * U.ld + U.pos0;
+            for (int32_t j = 0; j < kChunk; ++j)
+                for (int32_t i = 0; i < U.w; ++i) {
+                    double v = 0.0;
+                    for (int32_t m = 0; m <= i; ++m) v += X[i + m * kChunk] * Lp[m + (size_t)j * U.ld];
+                    F2[i + j * kChunk] = v;
+                }
+        }
+        if (snb_fold2_up(U)) {  // chunk two after (the unit is a full 32-column chunk)
+            const int32_t p2 = U.pos0 + U.w + kChunk, wn2 = std::min(kChunk, U.sn_w - p2);
+            const double* Ln = P.panels.data() + U.panel_col_off + p2;
+            for (int32_t j = 0; j < wn2; ++j)
+                for (int32_t i = 0; i < U.w; ++i) {
+                    double v = 0.0;
+                    for (int32_t m = i; m < U.w; ++m) v += X[m + i * kChunk] * Ln[j + (size_t)m * U.ld];
+                    F2[kMat + i + j * kChunk] = v;
                 }
         }
     }
@@ -442,7 +468,7 @@ void build_snb_upper(const SolvePlan& P, SnbUpperPlan& B) {
                 p0 = U.sn_w + (nrb - 1 - b) * kChunk;
                 nr = std::min(kChunk, U.ld - p0);
                 dep = P.unit_of_row[srows[p0]];
-            } else {        // later chunks of the supernode, last first
+            } else {        // later chunks of the supernode, last first (the one after next is last)
                 const int32_t c = nlater - 1 - (b - nrb);
                 p0 = wj + c * kChunk;
                 nr = std::min(kChunk, U.sn_w - p0);
@@ -485,7 +511,10 @@ void build_snb_lower(const SolvePlan& P, const SnbUpperPlan& B, const SnbOptions
     for (int32_t u = 0; u < nunits; ++u) {  // sources precede their destinations
         const SnUnit& U = P.units[u];
         const int32_t chain = U.pos0 > 0 ? 1 : 0;
-        const int32_t end = U.contrib_end - chain;
+        // the chunk before the chain one (its block is the list's second to
+        // last): with fold >= 2 a group of its own, the unit's last
+        const int32_t f2 = (o.fold >= 2 && snb_fold2_lo(U)) ? 1 : 0;
+        const int32_t end = U.contrib_end - chain - f2;
         const int32_t g0 = (int32_t)L.groups.size();
         const int32_t own_c0 = U.c0 - U.pos0;  // first column of the unit's supernode
         for (int32_t e = U.contrib_begin; e < end;) {
@@ -510,11 +539,16 @@ void build_snb_lower(const SolvePlan& P, const SnbUpperPlan& B, const SnbOptions
             std::stable_sort(L.groups.begin() + g0, L.groups.end(), [&](const SnbGroup& x, const SnbGroup& y) {
                 return fin_u[x.src_unit] < fin_u[y.src_unit];
             });
+        if (f2) {
+            const SnContrib& C = P.contribs[end];
+            L.groups.push_back(SnbGroup{end, C.w, C.src_unit, C.xcol, C.rowmask});
+        }
         const int32_t ng_u = (int32_t)L.groups.size() - g0;
         int32_t first = g0;
         const int32_t pb = (int32_t)L.parts.size();
-        if (o.group > 0 && ng_u > o.keep + o.group) {
-            const int32_t split = g0 + ng_u - o.keep;  // the unit keeps groups [split, end)
+        const int32_t keep = std::max(o.keep, f2);  // the folded group stays with the unit
+        if (o.group > 0 && ng_u > keep + o.group) {
+            const int32_t split = g0 + ng_u - keep;  // the unit keeps groups [split, end)
             const int32_t np = (split - g0 + o.group - 1) / o.group;
             for (int32_t q = 0; q < np; ++q) {  // equal shares of the split-off groups
                 SnPartial pp{};

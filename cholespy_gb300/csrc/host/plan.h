@@ -11,6 +11,12 @@ namespace gbchol {
 
 constexpr int kChunk = 32;  // columns per supernodal work unit (one warp lane per row)
 
+#ifdef __CUDACC__
+#define GBCHOL_HD __host__ __device__
+#else
+#define GBCHOL_HD
+#endif
+
 // One dense block L[rows, cols of a source chunk] applied to a unit in the
 // lower sweep: t[row - c0] -= L_block * x_src.
 struct SnContrib {
@@ -65,6 +71,7 @@ struct SolvePlan {
     std::vector<SnContrib> contribs;
     std::vector<SnPartial> parts;         // lower-sweep partial sums (by unit)
     std::vector<double> dinv;             // per unit: Dinv, M_lo, M_up (32x32 column-major each, plan.cpp)
+    std::vector<double> fold2;            // per unit: M2_lo, M2_up (32x32 column-major each, plan.cpp)
     std::vector<int32_t> unit_order_lo;   // lower-sweep items in ticket order (sorted by key):
                                           // unit u (>= 0) or partial sum p (~p)
     std::vector<int32_t> unit_order_up;   // units in upper-sweep ticket order
@@ -107,6 +114,13 @@ struct PlanOptions {
 // rows first, then its later chunks but the next, last first): where each
 // block lies in the panels, which work-array rows it multiplies and which
 // unit it waits for.
+// Second folded block of the bulk sweeps: the unit's block from the chunk
+// two before it (lower sweep) or two after it (upper sweep) in its own
+// supernode, the last block of the unit's list, applied with the tile
+// E L_block after the diagonal solve's product (x = E t' - M2 x_2 - M x_chain).
+GBCHOL_HD inline bool snb_fold2_lo(const SnUnit& U) { return U.pos0 >= 2 * kChunk; }
+GBCHOL_HD inline bool snb_fold2_up(const SnUnit& U) { return U.pos0 + U.w + kChunk < U.sn_w; }
+
 struct SnbUpperPlan {
     std::vector<int32_t> begin;  // per unit: first block (n_units + 1 entries)
     std::vector<int64_t> src;    // panel offset of (block row 0, unit column 0)
@@ -150,6 +164,10 @@ struct SnbOptions {
     // 5.73 / 5.75 ms per solve for 2.5 / 4 / 6 / 9 / 15 us): a long list is
     // best started as soon as its first source is done, ahead of the estimate.
     int64_t blk_ns = 9000;
+    // 2: the block of the chunk before the chain one is a group of its own,
+    // the unit's last (the sweeps may then fold it: snb_fold2_lo); 1: it is
+    // ordered like the others.
+    int32_t fold = 2;
 };
 
 struct SnbLowerPlan {

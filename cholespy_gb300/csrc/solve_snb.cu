@@ -26,9 +26,15 @@
 //   reduction across warps and no CTA-wide barrier per block) and release
 //   it on the stage's second mbarrier.
 // * After the last block: t' = t - sum, x = E t' (E = D^-1 lower, D^-T
-//   upper), then, once the chain unit's flag is set, x -= M x_chain; the x
-//   rows go to the work array (and, upper sweep, through perm to the output)
-//   and one release store publishes the unit.
+//   upper), then x -= M2 x_2 for the chunk two before (lower) / after
+//   (upper) in the unit's supernode (its block is the list's last; the
+//   producer streams the tile M2 = E L_block instead of L_block, so it needs
+//   no product by E), then, once the chain unit's flag is set, x -= M
+//   x_chain with the chain rows brought into shared memory in one round
+//   trip. The x rows go to the work array (and, upper sweep, through perm to
+//   the output) and one release store publishes the unit. So E t' waits
+//   only on chunks three or more back, and after the chain wait a unit does
+//   one load and one 32 x 32 product.
 // Reference: the same sweeps as kernels/kernels.cu:64-202 (solve_lower /
 // solve_upper), with the per-row flag waits of the reference replaced by one
 // flag per unit.
@@ -149,6 +155,13 @@ __device__ __forceinline__ SnbItem snb_item(const SnbArgs& a, int v, const SnUni
     return it;
 }
 
+// Whether the item's last block is the folded second block (tile M2 from
+// a.fold2, applied after the diagonal solve's product).
+template <bool LOWER>
+__device__ __forceinline__ bool snb_folds2(const SnbArgs& a, const SnbItem& it, const SnUnit& U) {
+    return !it.part && a.fold >= 2 && (LOWER ? snb_fold2_lo(U) : snb_fold2_up(U));
+}
+
 // The consumers' conversion of one landed stage into the tensor-core
 // operands: A(k, j) = x[j][k] (RHS column k, block row j), B(n, j) =
 // tile[j][n], each value v as hi = tf32(v), lo = tf32(v - hi); zero past the
@@ -261,6 +274,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             const SnUnit U = a.units[v >= 0 ? v : a.parts[~v].unit];
             const SnbItem it = snb_item<LOWER>(a, v, U);
             const unsigned umask = U.w == 32 ? 0xffffffffu : (1u << U.w) - 1u;
+            const bool f2 = snb_folds2<LOWER>(a, it, U);  // the last block's tile is M2
             // blocks in windows of 32: lane j reads the descriptor of the
             // window's j-th block and checks its source's flag (one round
             // trip for the window); the descriptors are broadcast by shuffles
@@ -338,7 +352,9 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                     // the source rows were published under the flag: order the
                     // bulk (async-proxy) reads after its acquire
                     bulk::fence_proxy_async_global();
-                    const float* ltile = (LOWER ? a.lo_tiles : a.up_tiles) + (size_t)tile * kTile;
+                    const float* ltile = (f2 && w0 + q == it.nblk - 1)
+                                             ? a.fold2 + ((size_t)it.uidx * 2 + (LOWER ? 0 : 1)) * kTile
+                                             : (LOWER ? a.lo_tiles : a.up_tiles) + (size_t)tile * kTile;
                     // the tile's first `rows` rows: the rest is zero and unread
                     if (lane == 0) bulk::copy_g2s(&sm.st[s].l[0][0], ltile, (uint32_t)rows * 32 * 4, &sm.full[s]);
                     if (start)
@@ -368,7 +384,8 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
         const int k4 = 4 * kg;
         const int r0 = 4 * warp + (lane / KG) * RR;
         const bool kin = k4 < nrhs;       // nrhs is a multiple of 4: all four columns or none
-        uint32_t gs = 0;
+        uint32_t gs = 0;   // ring stages consumed so far
+        uint32_t tcg = 0;  // blocks multiplied on the tensor cores so far (phases of mma_done)
         for (uint32_t n = 0;; ++n) {
             const int slot = (int)(n & 1);
             bulk::mbar_wait(&sm.item_full[slot], (n >> 1) & 1, a.status);
@@ -390,6 +407,8 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             }
             // E and M to shared memory (read after the consumers' barrier
             // below; the previous item's readers passed its last barrier)
+            const bool f2 = snb_folds2<LOWER>(a, it, U);
+            const int nreg = it.nblk - (f2 ? 1 : 0);  // blocks before the folded one
             if (!it.part) {
                 const float* dv = a.dinv + (size_t)uidx * 3 * kTile;
                 const float* mc = dv + (LOWER ? 1 : 2) * kTile;
@@ -403,13 +422,13 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             float4 acc[RR];
 #pragma unroll
             for (int r = 0; r < RR; ++r) acc[r] = make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int b = 0; b < it.nblk; ++b) {
+            for (int b = 0; b < nreg; ++b) {
                 const uint32_t g = gs + (uint32_t)b;
                 const int s = (int)(g % kStages);
                 bulk::mbar_wait(&sm.full[s], (g / kStages) & 1, a.status);
                 if constexpr (TC) {
                     // the previous block's MMAs have read the operand buffers
-                    if (g > 0) bulk::mbar_wait(&sm.tc.mma_done, (g - 1) & 1, a.status);
+                    if (tcg > 0) bulk::mbar_wait(&sm.tc.mma_done, (tcg - 1) & 1, a.status);
                     snb_split<SW>(sm.st[s], sm.tc, sm.ext[s], nrhs, tid);
                     tc::fence_proxy_async_smem();
                     __syncwarp();
@@ -419,6 +438,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                         tc::fence_after_sync();
                         snb_mma(sm.tc, b == 0);
                     }
+                    ++tcg;
                     continue;
                 }
                 const int ext = sm.ext[s];
@@ -448,12 +468,12 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                 __syncwarp();
                 if (lane == 0) bulk::mbar_arrive(&sm.empty[s]);
             }
-            gs += (uint32_t)it.nblk;
+            gs += (uint32_t)nreg;
             if constexpr (TC) {
                 // the accumulator (lane = RHS column, 16 columns = unit rows
                 // per warp) goes through shared memory into this mapping
-                if (it.nblk > 0) {
-                    bulk::mbar_wait(&sm.tc.mma_done, (gs - 1) & 1, a.status);
+                if (nreg > 0) {
+                    bulk::mbar_wait(&sm.tc.mma_done, (tcg - 1) & 1, a.status);
                     tc::fence_after_sync();
                     float t16[16];
                     const int kk = 32 * (warp & 3) + lane, rr0 = 16 * (warp >> 2);
@@ -515,36 +535,73 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                     xv[r].w = fmaf(ev, tj.w, xv[r].w);
                 }
             }
-            if (it.chain) {
-                const int cu = LOWER ? uidx - 1 : uidx + 1;                  // chain unit
-                const int crow = LOWER ? U.c0 - 32 : U.c0 + w;               // its first row
-                const int cw = LOWER ? 32 : min(32, U.sn_w - (U.pos0 + w));  // its width
+            // x -= M x_c for the chain chunk c (unit cu, work-array rows crow ..
+            // crow + cw - 1): once its flag is set, its rows replace t' in
+            // shared memory (every consumer has finished reading t')
+            auto fold = [&](int cu, int crow, int cw, const float (&mt)[32][32]) {
+                bulk::named_sync(1, kCW * 32);
                 if (lane == 0) dev::wait_geq(a.uflags + cu, epoch, a.status);
                 __syncwarp();
+                const int q4 = nrhs >> 2;  // 16-byte pieces per row
+                constexpr int kSteps = SW / 32;  // 32 rows x SW columns over the consumer threads
+                float4 xc[kSteps];
+#pragma unroll
+                for (int st = 0; st < kSteps; ++st) {
+                    const int f = tid + st * kCW * 32, j = f / q4;
+                    xc[st] = (f < 32 * q4 && j < cw)
+                                 ? __ldcg(reinterpret_cast<const float4*>(a.tmp + (size_t)(crow + j) * nrhs) + (f - j * q4))
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int st = 0; st < kSteps; ++st) {
+                    const int f = tid + st * kCW * 32, j = f / q4;
+                    if (f < 32 * q4) *reinterpret_cast<float4*>(&sm.t[j][4 * (f - j * q4)]) = xc[st];
+                }
+                bulk::named_sync(1, kCW * 32);
                 if (kin) {
+#pragma unroll 4
+                    for (int j = 0; j < 32; ++j) {
+                        const float4 xj = *reinterpret_cast<const float4*>(&sm.t[j][k4 < SW ? k4 : 0]);
+                        float mv4[RR];
+                        load_rows<RR>(&mt[j][r0], mv4);
 #pragma unroll
-                    for (int j0 = 0; j0 < 32; j0 += 8) {
-                        float4 xc[8];
-#pragma unroll
-                        for (int u = 0; u < 8; ++u)
-                            xc[u] = (j0 + u < cw) ? __ldcg(reinterpret_cast<const float4*>(
-                                                        a.tmp + (size_t)(crow + j0 + u) * nrhs + k4))
-                                                  : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-                        for (int u = 0; u < 8; ++u) {
-                            float mv4[RR];
-                            load_rows<RR>(&sm.m[j0 + u][r0], mv4);
-#pragma unroll
-                            for (int r = 0; r < RR; ++r) {
-                                const float mv = mv4[r];
-                                xv[r].x = fmaf(-mv, xc[u].x, xv[r].x);
-                                xv[r].y = fmaf(-mv, xc[u].y, xv[r].y);
-                                xv[r].z = fmaf(-mv, xc[u].z, xv[r].z);
-                                xv[r].w = fmaf(-mv, xc[u].w, xv[r].w);
-                            }
+                        for (int r = 0; r < RR; ++r) {
+                            const float mv = mv4[r];
+                            xv[r].x = fmaf(-mv, xj.x, xv[r].x);
+                            xv[r].y = fmaf(-mv, xj.y, xv[r].y);
+                            xv[r].z = fmaf(-mv, xj.z, xv[r].z);
+                            xv[r].w = fmaf(-mv, xj.w, xv[r].w);
                         }
                     }
                 }
+            };
+            if (f2) {  // the folded block: x -= M2 x_2 from its stage
+                const uint32_t g = gs++;
+                const int s = (int)(g % kStages);
+                bulk::mbar_wait(&sm.full[s], (g / kStages) & 1, a.status);
+                const int ext = sm.ext[s];
+                const auto& st = sm.st[s];
+                if (((sm.mask[s] >> (4 * warp)) & 0xFu) != 0 && kin) {
+                    for (int j = 0; j < ext; ++j) {
+                        const float4 xj = *reinterpret_cast<const float4*>(&st.x[j * nrhs + k4]);
+                        float mv4[RR];
+                        load_rows<RR>(&st.l[j][r0], mv4);
+#pragma unroll
+                        for (int r = 0; r < RR; ++r) {
+                            const float mv = mv4[r];
+                            xv[r].x = fmaf(-mv, xj.x, xv[r].x);
+                            xv[r].y = fmaf(-mv, xj.y, xv[r].y);
+                            xv[r].z = fmaf(-mv, xj.z, xv[r].z);
+                            xv[r].w = fmaf(-mv, xj.w, xv[r].w);
+                        }
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) bulk::mbar_arrive(&sm.empty[s]);
+            }
+            if (it.chain) {  // the chain unit: lower, the previous chunk; upper, the next one
+                if (LOWER) fold(uidx - 1, U.c0 - 32, 32, sm.m);
+                else fold(uidx + 1, U.c0 + w, min(32, U.sn_w - (U.pos0 + w)), sm.m);
             }
             if (kin) {
 #pragma unroll
@@ -561,7 +618,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             // every MMA has completed before the accumulator is freed (the
             // consumers waited for each item's last one; this matters only
             // after an abandoned wait)
-            if (tid == 0 && gs > 0) bulk::mbar_wait(&sm.tc.mma_done, (gs - 1) & 1, a.status, false);
+            if (tid == 0 && tcg > 0) bulk::mbar_wait(&sm.tc.mma_done, (tcg - 1) & 1, a.status, false);
         }
     }
     __syncthreads();

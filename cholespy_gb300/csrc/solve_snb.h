@@ -26,6 +26,8 @@ struct SnbArgs {
     float* pbuf = nullptr;              // lower: partial-sum slots, 32 x nrhs each
     int n_units = 0;                    // partial p's flag follows the units': n_units + p
     const float* dinv = nullptr;        // per unit: D^-1, M_lo, M_up (32 x 32, column-major each)
+    const float* fold2 = nullptr;       // per unit: M2_lo, M2_up (32 x 32, column-major each)
+    int fold = 1;                       // 2: the chunk two before / after is folded too (the plans' fold)
     const int32_t* perm = nullptr;
     float* tmp = nullptr;               // n x nrhs work array (permuted space), 16-byte aligned
     void* out = nullptr;                // upper sweep: the solution, through perm (TOut)

@@ -145,6 +145,8 @@ struct gbchol_solver {
     DevBuf<int32_t> snb_unit_info, snb_order_lo, snb_order_up;
     DevBuf<SnPartial> snb_parts;
     DevBuf<SnbGroup> snb_groups;
+    DevBuf<float> snb_fold2;       // per unit: M2_lo, M2_up (the second folded block of the bulk sweeps)
+    int32_t snb_fold = 1;
     int32_t snb_nparts = 0;
     bool snb_ready = false;
     // RHS counts from here on use the bulk sweeps (when supported). Measured,

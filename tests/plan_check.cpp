@@ -362,14 +362,34 @@ int check_snb(const SolvePlan& P, const SnbOptions& o) {
         const int32_t first = L.unit_info[(size_t)u * 4], gend = L.unit_info[(size_t)u * 4 + 1],
                       pb = L.unit_info[(size_t)u * 4 + 2], pe = L.unit_info[(size_t)u * 4 + 3];
         const int32_t chain = U.pos0 > 0 ? 1 : 0;
-        // the groups cover [contrib_begin, contrib_end - chain) exactly once
-        // (in any order: a unit applies them by estimated source finish)
+        // folded second block: the full block of the chunk two before (the
+        // contribution list's second to last), the unit's last group; its
+        // folded tile is D^{-1} L_block
+        const int32_t f2 = (o.fold >= 2 && snb_fold2_lo(U)) ? 1 : 0;
+        const int32_t gl = U.contrib_end - chain;  // end of the grouped blocks
+        if (f2) {
+            const SnContrib& C = P.contribs[U.contrib_end - 2];
+            bad += C.src_unit != u - 2 || C.xcol != U.c0 - 2 * kChunk || C.w != kChunk || C.nr != U.w;
+            const SnbGroup& G = L.groups[gend - 1];
+            bad += gend <= first || G.first != U.contrib_end - 2 || G.cols != kChunk || G.src_unit != u - 2;
+            const double* M2 = P.fold2.data() + (size_t)u * 2 * kChunk * kChunk;
+            const double* D = P.panels.data() + U.panel_col_off + U.pos0;
+            const double* Lb = P.panels.data() + U.panel_col_off - (int64_t)2 * kChunk * U.ld + U.pos0;
+            for (int32_t i = 0; i < U.w; ++i)
+                for (int32_t j = 0; j < kChunk; ++j) {
+                    double v = 0.0;
+                    for (int32_t m = 0; m <= i; ++m) v += D[i + (size_t)m * U.ld] * M2[m + j * kChunk];
+                    bad += std::fabs(v - Lb[i + (size_t)j * U.ld]) > 1e-9 * (1.0 + std::fabs(Lb[i + (size_t)j * U.ld]));
+                }
+        }
+        // the groups cover [contrib_begin, gl) exactly once (in any order: a
+        // unit applies them by estimated source finish)
         std::vector<char> seen((size_t)(U.contrib_end - U.contrib_begin), 0);
         for (int32_t g = gat; g < gend; ++g) {
             const SnbGroup& G = L.groups[g];
             int32_t cols = 0, f = G.first;
-            bad += G.first < U.contrib_begin || G.first >= U.contrib_end - chain;
-            while (cols < G.cols && f >= U.contrib_begin && f < U.contrib_end - chain) {
+            bad += G.first < U.contrib_begin || G.first >= gl;
+            while (cols < G.cols && f >= U.contrib_begin && f < gl) {
                 const SnContrib& C = P.contribs[f];
                 bad += C.rowmask != G.rowmask || C.xcol != G.xcol + cols || seen[f - U.contrib_begin]++ != 0;
                 if (cols + C.w < G.cols) bad += C.w != kChunk;
@@ -379,7 +399,7 @@ int check_snb(const SolvePlan& P, const SnbOptions& o) {
             bad += cols != G.cols || G.cols > std::max(o.max_cols, kChunk) || P.contribs[f - 1].src_unit != G.src_unit;
             bad += tu[G.src_unit] < 0 || tu[G.src_unit] >= tu[u];
         }
-        for (int32_t e = U.contrib_begin; e < U.contrib_end - chain; ++e) bad += seen[e - U.contrib_begin] != 1;
+        for (int32_t e = U.contrib_begin; e < gl; ++e) bad += seen[e - U.contrib_begin] != 1;
         if (chain) bad += tu[u - 1] >= tu[u];
         int32_t at = gat;
         for (int32_t q = pb; q < pe; ++q) {
@@ -394,9 +414,28 @@ int check_snb(const SolvePlan& P, const SnbOptions& o) {
         gat = gend;
         const int32_t wj = U.pos0 + U.w, nrb = (U.ld - U.sn_w + kChunk - 1) / kChunk;
         const int32_t nlater = (U.sn_w - wj + kChunk - 1) / kChunk, uchain = wj < U.sn_w ? 1 : 0;
+        const int32_t uf2 = snb_fold2_up(U) ? 1 : 0;
         bad += B.begin[u + 1] - B.begin[u] != nrb + nlater - uchain;
+        if (uf2) {
+            // the block of the chunk two after is the unit's last (the sweeps may fold it)
+            bad += B.begin[u + 1] <= B.begin[u] || B.dep[B.begin[u + 1] - 1] != u + 2;
+            // the folded tile is D^{-T} L[chunk two after, unit]^T: D^T M2 = L_block^T
+            const int32_t p2 = wj + kChunk, wn2 = std::min(kChunk, U.sn_w - p2);
+            const double* M2 = P.fold2.data() + ((size_t)u * 2 + 1) * kChunk * kChunk;
+            const double* D = P.panels.data() + U.panel_col_off + U.pos0;
+            const double* Ln = P.panels.data() + U.panel_col_off + p2;
+            for (int32_t i = 0; i < U.w; ++i)
+                for (int32_t j = 0; j < wn2; ++j) {
+                    // (D^T M2)(i, j): D^T(i, m) = D(m, i), the lower triangle read transposed
+                    double w2 = 0.0;
+                    for (int32_t m = i; m < U.w; ++m) w2 += D[m + (size_t)i * U.ld] * M2[m + j * kChunk];
+                    bad += std::fabs(w2 - Ln[j + (size_t)i * U.ld]) > 1e-9 * (1.0 + std::fabs(Ln[j + (size_t)i * U.ld]));
+                }
+        }
         for (int32_t t = B.begin[u]; t < B.begin[u + 1]; ++t) {
             bad += tup[B.dep[t]] >= tup[u];
+            // later chunks of the supernode: not the chain one
+            if (t - B.begin[u] >= nrb) bad += B.dep[t] < u + 1 + uchain;
             const int32_t nr = B.nrw[t] & 0xffff, w = B.nrw[t] >> 16;
             bad += nr < 1 || nr > kChunk || w != U.w;
             for (int32_t i = 0; i < kChunk; ++i) bad += (B.rows[(size_t)t * kChunk + i] >= 0) != (i < nr);
@@ -444,10 +483,11 @@ int main() {
         po.part_group = cs.group;
         build_plan(F, lo, up, po, P);
         if (cs.group == 0) {  // the bulk schedule is built on plans without 32-column partial sums
-            for (const SnbOptions& so : {SnbOptions{}, SnbOptions{2, 3, 32, false, 1000, 3000, 500}, SnbOptions{0, 1, 128, true, 10, 10, 10}}) {
+            for (const SnbOptions& so : {SnbOptions{}, SnbOptions{2, 3, 32, false, 1000, 3000, 500},
+                                         SnbOptions{0, 1, 128, true, 10, 10, 10}, SnbOptions{16, 0, 64, true, 1000, 5000, 9000, 1}}) {
                 const int bad = check_snb(P, so);
-                std::printf("%dD k=%d minw=%d bulk keep=%d group=%d: checks failed %d %s\n", cs.dim, cs.k, cs.minw,
-                            so.keep, so.group, bad, bad ? "FAIL" : "ok");
+                std::printf("%dD k=%d minw=%d bulk keep=%d group=%d fold=%d: checks failed %d %s\n", cs.dim, cs.k,
+                            cs.minw, so.keep, so.group, so.fold, bad, bad ? "FAIL" : "ok");
                 failed += bad != 0;
             }
         }

@@ -477,13 +477,16 @@ def test_refined_solve_nonfinite_rhs_never_converges(cuda, where):
 @pytest.mark.parametrize("name", ["grid3d_16", "ico4"])
 @pytest.mark.parametrize("group", ["0", "3"])
 @pytest.mark.parametrize("tensor_cores", ["0", "1"])
-def test_bulk_sweeps_match_oracle_and_narrow(cuda, name, group, tensor_cores, monkeypatch):
+@pytest.mark.parametrize("fold", ["1", "2"])
+def test_bulk_sweeps_match_oracle_and_narrow(cuda, name, group, tensor_cores, fold, monkeypatch):
     """The bulk-copy supernodal sweeps (FP32, 4..128 RHS in multiples of 4:
     one work item per unit holding every RHS column) against the oracle's
     FP32/FP64 sweeps and against the 32-column sweeps of a second solver on
     the same matrix (GBCHOL_BULK_MIN_RHS=129 keeps it on them), both
     shared-memory widths, with and without lower-sweep partial sums
-    (GBCHOL_BULK_GROUP), plain FP32 and the refined solve's mixed-precision
+    (GBCHOL_BULK_GROUP), one or two own-supernode blocks folded into the
+    diagonal solve (GBCHOL_BULK_FOLD; both matrices have supernodes of more
+    than three chunks), plain FP32 and the refined solve's mixed-precision
     sweeps."""
     from cholespy_gb300 import CholeskySolverD, CholeskySolverF, MatrixType
     torch = cuda
@@ -492,6 +495,7 @@ def test_bulk_sweeps_match_oracle_and_narrow(cuda, name, group, tensor_cores, mo
     monkeypatch.setenv("GBCHOL_BULK_KEEP", "2")
     monkeypatch.setenv("GBCHOL_BULK_TC", tensor_cores)
     monkeypatch.setenv("GBCHOL_BULK_MIN_RHS", "4")
+    monkeypatch.setenv("GBCHOL_BULK_FOLD", fold)
     s_bulk = _make(torch, n, vals, idx, CholeskySolverF)
     sr = CholeskySolverD(n, torch.tensor(idx[0], device="cuda"), torch.tensor(idx[1], device="cuda"),
                          torch.tensor(vals, device="cuda"), MatrixType.COO, refine=True)
