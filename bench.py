@@ -79,6 +79,19 @@ MEASURED_SOLVE_TRAFFIC_F32 = {
 }
 
 
+# DRAM bytes (read + write) of one batched solve (its 5 launches) and of one
+# autograd backward (solve + gradient kernel), from ncu captures of the same
+# workloads (profiles/batch256_grid2d_dram.md, profiles/autograd_icosphere7_dram.md).
+# Keys: (systems, total rows, total nnz(L), top-region width, row schedule)
+# and (n, nnz(L), RHS count); a changed workload or plan finds no entry.
+MEASURED_BATCH_TRAFFIC_F32 = {
+    (256, 5127876, 119810654, 16, "default"): 13217859584,
+}
+MEASURED_AUTOGRAD_BWD_TRAFFIC_F32 = {
+    (163842, 8557435, 3): 156580608,
+}
+
+
 def plan_signature(info, nrhs):
     kernel = "bulk" if (12 <= nrhs <= 128 and nrhs % 4 == 0) else "sliced"
     return (int(info.n), int(info.nnz_l), int(info.top_units), int(info.top_blocks), int(nrhs), kernel)
@@ -588,6 +601,8 @@ def run_batch(args, world, rank, local):
                  {"workload": "batch256_grid2d_n1e3-1e5_lam1-50_rhs1-128_seed3",
                   "systems": len(solvers), "total_rhs": total_rhs,
                   "top_width": 8 if args.no_autotune else 16,
+                  "row_schedule": batch.schedule or "library default: 8 MB groups, wavefront skew 4, "
+                                                    "lane mode fitted to each system's RHS count",
                   "total_rows": sum(i.n for i in infos), "total_nnz_l": sum(i.nnz_l for i in infos),
                   "ctor_s": t_ctor, "l2": "inputs larger than L2"},
                  sequential={"value": value_seq, "unit": "RHS-solves/s",
@@ -596,7 +611,11 @@ def run_batch(args, world, rank, local):
                              "max_rel_diff_vs_batched": maxdiff},
                  roofline={"kernel": "batched sweeps (5 launches per batch)", "bound": "hbm",
                            "achieved": achieved, "peak": peak, "peak_kind": kind, "unit": "GB/s",
-                           "frac": achieved / peak, "traffic": None, "algorithmic_bytes": bytes_b},
+                           "frac": achieved / peak,
+                           "traffic": MEASURED_BATCH_TRAFFIC_F32.get(
+                               (len(solvers), sum(i.n for i in infos), sum(i.nnz_l for i in infos),
+                                8 if args.no_autotune else 16, "default" if batch.schedule is None else "custom")),
+                           "algorithmic_bytes": bytes_b},
                  e2e={"value": world * total_rhs * args.steps / t_e2e, "unit": "RHS-solves/s",
                       "h2d_bytes_per_step": int(sum(b.numel() * 4 for b in bs_h)),
                       "d2h_bytes_per_step": int(sum(b.numel() * 4 for b in bs_h))},
@@ -655,7 +674,9 @@ def run_autograd(args, world, rank, local):
                  rhs_solves_per_s=world * 2 * 3 * args.steps / t,
                  roofline={"kernel": "backward: solve + sparse gradient", "bound": "hbm",
                            "achieved": achieved, "peak": peak, "peak_kind": kind, "unit": "GB/s",
-                           "frac": achieved / peak, "traffic": None, "algorithmic_bytes": bytes_bwd,
+                           "frac": achieved / peak,
+                           "traffic": MEASURED_AUTOGRAD_BWD_TRAFFIC_F32.get((n, info.nnz_l, 3)),
+                           "algorithmic_bytes": bytes_bwd,
                            "ms_backward": 1e3 * t_bwd},
                  gpu_launches=(2 * info.launches_per_solve + 1) * args.steps)
     if rank == 0:

@@ -38,6 +38,15 @@ class Info(C.Structure):
     ]
 
 
+class BatchOptions(C.Structure):
+    """gbchol_batch_options: the row sweeps' group budget, wavefront skew and lane-mode variant."""
+    _fields_ = [
+        ("group_bytes", C.c_int64),
+        ("skew", C.c_int32),
+        ("row_variant", C.c_int32),
+    ]
+
+
 class RefineStats(C.Structure):
     _fields_ = [
         ("iterations", C.c_int32),
@@ -74,6 +83,7 @@ def _declare(lib):
         "gbchol_factor_free": (C.c_int, [P]),
         "gbchol_factor_solve": (C.c_int, [P, I32, I32, P, P, I32]),
         "gbchol_batch_create": (C.c_int, [I32, P, P, I32, C.POINTER(P)]),
+        "gbchol_batch_create_ex": (C.c_int, [I32, P, P, I32, C.POINTER(BatchOptions), C.POINTER(P)]),
         "gbchol_batch_set_io": (C.c_int, [P, P, P]),
         "gbchol_batch_solve": (C.c_int, [P, P]),
         "gbchol_batch_info": (C.c_int, [P, C.POINTER(I32), C.POINTER(I64), C.POINTER(I64)]),

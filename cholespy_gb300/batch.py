@@ -7,6 +7,9 @@ persistent launch per sweep phase (gbchol_batch_* in include/gbchol.h).
     g.replay()
     width, batch = BatchSolver.tune([s0, s1, ...], nrhs=[r0, r1, ...])
 
+The row sweeps' schedule (group budget, wavefront skew, lane-mode variant;
+gbchol_batch_options) takes the library's defaults unless given.
+
 No counterpart in the reference (each of its solvers is solved separately).
 """
 from __future__ import annotations
@@ -18,7 +21,7 @@ from .solver import CholeskySolverD, CholeskySolverF
 
 
 class BatchSolver:
-    def __init__(self, solvers, nrhs):
+    def __init__(self, solvers, nrhs, group_mb=None, skew=None, row_variant=None):
         if not solvers:
             raise ValueError("A batch needs at least one solver.")
         kinds = {type(s) for s in solvers}
@@ -38,7 +41,15 @@ class BatchSolver:
         arr = (C.c_void_p * len(solvers))(*[s.handle.value for s in solvers])
         rr = (C.c_int32 * len(solvers))(*self._nrhs)
         h = C.c_void_p()
-        _ffi.check(_ffi.lib().gbchol_batch_create(len(solvers), arr, rr, self._precision, C.byref(h)))
+        if group_mb is None and skew is None and row_variant is None:
+            _ffi.check(_ffi.lib().gbchol_batch_create(len(solvers), arr, rr, self._precision, C.byref(h)))
+            self.schedule = None
+        else:
+            o = _ffi.BatchOptions(int((8 if group_mb is None else group_mb) * (1 << 20)),
+                                  4 if skew is None else int(skew), 2 if row_variant is None else int(row_variant))
+            _ffi.check(_ffi.lib().gbchol_batch_create_ex(len(solvers), arr, rr, self._precision, C.byref(o),
+                                                         C.byref(h)))
+            self.schedule = {"group_mb": o.group_bytes / (1 << 20), "skew": o.skew, "row_variant": o.row_variant}
         self._h = h
         self._bound = None
 
@@ -98,17 +109,19 @@ class BatchSolver:
         return {"launches": la.value, "nnz_l": z.value, "rows": r.value}
 
     @classmethod
-    def tune(cls, solvers, nrhs, candidates=(8, 16, 32), reps=3):
+    def tune(cls, solvers, nrhs, candidates=(8, 16, 32), reps=3, skews=(0, 4), group_mb=8):
         """Autotuner of the batch: for each candidate top-region width,
-        rebuild every solver's plan with it (`replan`), build the batch and
-        time `reps` batched solves (CUDA events, after one warm-up solve) on
-        zero right-hand sides of the batch's shapes; keep the fastest width
-        for all solvers. Returns (width, BatchSolver built on that width).
-        Batches built earlier from these solvers must be built again. No
-        counterpart in the reference."""
+        rebuild every solver's plan with it (`replan`); for each wavefront
+        skew of the row sweeps' schedule (groups of `group_mb` MB), build the
+        batch and time `reps` batched solves (CUDA events, after one warm-up
+        solve) on zero right-hand sides of the batch's shapes; keep the
+        fastest pair for all solvers. Returns (width, BatchSolver built on
+        that width and skew; its `schedule` names the skew). Batches built
+        earlier from these solvers must be built again. No counterpart in
+        the reference."""
         import torch
-        if not candidates or reps < 1:
-            raise ValueError("At least one candidate width and one repetition are needed.")
+        if not candidates or reps < 1 or not skews:
+            raise ValueError("At least one candidate width, one skew and one repetition are needed.")
         solvers = list(solvers)
         if len(nrhs) != len(solvers):
             raise ValueError("One RHS count per solver.")
@@ -123,23 +136,24 @@ class BatchSolver:
             for w in candidates:
                 for s in solvers:
                     s.replan(int(w))
-                batch = cls(solvers, nrhs)
-                batch.solve(bs, xs)
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record()
-                for _ in range(reps):
-                    batch.solve()
-                e1.record()
-                e1.synchronize()
-                batch.check()
-                t = e0.elapsed_time(e1)
-                if best_t is None or t < best_t:
-                    best, best_t = int(w), t
-                del batch
+                for k in skews:
+                    batch = cls(solvers, nrhs, group_mb=group_mb, skew=int(k))
+                    batch.solve(bs, xs)
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    for _ in range(reps):
+                        batch.solve()
+                    e1.record()
+                    e1.synchronize()
+                    batch.check()
+                    t = e0.elapsed_time(e1)
+                    if best_t is None or t < best_t:
+                        best, best_t = (int(w), int(k)), t
+                    del batch
             for s in solvers:
-                s.replan(best)
-        return best, cls(solvers, nrhs)
+                s.replan(best[0])
+        return best[0], cls(solvers, nrhs, group_mb=group_mb, skew=best[1])
 
     def capture(self, bs, xs):
         """CUDA graph of one batched solve on the given arrays (replay() to run)."""

@@ -5,15 +5,17 @@
 // Every task of every system goes into one merged schedule per phase, sorted
 // by its dependency level within its own system (ties: system, then the
 // system's own order), so all systems advance together and the ticket order
-// stays topological for each of them. Optionally (GBCHOL_BATCH_GROUP_MB)
-// the row sweeps go group by group: consecutive systems whose work arrays
-// together fit the budget form a group whose rows are ticketed level by
-// level before the next group's, so the x values each leaf row gathers stay
-// in L2. Measured on the 256-system benchmark batch (GB300, FP32): 21.6 ms
-// per replay with one group, 25.9 / 37.4 / 52.7 ms with 64 / 32 / 16 MB
-// groups: the replay is bound by the row sweeps' dependency chains, not by
-// the 31 GB of DRAM traffic of the gathers (against ~4.5 GB algorithmic), so
-// one group is the default. Each task carries its system index;
+// stays topological for each of them. The row sweeps' schedule is a
+// wavefront over groups of systems (gbchol_batch_options): consecutive
+// systems whose work arrays fit a budget form a group, and group g's tasks
+// are keyed `skew` levels after group g - 1's, so the x values a leaf row
+// gathers were written a few levels earlier by its own group and are still
+// in L2. Measured on the 256-system benchmark batch (GB300, FP32, one solve
+// without the graph): 19.5 ms with one group; groups one after another
+// (skew 0) are slower (21.6 -> 25.9 / 37.4 / 52.7 ms with 64 / 32 / 16 MB
+// groups: each group's dependency chain then runs alone), while a wavefront
+// of 8 MB groups and skew 4 takes 16.9 ms, 16.4 ms with the lane mode fitted
+// to each system's RHS count. Each task carries its system index;
 // the kernels read that system's arrays from a descriptor table. The batch
 // owns its scratch (permuted work arrays, row and unit flags, tickets and a
 // device-resident epoch), so a bound batch solve is free of host
@@ -50,18 +52,24 @@ struct gbchol_batch_s {
     DevBuf<unsigned char> tmp;
     DevBuf<int32_t> flags, uflags, counters, epoch, status;
     bool bound = false;
+    int32_t row_variant = 1;  // RowSweepArgs::batched_variant
 };
 
 namespace {
 
-// Merges per-system task lists by (group, key, system, position).
+// Merges per-system task lists by (group, key, system, position), or with
+// skew > 0 by (key + skew * group, system, position): group g then starts
+// skew levels after group g - 1 (a wavefront over the groups).
 void merge_tasks(const std::vector<const std::vector<int32_t>*>& tasks,
                  const std::vector<const std::vector<int32_t>*>& keys, const std::vector<int32_t>& group,
-                 std::vector<int32_t>& out_task, std::vector<int32_t>& out_sys) {
-    std::vector<std::tuple<int32_t, int32_t, int32_t, int32_t>> all;
+                 int32_t skew, std::vector<int32_t>& out_task, std::vector<int32_t>& out_sys) {
+    std::vector<std::tuple<int64_t, int64_t, int32_t, int32_t>> all;
     for (size_t s = 0; s < tasks.size(); ++s)
-        for (size_t i = 0; i < tasks[s]->size(); ++i)
-            all.emplace_back(group[s], keys[s] ? (*keys[s])[i] : 0, (int32_t)s, (int32_t)i);
+        for (size_t i = 0; i < tasks[s]->size(); ++i) {
+            const int64_t key = keys[s] ? (*keys[s])[i] : 0;
+            if (skew > 0) all.emplace_back(0, key + (int64_t)skew * group[s], (int32_t)s, (int32_t)i);
+            else all.emplace_back(group[s], key, (int32_t)s, (int32_t)i);
+        }
     std::sort(all.begin(), all.end());
     out_task.resize(all.size());
     out_sys.resize(all.size());
@@ -95,7 +103,22 @@ extern "C" {
 
 int gbchol_batch_create(int32_t count, const gbchol_handle* solvers, const int32_t* nrhs,
                         int32_t precision, gbchol_batch* out) {
+    gbchol_batch_options o;
+    o.group_bytes = (int64_t)8 << 20;
+    o.skew = 4;
+    o.row_variant = 2;
+    if (const char* env = std::getenv("GBCHOL_BATCH_GROUP_MB")) o.group_bytes = (int64_t)std::atol(env) << 20;
+    if (const char* env = std::getenv("GBCHOL_BATCH_SKEW")) o.skew = std::atoi(env);
+    if (const char* env = std::getenv("GBCHOL_BATCH_ROW_VARIANT")) o.row_variant = std::atoi(env);
+    return gbchol_batch_create_ex(count, solvers, nrhs, precision, &o, out);
+}
+
+int gbchol_batch_create_ex(int32_t count, const gbchol_handle* solvers, const int32_t* nrhs,
+                           int32_t precision, const gbchol_batch_options* options, gbchol_batch* out) {
     if (!out) return fail(GBCHOL_EINVAL, "out must not be NULL.");
+    if (!options) return fail(GBCHOL_EINVAL, "options must not be NULL.");
+    if (options->skew < 0 || (options->row_variant != 1 && options->row_variant != 2))
+        return fail(GBCHOL_EINVAL, "Batch options: skew must be >= 0 and row_variant 1 or 2.");
     *out = nullptr;
     if (count < 1 || !solvers || !nrhs) return fail(GBCHOL_EINVAL, "A batch needs at least one solver.");
     if (precision != 0 && precision != 1) return fail(GBCHOL_EINVAL, "precision must be 0 or 1.");
@@ -152,32 +175,29 @@ int gbchol_batch_create(int32_t count, const gbchol_handle* solvers, const int32
         const int32_t one = 1;
         CUDA_TRY(b->epoch.upload(&one, 1));
     }
-    // merged schedules; GBCHOL_BATCH_GROUP_MB > 0 sets a group budget for the
-    // row sweeps (default: one group)
+    // merged schedules of the row sweeps: groups of systems in a wavefront
     std::vector<size_t> xbytes;
     for (int32_t s = 0; s < count; ++s) xbytes.push_back((size_t)solvers[s]->n * nrhs[s] * es);
-    size_t budget = SIZE_MAX;
-    if (const char* env = std::getenv("GBCHOL_BATCH_GROUP_MB")) {
-        const long mb = std::atol(env);
-        budget = mb > 0 ? (size_t)mb << 20 : SIZE_MAX;
-    }
+    const size_t budget = options->group_bytes > 0 ? (size_t)options->group_bytes : SIZE_MAX;
+    const int32_t skew = options->skew;
+    b->row_variant = options->row_variant;
     const std::vector<int32_t> grp = l2_groups(xbytes, budget), one(count, 0);
     std::vector<const std::vector<int32_t>*> tl, kl;
     std::vector<int32_t> t, sy;
     for (auto* h : b->solvers) { tl.push_back(&h->plan.lo_tasks); kl.push_back(&h->plan.lo_task_key); }
-    merge_tasks(tl, kl, grp, t, sy);
+    merge_tasks(tl, kl, grp, skew, t, sy);
     b->n_lo = (int32_t)t.size();
     CUDA_TRY(b->lo_tasks.upload(t.data(), t.size()));
     CUDA_TRY(b->lo_sys.upload(sy.data(), sy.size()));
     tl.clear(); kl.clear();
     for (auto* h : b->solvers) { tl.push_back(&h->plan.upt_tasks); kl.push_back(nullptr); }
-    merge_tasks(tl, kl, one, t, sy);
+    merge_tasks(tl, kl, one, 0, t, sy);
     b->n_pt = (int32_t)t.size();
     CUDA_TRY(b->pt_tasks.upload(t.data(), t.size()));
     CUDA_TRY(b->pt_sys.upload(sy.data(), sy.size()));
     tl.clear(); kl.clear();
     for (auto* h : b->solvers) { tl.push_back(&h->plan.up_tasks); kl.push_back(&h->plan.up_task_key); }
-    merge_tasks(tl, kl, grp, t, sy);
+    merge_tasks(tl, kl, grp, skew, t, sy);
     b->n_up = (int32_t)t.size();
     CUDA_TRY(b->up_tasks.upload(t.data(), t.size()));
     CUDA_TRY(b->up_sys.upload(sy.data(), sy.size()));
@@ -292,7 +312,7 @@ int gbchol_batch_solve(gbchol_batch b, void* stream) {
     ra.epoch = b->epoch.p;
     ra.chunk = row_chunk();
     ra.max_nrhs = maxr;
-    ra.batched_variant = 1;
+    ra.batched_variant = b->row_variant;
     RowSweepArgs lo = ra;
     lo.sys = b->lo_d.p;
     lo.tasks = b->lo_tasks.p;

@@ -60,7 +60,8 @@ struct RowSweepArgs {
     int chunk = 1;                // consecutive tasks taken per ticket
     int max_nrhs = 0;             // largest nrhs over the systems (kernel variant choice)
     int rhs_split = 0;            // 1: lanes over the RHS columns even for <= 8 RHS (autotuned)
-    int batched_variant = 0;      // 1: one variant for every nrhs (per-system dispatch)
+    int batched_variant = 0;      // 1: per-system dispatch, two lane modes (<= 8 RHS, more);
+                                  // 2: per-system dispatch to the mode fitted to its RHS count
 };
 
 enum class SweepIO {

@@ -348,6 +348,28 @@ typedef struct gbchol_batch_s* gbchol_batch;
 int gbchol_batch_create(int32_t count, const gbchol_handle* solvers, const int32_t* nrhs,
                         int32_t precision, gbchol_batch* out);
 
+/*
+ * Schedule of a batch's row sweeps. Consecutive systems whose work arrays
+ * (n_s x nrhs[s] values) fit group_bytes form a group, and group g's tasks
+ * are ticketed `skew` dependency levels after group g - 1's (a wavefront: the
+ * x values a leaf row gathers were written recently and are still in L2;
+ * skew 0 runs the groups one after another). row_variant 1 uses two lane
+ * modes (lanes over the nonzeros up to 8 RHS, over the RHS columns above);
+ * 2 fits the mode to each system's RHS count. gbchol_batch_create uses
+ * group_bytes = 8 MiB, skew = 4, row_variant = 2 (the 256-system benchmark
+ * batch on GB300: 19.5 ms per batch with one group and two modes, 16.4 ms
+ * with these), unless GBCHOL_BATCH_GROUP_MB, GBCHOL_BATCH_SKEW or
+ * GBCHOL_BATCH_ROW_VARIANT say otherwise.
+ */
+typedef struct {
+    int64_t group_bytes;  /* <= 0: one group */
+    int32_t skew;         /* >= 0 */
+    int32_t row_variant;  /* 1 or 2 */
+} gbchol_batch_options;
+
+int gbchol_batch_create_ex(int32_t count, const gbchol_handle* solvers, const int32_t* nrhs,
+                           int32_t precision, const gbchol_batch_options* options, gbchol_batch* out);
+
 /* Bind the device arrays of every system: bs[s], xs[s] are (n_s, nrhs[s]). */
 int gbchol_batch_set_io(gbchol_batch b, const void* const* bs, void* const* xs);
 

@@ -25,8 +25,17 @@ def _systems(torch, cls, seed, count):
     return out
 
 
+# row-sweep schedules: the library default (8 MB groups, skew 4, fitted lane
+# modes), a wavefront over groups of about one system, groups one after
+# another with the two-mode variant, and one group
+SCHEDULES = {"default": {}, "wavefront": {"group_mb": 0.25, "skew": 2, "row_variant": 2},
+             "sequential": {"group_mb": 0.1, "skew": 0, "row_variant": 1},
+             "one_group": {"group_mb": 0, "skew": 0, "row_variant": 2}}
+
+
 @pytest.mark.parametrize("variant", ["float", "double"])
-def test_batch_matches_single_and_oracle(cuda, variant):
+@pytest.mark.parametrize("schedule", list(SCHEDULES))
+def test_batch_matches_single_and_oracle(cuda, variant, schedule):
     from cholespy_gb300 import BatchSolver, CholeskySolverD, CholeskySolverF
     torch = cuda
     cls = CholeskySolverF if variant == "float" else CholeskySolverD
@@ -35,7 +44,7 @@ def test_batch_matches_single_and_oracle(cuda, variant):
     systems = _systems(torch, cls, 3, 12)
     bs = [torch.randn(n, r, device="cuda", dtype=dt) for _, n, r in systems]
     xs = [torch.zeros_like(b) for b in bs]
-    batch = BatchSolver([s for s, _, _ in systems], [r for _, _, r in systems])
+    batch = BatchSolver([s for s, _, _ in systems], [r for _, _, r in systems], **SCHEDULES[schedule])
     batch.solve(bs, xs)
     batch.check()
     for (s, n, r), b, x in zip(systems, bs, xs):
@@ -100,14 +109,17 @@ def test_single_solve_graph_replay(cuda):
 
 def test_batch_tune(cuda):
     """BatchSolver.tune: the batch autotuner picks one of the candidate
-    top-region widths, replans every solver with it and returns a batch that
-    solves like the individual (replanned) solvers."""
+    top-region widths and wavefront skews, replans every solver with the
+    width and returns a batch that solves like the individual (replanned)
+    solvers."""
     from cholespy_gb300 import BatchSolver, CholeskySolverF
     torch = cuda
     systems = _systems(torch, CholeskySolverF, 11, 6)
     solvers = [s for s, _, _ in systems]
-    width, batch = BatchSolver.tune(solvers, [r for _, _, r in systems], candidates=(4, 16), reps=2)
+    width, batch = BatchSolver.tune(solvers, [r for _, _, r in systems], candidates=(4, 16), reps=2,
+                                    skews=(0, 3), group_mb=0.05)
     assert width in (4, 16)
+    assert batch.schedule["skew"] in (0, 3)
     bs = [torch.randn(n, r, device="cuda") for _, n, r in systems]
     xs = [torch.zeros_like(b) for b in bs]
     batch.solve(bs, xs)
@@ -117,3 +129,15 @@ def test_batch_tune(cuda):
         s.solve(b, x1)
         err = ((x - x1).abs().max() / x1.abs().max()).item()
         assert err <= 1e-5, err
+
+
+def test_batch_options_rejected(cuda):
+    """Invalid schedules are refused with ValueError (the C ABI's EINVAL)."""
+    from cholespy_gb300 import BatchSolver, CholeskySolverF
+    torch = cuda
+    systems = _systems(torch, CholeskySolverF, 5, 2)
+    solvers, nrhs = [s for s, _, _ in systems], [r for _, _, r in systems]
+    with pytest.raises(ValueError):
+        BatchSolver(solvers, nrhs, skew=-1)
+    with pytest.raises(ValueError):
+        BatchSolver(solvers, nrhs, row_variant=3)
