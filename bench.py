@@ -57,6 +57,9 @@ def parse_args():
     p.add_argument("--cpu-sample-rhs", type=int, default=32,
                    help="RHS columns of the bounded CPU sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--capture-only", action="store_true",
+                   help="batch, autograd: build the workload, run --warmup then --steps untimed steps and "
+                        "exit (the program of the ncu captures; prints nothing)")
     p.add_argument("--no-autotune", action="store_true",
                    help="ico6/grid64: keep the default top-region width instead of autotuning it; "
                         "batch: keep it instead of the tuned width 16")
@@ -546,6 +549,11 @@ def run_batch(args, world, rank, local):
     bs = [b.to(dev) for b in bs_h]
     xs = [torch.zeros_like(b) for b in bs]
     batch = BatchSolver(solvers, nrhs)
+    if args.capture_only:
+        for _ in range(args.warmup + args.steps):
+            batch.solve(bs, xs)
+        batch.check()
+        return
     graph = batch.capture(bs, xs)
     infos = [s.info() for s in solvers]
     total_rhs = sum(nrhs)
@@ -650,6 +658,12 @@ def run_autograd(args, world, rank, local):
         bt.grad = None
         x = ds(bt)
         (wt * x).sum().backward()
+
+    if args.capture_only:
+        for _ in range(args.warmup + args.steps):
+            step()
+        torch.cuda.synchronize(dev)
+        return
 
     t = _events_time(torch, dev, stream, step, args.steps, args.warmup, world)
     info = ds.solver.info()
