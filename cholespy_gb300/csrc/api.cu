@@ -249,11 +249,21 @@ cudaError_t upload_values(DevBuf<float>& d32, DevBuf<double>& d64, const std::ve
     return e != cudaSuccess ? e : cudaDeviceSynchronize();
 }
 
+// The leaf sweeps' wavefront (PlanOptions::leaf_group_rows, leaf_skew):
+// the defaults, or GBCHOL_LEAF_GROUP_ROWS / GBCHOL_LEAF_SKEW.
+void leaf_wavefront_options(PlanOptions& o) {
+    o.leaf_group_rows = 0;
+    o.leaf_skew = 0;
+    if (const char* env = std::getenv("GBCHOL_LEAF_GROUP_ROWS")) o.leaf_group_rows = std::max(0, std::atoi(env));
+    if (const char* env = std::getenv("GBCHOL_LEAF_SKEW")) o.leaf_skew = std::max(0, std::atoi(env));
+}
+
 // Builds the solve plan from the factor and the level orders and uploads it.
 int setup_plan(gbchol_solver* h) {
     const Factor& F = h->F;
     const int32_t n = F.n;
     SolvePlan& P = h->plan;
+    leaf_wavefront_options(h->plan_opt);
     try {
         build_plan(F, h->lower.order_h, h->upper.order_h, h->plan_opt, P);
     } catch (const std::exception& ex) {

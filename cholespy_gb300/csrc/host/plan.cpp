@@ -375,6 +375,26 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
                 P.lo_tasks.push_back(~i);
                 P.lo_task_key.push_back(maxh + 1);
             }
+        // the wavefront (the batch merges systems by lo_task_key, which stays
+        // the level: any order within a level is topological)
+        if (opt.leaf_group_rows > 0 && opt.leaf_skew > 0) {
+            const size_t nt = P.lo_tasks.size();
+            std::vector<int64_t> wkey(nt);
+            for (size_t t = 0; t < nt; ++t) {
+                const int32_t v = P.lo_tasks[t], row = v >= 0 ? v : ~v;
+                wkey[t] = P.lo_task_key[t] + (int64_t)opt.leaf_skew * (row / opt.leaf_group_rows);
+            }
+            std::vector<int32_t> idx(nt);
+            for (size_t t = 0; t < nt; ++t) idx[t] = (int32_t)t;
+            std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return wkey[a] < wkey[b]; });
+            std::vector<int32_t> tasks(nt), keys(nt);
+            for (size_t t = 0; t < nt; ++t) {
+                tasks[t] = P.lo_tasks[idx[t]];
+                keys[t] = P.lo_task_key[idx[t]];
+            }
+            P.lo_tasks.swap(tasks);
+            P.lo_task_key.swap(keys);
+        }
     }
     // upper leaf sweep: order by depth below the top region (number of leaf
     // ancestors), so every leaf subtree advances one level per step whatever
@@ -401,6 +421,23 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
                 P.up_task_key[cnt[ldepth[j]]] = ldepth[j];
                 P.up_tasks[cnt[ldepth[j]]++] = j;
             }
+        if (opt.leaf_group_rows > 0 && opt.leaf_skew > 0) {  // the wavefront, from the last group down
+            const int64_t last = (n - 1) / opt.leaf_group_rows;
+            const size_t nt = P.up_tasks.size();
+            std::vector<int32_t> idx(nt);
+            for (size_t t = 0; t < nt; ++t) idx[t] = (int32_t)t;
+            auto wkey = [&](int32_t t) {
+                return P.up_task_key[t] + (int64_t)opt.leaf_skew * (last - P.up_tasks[t] / opt.leaf_group_rows);
+            };
+            std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return wkey(a) < wkey(b); });
+            std::vector<int32_t> tasks(nt), keys(nt);
+            for (size_t t = 0; t < nt; ++t) {
+                tasks[t] = P.up_tasks[idx[t]];
+                keys[t] = P.up_task_key[idx[t]];
+            }
+            P.up_tasks.swap(tasks);
+            P.up_task_key.swap(keys);
+        }
     }
     (void)upper_order;
     // upper sweep: split every leaf column of L into its top-row entries and

@@ -107,6 +107,22 @@ struct PlanOptions {
     // sums measured slower on every RHS count)
     int32_t part_keep = 16;
     int32_t part_group = 0;
+    // Ticket order of the leaf sweeps: a wavefront over groups of
+    // leaf_group_rows consecutive rows (subtrees of the nested-dissection
+    // order are row ranges), group g keyed leaf_skew levels after group g - 1
+    // (the upper sweep from the last group down), so the x values a leaf row
+    // gathers were written a few levels earlier by its own group and are
+    // still in L2. Dependencies never point to a later group (lower sweep) /
+    // an earlier one (upper sweep), so the order stays topological. 0 in
+    // either: plain level order, the default: one system's leaf sweeps are
+    // bound by their dependency chains, which the wavefront lengthens
+    // (GB300, FP32, 64^3 / 128 RHS: 4.33 ms per solve in level order, 4.37 /
+    // 4.56 / 5.11 ms with 32768 / 16384 / 8192 rows per group and skew 4;
+    // icosphere 7 / 3 RHS: 0.94 -> 1.02 / 1.15 / 1.43 ms). The batch, whose
+    // leaf sweeps are bound by their gathers, uses a wavefront over groups
+    // of systems instead (batch.cu).
+    int32_t leaf_group_rows = 0;
+    int32_t leaf_skew = 0;
 };
 
 // Upper-sweep blocks of the bulk supernodal sweeps, per unit in the order
