@@ -51,6 +51,10 @@ def parse_args():
                         "reference's published configuration, icosphere 6 with --nrhs float32 RHS")
     p.add_argument("--fp64", action="store_true", help="solve workload: FP64 instead of FP32")
     p.add_argument("--k", type=int, default=64, help="grid side (n = k^3)")
+    p.add_argument("--top-width", type=int, default=6,
+                   help="poisson64, solve: top-region width of the solve plan (64^3, 128 RHS, FP32 + "
+                        "refinement on GB300: 10.6 / 10.3 / 10.5 / 11.0 ms per refined solve for widths "
+                        "4 / 6 / 8 / 12)")
     p.add_argument("--nrhs", type=int, default=128)
     p.add_argument("--tol", type=float, default=1e-10)
     p.add_argument("--max-iter", type=int, default=5)
@@ -77,7 +81,8 @@ def parse_args():
 # no entry and reports null instead of a stale figure.
 MEASURED_SOLVE_TRAFFIC_F32 = {
     # 64^3 Poisson, 128 RHS, bulk supernodal sweeps: 6 launches
-    # (profiles/sweeps_poisson64_nrhs128_dram.md)
+    # (profiles/sweeps_poisson64_nrhs128_dram.md), top-region width 6 / 8
+    (262144, 91560819, 7905, 327532, 128, "bulk"): 2373101312,
     (262144, 91560819, 5874, 281246, 128, "bulk"): 2315037696,
 }
 
@@ -262,6 +267,7 @@ def config_dict(args, n, nnz_a, nnz_l, extra=None):
         "workload": f"poisson3d_7pt_{args.k}^3_shift1e-3_nrhs{args.nrhs}",
         "n": n, "nnz_a": int(nnz_a), "nnz_l": int(nnz_l), "n_rhs": args.nrhs,
         "tol": args.tol, "rhs": "N(0,1) seed 2", "ordering": "nested dissection (host)",
+        "top_width": args.top_width,
         "l2": "inputs larger than L2 (factor alone exceeds 129 MB)",
     }
     if extra:
@@ -350,6 +356,8 @@ def run_ours(args, world, rank, local):
                              torch.tensor(vals).to(dev), MatrixType.COO, refine=True,
                              tol=args.tol, max_iter=args.max_iter)
     t_ctor = time.perf_counter() - t0
+    if args.top_width != 8:  # the constructor's plan uses width 8
+        solver.replan(args.top_width)
     info = solver.info()
     solver.reserve(args.nrhs)
     bd = torch.tensor(b, device=dev)
@@ -773,6 +781,8 @@ def run_solve(args, world, rank, local):
     cls = CholeskySolverD if args.fp64 else CholeskySolverF
     s = cls(n, torch.tensor(idx[0]).to(dev), torch.tensor(idx[1]).to(dev), torch.tensor(vals).to(dev),
             MatrixType.COO)
+    if args.top_width != 8:  # the constructor's plan uses width 8
+        s.replan(args.top_width)
     dt = torch.float64 if args.fp64 else torch.float32
     bd = torch.tensor(b, dtype=dt, device=dev)
     xd = torch.zeros_like(bd)
