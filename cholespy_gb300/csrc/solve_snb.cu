@@ -517,12 +517,15 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                 *reinterpret_cast<float4*>(&sm.t[r0 + r][k4 < SW ? k4 : 0]) =
                     make_float4(tv[r].x - acc[r].x, tv[r].y - acc[r].y, tv[r].z - acc[r].z, tv[r].w - acc[r].w);
             bulk::named_sync(1, kCW * 32);
-            // x = E t' (my rows, my columns)
+            // x = E t' (my rows, my columns). E is triangular (lower: D^-1,
+            // upper: D^-T), so the warp's rows 4 warp .. 4 warp + 3 need only
+            // j <= 4 warp + 3 (lower) / j >= 4 warp (upper)
             float4 xv[RR];
 #pragma unroll
             for (int r = 0; r < RR; ++r) xv[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+            const int ej0 = LOWER ? 0 : 4 * warp, ej1 = LOWER ? 4 * warp + 4 : 32;
 #pragma unroll 4
-            for (int j = 0; j < 32; ++j) {
+            for (int j = ej0; j < ej1; ++j) {
                 const float4 tj = *reinterpret_cast<const float4*>(&sm.t[j][k4 < SW ? k4 : 0]);
                 float ev4[RR];
                 load_rows<RR>(&sm.e[j][r0], ev4);
