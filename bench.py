@@ -87,7 +87,7 @@ MEASURED_SOLVE_TRAFFIC_F32 = {
 }
 
 
-# DRAM bytes (read + write) of one batched solve (its 5 launches) and of one
+# DRAM bytes (read + write) of one batched solve (its launches) and of one
 # autograd backward (solve + gradient kernel), from ncu captures of the same
 # workloads (profiles/batch256_grid2d_dram.md, profiles/autograd_icosphere7_dram.md).
 # Keys: (systems, total rows, total nnz(L), top-region width, row schedule)
@@ -625,7 +625,7 @@ def run_batch(args, world, rank, local):
                              "ms_per_batch": 1e3 * t_seq / max(1, args.steps // 2),
                              "batched_over_sequential": value / value_seq,
                              "max_rel_diff_vs_batched": maxdiff},
-                 roofline={"kernel": "batched sweeps (5 launches per batch)", "bound": "hbm",
+                 roofline={"kernel": "batched sweeps (one launch per phase)", "bound": "hbm",
                            "achieved": achieved, "peak": peak, "peak_kind": kind, "unit": "GB/s",
                            "frac": achieved / peak,
                            "traffic": MEASURED_BATCH_TRAFFIC_F32.get(

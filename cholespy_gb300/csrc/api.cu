@@ -256,6 +256,8 @@ void leaf_wavefront_options(PlanOptions& o) {
     o.leaf_skew = 0;
     if (const char* env = std::getenv("GBCHOL_LEAF_GROUP_ROWS")) o.leaf_group_rows = std::max(0, std::atoi(env));
     if (const char* env = std::getenv("GBCHOL_LEAF_SKEW")) o.leaf_skew = std::max(0, std::atoi(env));
+    o.partial_last = true;
+    if (const char* env = std::getenv("GBCHOL_PARTIAL_LAST")) o.partial_last = std::atoi(env) != 0;
 }
 
 // Builds the solve plan from the factor and the level orders and uploads it.
@@ -264,6 +266,7 @@ int setup_plan(gbchol_solver* h) {
     const int32_t n = F.n;
     SolvePlan& P = h->plan;
     leaf_wavefront_options(h->plan_opt);
+    if (const char* env = std::getenv("GBCHOL_UP_MERGE")) h->up_merge = std::atoi(env) != 0;
     try {
         build_plan(F, h->lower.order_h, h->upper.order_h, h->plan_opt, P);
     } catch (const std::exception& ex) {
@@ -511,7 +514,13 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
         sn.counters = h->counters.p + 4;
         CUDA_TRY(launch_sn_sweep(sn, false, io, s));
     }
-    RowSweepArgs pt = lo;  // top-row terms of the leaf rows: no waits
+    // the leaf rows' top-row terms (final after the supernodal sweeps):
+    // summed first by each leaf row of the upper sweep, with no flag checks,
+    // so they overlap the leaf chain's waits (GB300 FP32, with / without a
+    // separate wait-free pass launch: icosphere 7 / 3 RHS 0.854 / 0.942 ms,
+    // 64^3 / 16 RHS 2.94 / 3.06 ms, / 128 RHS 4.17 / 4.20 ms; the 256-system
+    // batch 16.0 / 16.5 ms); GBCHOL_UP_MERGE=0 keeps the separate pass
+    RowSweepArgs pt = lo;
     pt.sys0.rowptr = h->upt_rowptr.p;
     pt.sys0.cols = h->upt_cols.p;
     pt.sys0.vals = f32 ? (const void*)h->upt_v32.p : (const void*)h->upt_v64.p;
@@ -520,11 +529,16 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
     pt.tasks = h->upt_tasks.p;
     pt.ntasks = (int)P.upt_tasks.size();
     pt.counters = h->counters.p + 8;
-    CUDA_TRY(launch_row_sweep(pt, false, io, s));
+    if (!h->up_merge) CUDA_TRY(launch_row_sweep(pt, false, io, s));
     RowSweepArgs up = pt;
     up.sys0.rowptr = h->up_rowptr.p;
     up.sys0.cols = h->up_cols.p;
     up.sys0.vals = f32 ? (const void*)h->up_v32.p : (const void*)h->up_v64.p;
+    if (h->up_merge) {
+        up.sys0.nw_rowptr = pt.sys0.rowptr;
+        up.sys0.nw_cols = pt.sys0.cols;
+        up.sys0.nw_vals = pt.sys0.vals;
+    }
     up.tasks = h->up_tasks.p;
     up.ntasks = (int)P.up_tasks.size();
     up.counters = h->counters.p + 6;
@@ -542,7 +556,7 @@ int run_sweeps(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in,
 // Kernel launches of one run_sweeps call.
 int sweep_launches(const gbchol_solver* h) {
     const SolvePlan& P = h->plan;
-    return (P.lo_tasks.empty() ? 0 : 1) + (P.units.empty() ? 0 : 2) + (P.upt_tasks.empty() ? 0 : 1) +
+    return (P.lo_tasks.empty() ? 0 : 1) + (P.units.empty() ? 0 : 2) + (P.upt_tasks.empty() || h->up_merge ? 0 : 1) +
            (P.up_tasks.empty() ? 0 : 1);
 }
 

@@ -1,5 +1,5 @@
 // Batched solves: many factors of uneven sizes and RHS counts swept by ONE
-// persistent launch per phase (5 launches for the whole batch, whatever the
+// persistent launch per phase (4 launches for the whole batch, whatever the
 // number of systems). No counterpart in the reference.
 //
 // Every task of every system goes into one merged schedule per phase, sorted
@@ -53,6 +53,7 @@ struct gbchol_batch_s {
     DevBuf<int32_t> flags, uflags, counters, epoch, status;
     bool bound = false;
     int32_t row_variant = 1;  // RowSweepArgs::batched_variant
+    bool up_merge = true;     // leaf rows sum their top-row terms in the upper leaf sweep (no pass launch)
 };
 
 namespace {
@@ -181,6 +182,7 @@ int gbchol_batch_create_ex(int32_t count, const gbchol_handle* solvers, const in
     const size_t budget = options->group_bytes > 0 ? (size_t)options->group_bytes : SIZE_MAX;
     const int32_t skew = options->skew;
     b->row_variant = options->row_variant;
+    if (const char* env = std::getenv("GBCHOL_UP_MERGE")) b->up_merge = std::atoi(env) != 0;
     const std::vector<int32_t> grp = l2_groups(xbytes, budget), one(count, 0);
     std::vector<const std::vector<int32_t>*> tl, kl;
     std::vector<int32_t> t, sy;
@@ -252,6 +254,11 @@ int gbchol_batch_create_ex(int32_t count, const gbchol_handle* solvers, const in
         up.rowptr = h->up_rowptr.p;
         up.cols = h->up_cols.p;
         up.vals = f32 ? (const void*)h->up_v32.p : (const void*)h->up_v64.p;
+        if (b->up_merge) {
+            up.nw_rowptr = pt.rowptr;
+            up.nw_cols = pt.cols;
+            up.nw_vals = pt.vals;
+        }
         b->lo_h.push_back(lo);
         b->pt_h.push_back(pt);
         b->up_h.push_back(up);
@@ -342,7 +349,7 @@ int gbchol_batch_solve(gbchol_batch b, void* stream) {
     pt.task_sys = b->pt_sys.p;
     pt.ntasks = b->n_pt;
     pt.counters = b->counters.p + 8;
-    CUDA_TRY(launch_row_sweep(pt, false, io, s));
+    if (!b->up_merge) CUDA_TRY(launch_row_sweep(pt, false, io, s));
     RowSweepArgs up = ra;
     up.sys = b->up_d.p;
     up.tasks = b->up_tasks.p;
@@ -355,7 +362,8 @@ int gbchol_batch_solve(gbchol_batch b, void* stream) {
 
 int gbchol_batch_info(gbchol_batch b, int32_t* launches, int64_t* nnz_l, int64_t* rows) {
     if (!b) return fail(GBCHOL_EINVAL, "Null batch.");
-    if (launches) *launches = (b->n_lo > 0) + (b->n_snlo > 0) + (b->n_snup > 0) + (b->n_pt > 0) + (b->n_up > 0);
+    if (launches)
+        *launches = (b->n_lo > 0) + (b->n_snlo > 0) + (b->n_snup > 0) + (b->n_pt > 0 && !b->up_merge) + (b->n_up > 0);
     int64_t z = 0, r = 0;
     for (auto* h : b->solvers) {
         z += h->F.nnz();

@@ -357,7 +357,9 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
     for (int32_t i = 0; i < n; ++i) P.max_row_len = std::max(P.max_row_len, P.lo_rowptr[i + 1] - P.lo_rowptr[i]);
     {
         // leaf rows by their level in L (= etree height: their dependencies
-        // are all leaf rows), then the partial tasks of the top rows
+        // are all leaf rows); the partial task of a top row keyed one past
+        // the highest leaf column it reads, so it runs as soon as its own
+        // inputs are done (with opt.partial_last, after every leaf row)
         std::vector<int32_t> parent((size_t)n, -1), height((size_t)n, 0);
         for (int32_t j = 0; j < n; ++j)
             if (F.colptr[j + 1] - F.colptr[j] > 1) parent[j] = F.rowidx[F.colptr[j] + 1];
@@ -372,9 +374,26 @@ void build_plan(const Factor& F, const std::vector<int32_t>& lower_order,
             }
         for (int32_t i = 0; i < n; ++i)
             if (P.row_top[i]) {
+                int32_t key = 0;
+                for (int32_t k = P.lo_rowptr[i]; k < P.lo_rowptr[i + 1]; ++k)
+                    key = std::max(key, height[P.lo_cols[k]] + 1);
                 P.lo_tasks.push_back(~i);
-                P.lo_task_key.push_back(maxh + 1);
+                P.lo_task_key.push_back(opt.partial_last ? maxh + 1 : key);
             }
+        if (!opt.partial_last) {  // one topological order: by key, leaf rows first within a key
+            const size_t nt = P.lo_tasks.size();
+            std::vector<int32_t> idx(nt);
+            for (size_t t = 0; t < nt; ++t) idx[t] = (int32_t)t;
+            std::stable_sort(idx.begin(), idx.end(),
+                             [&](int32_t a, int32_t b) { return P.lo_task_key[a] < P.lo_task_key[b]; });
+            std::vector<int32_t> tasks(nt), keys(nt);
+            for (size_t t = 0; t < nt; ++t) {
+                tasks[t] = P.lo_tasks[idx[t]];
+                keys[t] = P.lo_task_key[idx[t]];
+            }
+            P.lo_tasks.swap(tasks);
+            P.lo_task_key.swap(keys);
+        }
         // the wavefront (the batch merges systems by lo_task_key, which stays
         // the level: any order within a level is topological)
         if (opt.leaf_group_rows > 0 && opt.leaf_skew > 0) {

@@ -123,6 +123,11 @@ struct PlanOptions {
     // of systems instead (batch.cu).
     int32_t leaf_group_rows = 0;
     int32_t leaf_skew = 0;
+    // lower leaf sweep: the top rows' partial tasks after every leaf row
+    // (true, the default) or each one past its own highest leaf input (false:
+    // measured no faster, GB300 FP32: 64^3 / 128 RHS 4.22 vs 4.17 ms,
+    // icosphere 7 / 3 RHS 0.853 vs 0.854 ms)
+    bool partial_last = true;
 };
 
 // Upper-sweep blocks of the bulk supernodal sweeps, per unit in the order

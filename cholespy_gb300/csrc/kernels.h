@@ -45,6 +45,12 @@ struct RowSys {
     int* flags = nullptr;         // row completion flags (epoch-valued)
     int nrhs = 0;
     int pad = 0;
+    // upper sweep, optional: entries of each row whose values are final
+    // before the launch (the top rows' terms of a leaf row), summed first
+    // with no flag checks
+    const int* nw_rowptr = nullptr;
+    const int* nw_cols = nullptr;
+    const void* nw_vals = nullptr;  // T
 };
 
 struct RowSweepArgs {

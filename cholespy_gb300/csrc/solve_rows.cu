@@ -81,6 +81,17 @@ __device__ __forceinline__ void row_nnz(const RowSys& d, int task, int s, int e,
     T acc[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) acc[j] = T(0);
+    if (!LOWER && !partial && d.nw_rowptr) {  // terms final before the launch: no flag checks
+        const T* nv = static_cast<const T*>(d.nw_vals);
+        const int ne = d.nw_rowptr[row + 1];
+        for (int k = d.nw_rowptr[row] + lane; k < ne; k += 32) {
+            const T v = nv[k];
+            const T* xc = tmp + (size_t)d.nw_cols[k] * nrhs;
+#pragma unroll
+            for (int j = 0; j < R; ++j)
+                if (j < nrhs) acc[j] = fma(v, __ldcg(xc + j), acc[j]);
+        }
+    }
     for (int base = lo; base < hi; base += 64) {
         // two entries per lane: flags checked together, then one fence
         int c[2];
@@ -153,16 +164,8 @@ __device__ __forceinline__ void row_rhs(const RowSys& d, int task, int s, int e,
     T acc[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) acc[q] = T(0);
-    for (int base = lo; base < hi; base += 32) {
-        const int k = base + lane;
-        const int mycol = k < hi ? d.cols[k] : 0;
-        const T myv = k < hi ? vals[k] : T(0);
-        // every lane waits for its own entry, then the warp consumes the 32
-        // entries without further waits (independent loads in flight)
-        if (k < hi && dev::ld_acquire(d.flags + mycol) < epoch)
-            dev::wait_geq(d.flags + mycol, epoch, status);
-        __syncwarp();  // orders every lane's observation before the warp's x loads
-        const int cnt = min(32, hi - base);
+    // the warp consumes `cnt` entries held one per lane (column, value)
+    auto consume = [&](int mycol, T myv, int cnt) {
         const int steps = (cnt + NG - 1) / NG;
 #pragma unroll 8
         for (int st = 0; st < steps; ++st) {
@@ -178,6 +181,25 @@ __device__ __forceinline__ void row_rhs(const RowSys& d, int task, int s, int e,
                 if (j < nrhs) acc[q] = fma(v, __ldcg(xc + j), acc[q]);
             }
         }
+    };
+    if (!LOWER && !partial && d.nw_rowptr) {  // terms final before the launch: no flag checks
+        const T* nv = static_cast<const T*>(d.nw_vals);
+        const int ns = d.nw_rowptr[row], ne = d.nw_rowptr[row + 1];
+        for (int base = ns; base < ne; base += 32) {
+            const int k = base + lane;
+            consume(k < ne ? d.nw_cols[k] : 0, k < ne ? nv[k] : T(0), min(32, ne - base));
+        }
+    }
+    for (int base = lo; base < hi; base += 32) {
+        const int k = base + lane;
+        const int mycol = k < hi ? d.cols[k] : 0;
+        const T myv = k < hi ? vals[k] : T(0);
+        // every lane waits for its own entry, then the warp consumes the 32
+        // entries without further waits (independent loads in flight)
+        if (k < hi && dev::ld_acquire(d.flags + mycol) < epoch)
+            dev::wait_geq(d.flags + mycol, epoch, status);
+        __syncwarp();  // orders every lane's observation before the warp's x loads
+        consume(mycol, myv, min(32, hi - base));
     }
     if (NG > 1) {
 #pragma unroll

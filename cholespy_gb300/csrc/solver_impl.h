@@ -124,6 +124,9 @@ struct gbchol_solver {
     // (batches record it and refuse a solver whose plan changed)
     SolvePlan plan;
     PlanOptions plan_opt;
+    // upper leaf sweep: each leaf row sums its top-row terms itself (no
+    // separate wait-free pass launch)
+    bool up_merge = true;
     int32_t plan_gen = 0;
     DevBuf<int32_t> lo_rowptr, lo_cols, lo_tasks, up_rowptr, up_cols, up_tasks, sn_rows;
     DevBuf<int32_t> upt_rowptr, upt_cols, upt_tasks;

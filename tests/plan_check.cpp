@@ -448,13 +448,15 @@ int check_snb(const SolvePlan& P, const SnbOptions& o) {
 
 int main() {
     if (!check_transpose()) return 1;
-    // the last two fields: leaf-sweep wavefront (rows per group, skew; 0: level order)
-    struct Case { int dim, k, minw, keep, group, lgr, lskew; };
+    // lgr, lskew: leaf-sweep wavefront (rows per group, skew; 0: level order);
+    // early: the top rows' partial tasks keyed by their own inputs (not last)
+    struct Case { int dim, k, minw, keep, group, lgr, lskew, early = 0; };
     const Case cases[] = {
         {2, 8, 1, 16, 32, 0, 0},  {2, 20, 4, 16, 32, 0, 0}, {2, 20, 8, 2, 3, 0, 0},   {2, 40, 1, 1, 2, 0, 0},
         {3, 8, 1, 2, 3, 0, 0},    {3, 14, 4, 16, 32, 0, 0}, {3, 14, 8, 4, 5, 0, 0},   {3, 18, 8, 16, 32, 0, 0},
         {3, 18, 8, 0, 0, 0, 0},   {3, 14, 100000, 16, 32, 0, 0}, {2, 40, 1, 0, 0, 0, 0}, {3, 14, 4, 0, 0, 0, 0},
         {2, 40, 4, 0, 0, 64, 2},  {3, 14, 4, 0, 0, 100, 3}, {3, 18, 8, 16, 32, 50, 1},
+        {2, 40, 4, 0, 0, 0, 0, 1}, {3, 14, 4, 0, 0, 100, 3, 1},
     };
     int failed = 0;
     for (const Case& cs : cases) {
@@ -485,6 +487,7 @@ int main() {
         po.part_group = cs.group;
         po.leaf_group_rows = cs.lgr;
         po.leaf_skew = cs.lskew;
+        po.partial_last = !cs.early;
         build_plan(F, lo, up, po, P);
         if (cs.group == 0) {  // the bulk schedule is built on plans without 32-column partial sums
             for (const SnbOptions& so : {SnbOptions{}, SnbOptions{2, 3, 32, false, 1000, 3000, 500},

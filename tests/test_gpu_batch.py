@@ -57,7 +57,7 @@ def test_batch_matches_single_and_oracle(cuda, variant, schedule):
         xo = oracle.reference_solve(perm, colptr, rowidx, lv, b.cpu().numpy(), npdt)
         erro = np.abs(x.cpu().numpy() - xo).max() / np.abs(xo).max()
         assert erro <= tol, erro
-    assert batch.info()["launches"] <= 5
+    assert batch.info()["launches"] <= 4  # one per phase: lower rows, lower and upper supernodal, upper rows
 
 
 def test_batch_graph_replay(cuda):

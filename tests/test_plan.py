@@ -21,5 +21,5 @@ def test_plan_schedule_and_solution(tmp_path):
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     p = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
     assert p.returncode == 0, p.stdout[-4000:] + p.stderr[-2000:]
-    # 15 plans x 2 RHS counts, the transpose check, 5 plans x 4 bulk schedules
-    assert "FAIL" not in p.stdout and p.stdout.count(" ok") == 51, p.stdout
+    # 17 plans x 2 RHS counts, the transpose check, 7 plans x 4 bulk schedules
+    assert "FAIL" not in p.stdout and p.stdout.count(" ok") == 63, p.stdout
