@@ -80,10 +80,9 @@ def parse_args():
 # supernodal kernel): a plan or kernel that changed since the capture finds
 # no entry and reports null instead of a stale figure.
 MEASURED_SOLVE_TRAFFIC_F32 = {
-    # 64^3 Poisson, 128 RHS, bulk supernodal sweeps: 6 launches
-    # (profiles/sweeps_poisson64_nrhs128_dram.md), top-region width 6 / 8
-    (262144, 91560819, 7905, 327532, 128, "bulk"): 2373101312,
-    (262144, 91560819, 5874, 281246, 128, "bulk"): 2315037696,
+    # 64^3 Poisson, 128 RHS, top-region width 6, bulk supernodal sweeps: 5
+    # launches (profiles/sweeps_poisson64_nrhs128_dram.md)
+    (262144, 91560819, 7905, 327532, 128, "bulk"): 2340551168,
 }
 
 
@@ -93,10 +92,10 @@ MEASURED_SOLVE_TRAFFIC_F32 = {
 # Keys: (systems, total rows, total nnz(L), top-region width, row schedule)
 # and (n, nnz(L), RHS count); a changed workload or plan finds no entry.
 MEASURED_BATCH_TRAFFIC_F32 = {
-    (256, 5127876, 119810654, 16, "default"): 13217859584,
+    (256, 5127876, 119810654, 16, "default"): 11874094592,
 }
 MEASURED_AUTOGRAD_BWD_TRAFFIC_F32 = {
-    (163842, 8557435, 3): 156580608,
+    (163842, 8557435, 3): 153481728,
 }
 
 
