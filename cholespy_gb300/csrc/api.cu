@@ -184,6 +184,7 @@ int setup_snb(gbchol_solver* h) {
     if (!(h->store & GBCHOL_STORE_F32) || P.units.empty() || !P.parts.empty()) return GBCHOL_OK;
     if (const char* env = std::getenv("GBCHOL_BULK_MIN_RHS")) h->snb_min_rhs = std::atoi(env);
     if (const char* env = std::getenv("GBCHOL_BULK_TC")) h->snb_tc = std::atoi(env) != 0;
+    if (const char* env = std::getenv("GBCHOL_BULK_SLICES")) h->snb_slices = std::atoi(env);
     SnbOptions so;
     if (const char* env = std::getenv("GBCHOL_BULK_FOLD")) so.fold = std::atoi(env);
     SnbUpperPlan B;
@@ -217,9 +218,9 @@ int setup_snb(gbchol_solver* h) {
     // the folded tiles depend only on the factor: a rebuild for other group
     // widths (after the host copy was dropped) keeps the uploaded ones
     if (!P.fold2.empty()) CUDA_TRY(upload_cast(h->snb_fold2, P.fold2));
-    // flags of the bulk partial sums follow the units'
-    if (h->uflags.count < P.units.size() + L.parts.size()) {
-        CUDA_TRY(h->uflags.alloc(P.units.size() + L.parts.size()));
+    // flags of the bulk partial sums follow the units', per column slice (up to 4)
+    if (h->uflags.count < (P.units.size() + L.parts.size()) * 4) {
+        CUDA_TRY(h->uflags.alloc((P.units.size() + L.parts.size()) * 4));
         CUDA_TRY(cudaMemset(h->uflags.p, 0, sizeof(int32_t) * h->uflags.count));
     }
     CUDA_TRY(h->snb_lo_tiles.alloc(std::max<size_t>(1, nlo) * 32 * 32));
@@ -402,12 +403,25 @@ namespace {
 // Supernodal kernel of a solve: 0 the 32-column sweeps, 1 the bulk sweeps,
 // 2 the bulk sweeps on the tensor cores (tiles built for groups of <= 32
 // columns). An autotuned choice for this RHS count wins over the defaults.
+// Column slices of a bulk-sweep kind (3: two, 4: four), when nrhs splits into
+// that many slices of a multiple of 4 columns; else 1.
+int snb_kind_slices(int kind, int nrhs) {
+    const int s = kind == 3 ? 2 : (kind == 4 ? 4 : 1);
+    return (s > 1 && nrhs % (4 * s) == 0) ? s : 1;
+}
+
 int sn_kind(const gbchol_solver* h, int nrhs, bool f32) {
     if (!f32 || !h->snb_ready || !snb_supported(nrhs)) return 0;
     const auto& t = h->tuned[nrhs];
-    if (t.valid) return (t.sn == 2 && h->snb_group_cols > 32) ? 1 : t.sn;
+    if (t.valid) {
+        if (t.sn == 2 && h->snb_group_cols > 32) return 1;
+        if (t.sn >= 3 && snb_kind_slices(t.sn, nrhs) == 1) return 1;
+        return t.sn;
+    }
     if (nrhs < h->snb_min_rhs) return 0;
-    return (h->snb_tc && h->snb_group_cols <= 32) ? 2 : 1;
+    if (h->snb_tc && h->snb_group_cols <= 32) return 2;
+    const int kind = h->snb_slices == 4 ? 4 : (h->snb_slices == 2 ? 3 : 1);
+    return snb_kind_slices(kind, nrhs) > 1 ? kind : 1;
 }
 bool use_snb(const gbchol_solver* h, int nrhs, bool f32) { return sn_kind(h, nrhs, f32) != 0; }
 }  // namespace
@@ -481,21 +495,29 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
         b.perm = h->perm.p;
         b.tmp = static_cast<float*>(work);
         b.uflags = h->uflags.p;
-        b.nrhs = nrhs;
-        b.tensor_cores = sn_kind(h, nrhs, f32) == 2 ? 1 : 0;
+        const int kind = sn_kind(h, nrhs, f32);
+        const int nsl = snb_kind_slices(kind, nrhs);  // column slices: independent items per unit
+        b.nrhs = nrhs / nsl;
+        b.ld = nrhs;
+        b.nslices = nsl;
+        b.flag_stride = (int)P.units.size() + h->snb_nparts;
+        b.tensor_cores = kind == 2 ? 1 : 0;
         b.status = h->status.p;
         b.skip = skip;
         b.epoch = h->dev_epoch.p;
-        b.nitems = (int)P.units.size() + h->snb_nparts;
+        b.nitems = ((int)P.units.size() + h->snb_nparts) * nsl;
         b.order = h->snb_order_lo.p;
         b.counters = h->counters.p + 2;
         CUDA_TRY(launch_snb_sweep(b, true, io, s));
         b.out = nullptr;  // the top rows' output is scattered afterwards, off the chain
-        b.nitems = (int)P.units.size();
+        b.nitems = (int)P.units.size() * nsl;
         b.order = h->snb_order_up.p;
         b.counters = h->counters.p + 4;
         CUDA_TRY(launch_snb_sweep(b, false, io, s));
         b.out = out;
+        b.nrhs = nrhs;  // the scatter covers every column
+        b.ld = 0;
+        b.nslices = 1;
         CUDA_TRY(launch_snb_scatter(b, (int)P.units.size(), io, s));
     } else {
         sn.sys0.n_units = (int)P.units.size();
@@ -959,8 +981,9 @@ int gbchol_autotune_sweeps(gbchol_handle h, int32_t precision, int32_t nrhs, int
     const SweepIO io = f32 ? SweepIO::F32 : SweepIO::F64;
     gbchol_solver::SweepTune best;
     float best_ms = 0.f;
-    const int sn_max = bulk_ok ? 2 : 0;
-    for (int sn = 0; sn <= sn_max && rc == GBCHOL_OK; ++sn)
+    const int sn_max = bulk_ok ? 4 : 0;
+    for (int sn = 0; sn <= sn_max && rc == GBCHOL_OK; ++sn) {
+        if (sn >= 3 && snb_kind_slices(sn, nrhs) == 1) continue;  // no such column split
         for (int split = 0; split <= (nrhs <= 8 ? 1 : 0) && rc == GBCHOL_OK; ++split)
             for (int chunk : {1, 2, 4}) {
                 if (rc != GBCHOL_OK) break;
@@ -991,6 +1014,7 @@ int gbchol_autotune_sweeps(gbchol_handle h, int32_t precision, int32_t nrhs, int
                     best_ms = ms;
                 }
             }
+    }
     h->last_stream = nullptr;
     h->tuned[nrhs] = rc == GBCHOL_OK ? best : gbchol_solver::SweepTune{};
     if (rc == GBCHOL_OK && choice) *choice = best.sn | (best.rhs_split << 4) | (best.chunk << 8);

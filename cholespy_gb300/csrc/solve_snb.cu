@@ -100,7 +100,7 @@ struct SnbSmem {
     uint64_t full[kStages], empty[kStages];
     uint64_t item_full[2], item_empty[2];  // the two item-descriptor slots
     SnUnit item_unit[2];
-    int item_v[2], item_valid[2];
+    int item_v[2], item_valid[2], item_slice[2];
     int ext[kStages];        // rows of the stage's x block (lower: source columns, upper: block rows)
     unsigned mask[kStages];  // unit rows (lower) / columns (upper) the block has
     SnbTc<TC> tc;
@@ -250,7 +250,9 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
     }
     __syncthreads();
     if constexpr (TC) tc::fence_after_sync();
-    const int nrhs = a.nrhs;
+    const int nrhs = a.nrhs;                       // columns of one item (its slice)
+    const int ld = a.ld > 0 ? a.ld : nrhs;         // row stride of the work array
+    const int ns = a.nslices;
     if (warp == kCW) {
         // ---- producer: tickets, then the item's blocks into the stage ring
         uint32_t gs = 0;  // ring stages used so far
@@ -260,17 +262,22 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             if (lane == 0) tk = atomicAdd(a.counters, 1);
             tk = __shfl_sync(0xffffffffu, tk, 0);
             const bool valid = tk < a.nitems;
-            const int v = valid ? a.order[tk] : 0;
+            // tickets: the slices of an item are consecutive
+            const int v = valid ? a.order[tk / ns] : 0;
+            const int slice = tk % ns;
             if (lane == 0) {
                 if (n >= 2) bulk::mbar_wait(&sm.item_empty[slot], ((n >> 1) - 1) & 1, a.status);
                 sm.item_valid[slot] = valid ? 1 : 0;
                 if (valid) {
                     sm.item_v[slot] = v;
+                    sm.item_slice[slot] = slice;
                     sm.item_unit[slot] = a.units[v >= 0 ? v : a.parts[~v].unit];
                 }
                 bulk::mbar_arrive(&sm.item_full[slot]);
             }
             if (!valid) break;
+            const int* uf = a.uflags + (size_t)slice * a.flag_stride;  // the slice's flags
+            const float* xs = a.tmp + (size_t)slice * nrhs;            // the slice's first column
             const SnUnit U = a.units[v >= 0 ? v : a.parts[~v].unit];
             const SnbItem it = snb_item<LOWER>(a, v, U);
             const unsigned umask = U.w == 32 ? 0xffffffffu : (1u << U.w) - 1u;
@@ -294,7 +301,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                     } else {
                         src_j = a.up_dep[t];
                     }
-                    ready_j = dev::ld_acquire(a.uflags + src_j) >= epoch;
+                    ready_j = dev::ld_acquire(uf + src_j) >= epoch;
                 }
                 // upper: the rows of the window's first block (later blocks'
                 // rows are read one block ahead)
@@ -320,10 +327,19 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                         mask = umask;
                     }
                     // upper: the block's rows are a prefix of the lanes; runs of
-                    // consecutive work-array rows go in one bulk copy each
+                    // consecutive work-array rows go in one bulk copy each (with
+                    // column slices a row's columns are not contiguous with the
+                    // next row's: one copy per row)
                     int rows, run = 0;
                     bool start;
-                    if (LOWER) {
+                    if (ld != nrhs) {
+                        if (LOWER) {
+                            rows = rows_l;
+                        } else {
+                            rows = __popc(__ballot_sync(0xffffffffu, row >= 0));
+                        }
+                        start = false;
+                    } else if (LOWER) {
                         rows = rows_l;
                         start = lane == 0;
                         run = rows;
@@ -343,7 +359,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                             // long since: its consumers waited for them)
                             bulk::mbar_wait(&sm.full[s], par, a.status, false);
                         }
-                        if (!ready) dev::wait_geq(a.uflags + src, epoch, a.status);
+                        if (!ready) dev::wait_geq(uf + src, epoch, a.status);
                         sm.ext[s] = rows;
                         sm.mask[s] = mask;
                         bulk::mbar_arrive_expect_tx(&sm.full[s], (uint32_t)(rows * (32 + nrhs) * 4));
@@ -358,8 +374,18 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                     // the tile's first `rows` rows: the rest is zero and unread
                     if (lane == 0) bulk::copy_g2s(&sm.st[s].l[0][0], ltile, (uint32_t)rows * 32 * 4, &sm.full[s]);
                     if (start)
-                        bulk::copy_g2s(&sm.st[s].x[(LOWER ? 0 : lane) * nrhs], a.tmp + (size_t)row * nrhs,
+                        bulk::copy_g2s(&sm.st[s].x[(LOWER ? 0 : lane) * nrhs], xs + (size_t)row * ld,
                                        (uint32_t)(run * nrhs) * 4, &sm.full[s]);
+                    if (ld != nrhs) {  // one copy per row: lower, rows row .. row + rows - 1; upper, lane's row
+                        if (LOWER) {
+                            for (int i = lane; i < rows; i += 32)
+                                bulk::copy_g2s(&sm.st[s].x[i * nrhs], xs + (size_t)(row + i) * ld,
+                                               (uint32_t)nrhs * 4, &sm.full[s]);
+                        } else if (row >= 0) {
+                            bulk::copy_g2s(&sm.st[s].x[lane * nrhs], xs + (size_t)row * ld, (uint32_t)nrhs * 4,
+                                           &sm.full[s]);
+                        }
+                    }
                 }
             }
             gs += (uint32_t)it.nblk;
@@ -392,6 +418,10 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             if (!sm.item_valid[slot]) break;
             const int v = sm.item_v[slot];
             const SnUnit U = sm.item_unit[slot];
+            const int slice = sm.item_slice[slot];
+            int* uf = a.uflags + (size_t)slice * a.flag_stride;  // the slice's flags
+            float* xs = a.tmp + (size_t)slice * nrhs;            // the slice's first column
+            float* pbs = a.pbuf + (size_t)slice * (a.flag_stride - a.n_units) * 32 * nrhs;  // its partial slots
             __syncwarp();
             if (lane == 0) bulk::mbar_arrive(&sm.item_empty[slot]);  // the descriptor has been read
             const SnbItem it = snb_item<LOWER>(a, v, U);
@@ -402,7 +432,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             for (int r = 0; r < RR; ++r) {
                 const int i = r0 + r;
                 tv[r] = (!it.part && i < w && kin)
-                            ? __ldcg(reinterpret_cast<const float4*>(a.tmp + (size_t)(U.c0 + i) * nrhs + k4))
+                            ? __ldcg(reinterpret_cast<const float4*>(xs + (size_t)(U.c0 + i) * ld + k4))
                             : make_float4(0.f, 0.f, 0.f, 0.f);
             }
             // E and M to shared memory (read after the consumers' barrier
@@ -488,21 +518,21 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                 }
             }
             if (it.part) {  // the sum goes to the partial's slot, then its flag
-                float* ps = a.pbuf + (size_t)(~v) * 32 * nrhs;
+                float* ps = pbs + (size_t)(~v) * 32 * nrhs;
                 if (kin) {
 #pragma unroll
                     for (int r = 0; r < RR; ++r) *reinterpret_cast<float4*>(ps + (r0 + r) * nrhs + k4) = acc[r];
                 }
                 bulk::named_sync(1, kCW * 32);
-                if (tid == 0) dev::st_release(a.uflags + a.n_units + ~v, epoch);
+                if (tid == 0) dev::st_release(uf + a.n_units + ~v, epoch);
                 continue;
             }
             if (LOWER) {  // the unit's partial sums, in a fixed order
                 const int pb = a.unit_info[(size_t)uidx * 4 + 2], pe = a.unit_info[(size_t)uidx * 4 + 3];
                 for (int q = pb; q < pe; ++q) {
-                    if (lane == 0) dev::wait_geq(a.uflags + a.n_units + q, epoch, a.status);
+                    if (lane == 0) dev::wait_geq(uf + a.n_units + q, epoch, a.status);
                     __syncwarp();
-                    const float* ps = a.pbuf + (size_t)q * 32 * nrhs;
+                    const float* ps = pbs + (size_t)q * 32 * nrhs;
                     if (kin) {
 #pragma unroll
                         for (int r = 0; r < RR; ++r) {
@@ -543,7 +573,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             // shared memory (every consumer has finished reading t')
             auto fold = [&](int cu, int crow, int cw, const float (&mt)[32][32]) {
                 bulk::named_sync(1, kCW * 32);
-                if (lane == 0) dev::wait_geq(a.uflags + cu, epoch, a.status);
+                if (lane == 0) dev::wait_geq(uf + cu, epoch, a.status);
                 __syncwarp();
                 const int q4 = nrhs >> 2;  // 16-byte pieces per row
                 constexpr int kSteps = SW / 32;  // 32 rows x SW columns over the consumer threads
@@ -552,7 +582,7 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
                 for (int st = 0; st < kSteps; ++st) {
                     const int f = tid + st * kCW * 32, j = f / q4;
                     xc[st] = (f < 32 * q4 && j < cw)
-                                 ? __ldcg(reinterpret_cast<const float4*>(a.tmp + (size_t)(crow + j) * nrhs) + (f - j * q4))
+                                 ? __ldcg(reinterpret_cast<const float4*>(xs + (size_t)(crow + j) * ld) + (f - j * q4))
                                  : make_float4(0.f, 0.f, 0.f, 0.f);
                 }
 #pragma unroll
@@ -610,12 +640,12 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
 #pragma unroll
                 for (int r = 0; r < RR; ++r) {
                     const int i = r0 + r;
-                    if (i < w) *reinterpret_cast<float4*>(a.tmp + (size_t)(U.c0 + i) * nrhs + k4) = xv[r];
+                    if (i < w) *reinterpret_cast<float4*>(xs + (size_t)(U.c0 + i) * ld + k4) = xv[r];
                 }
             }
             // the barrier orders the consumers' writes before the release
             bulk::named_sync(1, kCW * 32);
-            if (tid == 0) dev::st_release(a.uflags + uidx, epoch);
+            if (tid == 0) dev::st_release(uf + uidx, epoch);
         }
         if constexpr (TC) {
             // every MMA has completed before the accumulator is freed (the

@@ -32,8 +32,11 @@ struct SnbArgs {
     float* tmp = nullptr;               // n x nrhs work array (permuted space), 16-byte aligned
     void* out = nullptr;                // upper sweep: the solution, through perm (TOut)
     int* uflags = nullptr;              // completion flags: units, then partial sums
-    int nrhs = 0;
-    int nitems = 0;                     // lower: n_units + partial sums; upper: n_units
+    int nrhs = 0;                       // RHS columns of one work item (a slice)
+    int ld = 0;                         // row stride of the work array (0: nrhs)
+    int nslices = 1;                    // column slices: items = (unit or partial sum, slice)
+    int flag_stride = 0;                // flags per slice (n_units + partial sums)
+    int nitems = 0;                     // tickets: (lower: n_units + partial sums; upper: n_units) x nslices
     int* epoch = nullptr;               // device sweep counter: read at start, +1 by the last CTA out
     int* status = nullptr;
     const int* skip = nullptr;
@@ -43,7 +46,10 @@ struct SnbArgs {
 
 // The bulk sweeps take RHS counts that are multiples of 4 (rows of the work
 // array are copied in 16-byte units) up to 128; one work item holds every
-// RHS column of its unit.
+// RHS column of its unit, or one of `nslices` equal column slices (each a
+// multiple of 4 wide): the slices are independent solves on the same tiles,
+// each with its own flags, so a dependency chain steps through half (a
+// quarter) of the columns per unit.
 inline bool snb_supported(int nrhs) { return nrhs >= 4 && nrhs <= 128 && nrhs % 4 == 0; }
 // Shared-memory width of a work item: 32, 64 or 128 columns.
 inline int snb_width(int nrhs) { return nrhs <= 32 ? 32 : (nrhs <= 64 ? 64 : 128); }

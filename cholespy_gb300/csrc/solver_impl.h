@@ -157,6 +157,7 @@ struct gbchol_solver {
     // 3.36, 16 3.20 / 4.28, 32 3.44 / 5.32
     int32_t snb_min_rhs = 12;
     bool snb_tc = false;       // bulk sweeps: block products on the tensor cores
+    int32_t snb_slices = 1;    // bulk sweeps: column slices per unit when not tuned (1, 2 or 4)
     bool snb_tc_groups = false;  // build the lower groups for the tensor cores (<= 32 columns)
     int32_t snb_group_cols = 0;  // source columns per lower group the tiles were built for
     // per RHS count, the sweep variant chosen by gbchol_autotune_sweeps:

@@ -408,7 +408,8 @@ class _CholeskySolver:
         the fastest for later solves of that RHS count (gbchol_autotune_sweeps):
         the top-region kernel ("sliced": 32-column RHS slices, "bulk": one work
         item per unit for every RHS column, "bulk_tc": the same on the tensor
-        cores), the row sweeps' lane mode (lanes over the RHS for <= 8 RHS) and
+        cores, "bulk_2slices" / "bulk_4slices": one work item per unit and
+        column half / quarter), the row sweeps' lane mode (lanes over the RHS for <= 8 RHS) and
         the rows per row-sweep ticket. Returns the choice as a dict. No
         counterpart in the reference."""
         self._gpu_only("autotune_sweeps")
@@ -419,7 +420,8 @@ class _CholeskySolver:
         choice = C.c_int32(0)
         _ffi.check(_ffi.lib().gbchol_autotune_sweeps(self._h, prec, int(n_rhs), int(reps), C.byref(choice)))
         v = int(choice.value)
-        return {"kernel": ("sliced", "bulk", "bulk_tc")[v & 15], "rhs_split": bool((v >> 4) & 15),
+        return {"kernel": ("sliced", "bulk", "bulk_tc", "bulk_2slices", "bulk_4slices")[v & 15],
+                "rhs_split": bool((v >> 4) & 15),
                 "rows_per_ticket": v >> 8}
 
     def info(self) -> SolverInfo:

@@ -310,8 +310,10 @@ int gbchol_autotune(gbchol_handle h, int32_t precision, int32_t nrhs, const int3
  * the given precision (`reps` timed solves each, after two untimed ones)
  * and keeps the fastest for later solves of that RHS count: the
  * top-region kernel (0: 32-column RHS slices, 1: one work item per unit for
- * every RHS column, CUDA cores, 2: the same on the tensor cores; 1 and 2
- * only for FP32 and 4..128 RHS in multiples of 4), for <= 8 RHS whether
+ * every RHS column, CUDA cores, 2: the same on the tensor cores, 3 / 4: one
+ * work item per unit and column half / quarter (the RHS tile width); 1-4 only
+ * for FP32 and 4..128 RHS in multiples of 4, 3 and 4 when the columns split
+ * into multiples of 4), for <= 8 RHS whether
  * the row sweeps put their lanes over the RHS columns instead of the
  * nonzeros (threads per column), and the rows each row-sweep ticket takes
  * (1, 2 or 4: how many consecutive level-ordered rows are merged into one

@@ -530,6 +530,45 @@ def test_bulk_sweeps_match_oracle_and_narrow(cuda, name, group, tensor_cores, fo
     assert res.max() <= 1e-10
 
 
+@pytest.mark.parametrize("slices", ["2", "4"])
+def test_bulk_column_slices_match_oracle(cuda, slices, monkeypatch):
+    """The bulk sweeps with the RHS columns cut into 2 or 4 independent
+    slices per unit (GBCHOL_BULK_SLICES; RHS counts that do not split into
+    multiples of 4 keep one slice) against the oracle's FP32 sweeps and the
+    single-slice bulk sweeps of a second solver, plain FP32 and refined."""
+    from cholespy_gb300 import CholeskySolverD, CholeskySolverF, MatrixType
+    torch = cuda
+    n, vals, idx = PROBLEMS["grid3d_16"]()
+    monkeypatch.setenv("GBCHOL_BULK_MIN_RHS", "4")
+    monkeypatch.setenv("GBCHOL_BULK_SLICES", slices)
+    s_sl = _make(torch, n, vals, idx, CholeskySolverF)
+    sr = CholeskySolverD(n, torch.tensor(idx[0], device="cuda"), torch.tensor(idx[1], device="cuda"),
+                         torch.tensor(vals, device="cuda"), MatrixType.COO, refine=True)
+    monkeypatch.setenv("GBCHOL_BULK_SLICES", "1")
+    s_one = _make(torch, n, vals, idx, CholeskySolverF)
+    perm, colptr, rowidx, lv = s_sl.factor()
+    for nrhs in (8, 16, 24, 64, 100, 128):
+        b = np.random.default_rng(nrhs).standard_normal((n, nrhs)).astype(np.float32)
+        bt = torch.tensor(b, device="cuda")
+        x1, x2 = torch.zeros_like(bt), torch.zeros_like(bt)
+        s_sl.solve(bt, x1)
+        s_one.solve(bt, x2)
+        s_sl.check()
+        s_one.check()
+        xo = oracle.reference_solve(perm, colptr, rowidx, lv, b, np.float32)
+        scale = np.abs(xo).max()
+        assert np.abs(x1.cpu().numpy() - xo).max() / scale <= 1e-5, nrhs
+        assert np.abs(x1.cpu().numpy() - x2.cpu().numpy()).max() / scale <= 1e-5, nrhs
+    b = np.random.default_rng(9).standard_normal((n, 128))
+    bt = torch.tensor(b, device="cuda")
+    xt = torch.zeros_like(bt)
+    st = sr.solve_refined(bt, xt, tol=1e-10, max_iter=5)
+    assert st.converged
+    A = sym_matrix(n, vals, idx)
+    res = np.linalg.norm(b - A @ xt.cpu().numpy(), axis=0) / np.linalg.norm(b, axis=0)
+    assert res.max() <= 1e-10
+
+
 @pytest.mark.parametrize("nrhs", [4, 64])
 def test_autotune_sweeps(cuda, nrhs):
     """gbchol_autotune_sweeps times every sweep variant for an RHS count
@@ -541,7 +580,7 @@ def test_autotune_sweeps(cuda, nrhs):
     n, vals, idx = PROBLEMS["grid3d_16"]()
     s = _make(torch, n, vals, idx, CholeskySolverF)
     choice = s.autotune_sweeps(nrhs, reps=2)
-    assert choice["kernel"] in ("sliced", "bulk", "bulk_tc")
+    assert choice["kernel"] in ("sliced", "bulk", "bulk_tc", "bulk_2slices", "bulk_4slices")
     assert choice["rows_per_ticket"] in (1, 2, 4)
     assert choice["rhs_split"] in ((False, True) if nrhs <= 8 else (False,))
     perm, colptr, rowidx, lv = s.factor()
