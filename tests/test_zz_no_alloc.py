@@ -58,3 +58,28 @@ def test_solve_noalloc_rejects_oversize(cuda):
                                          C.c_void_p(b.data_ptr()), None)
     assert st == _ffi.EINVAL
     assert "16 MiB" in _ffi.last_error()
+
+
+def test_solve_noalloc_leaves_free_memory_unchanged(cuda):
+    """A steady-state call allocates no device memory: the driver's free
+    memory is the same before and after it (the first call with these
+    shapes, which may load kernel code lazily, is made before measuring)."""
+    from cholespy_gb300 import CholeskySolverF, _ffi
+    torch = cuda
+    s, n = _solver(torch, CholeskySolverF)
+    lib = _ffi.lib()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    b = torch.randn(n, 96, device="cuda")
+    x = torch.zeros_like(b)
+
+    def call():
+        _ffi.check(lib.gbchol_solve_noalloc(s.handle, 0, 96, C.c_void_p(b.data_ptr()),
+                                            C.c_void_p(x.data_ptr()), stream))
+        torch.cuda.synchronize()
+
+    call()
+    free0 = torch.cuda.mem_get_info()[0]
+    call()
+    free1 = torch.cuda.mem_get_info()[0]
+    _ffi.check(lib.gbchol_check(s.handle))
+    assert free1 == free0, (free0, free1)
