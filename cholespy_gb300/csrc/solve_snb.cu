@@ -572,9 +572,11 @@ __global__ void __launch_bounds__(kThreads, 2) snb_sweep_kernel(SnbArgs a) {
             // crow + cw - 1): once its flag is set, its rows replace t' in
             // shared memory (every consumer has finished reading t')
             auto fold = [&](int cu, int crow, int cw, const float (&mt)[32][32]) {
+                // one poller: its acquire and the barrier order every
+                // consumer's loads after the chain unit's release (eight
+                // pollers would wait for the slowest one's round trip)
+                if (tid == 0) dev::wait_geq(uf + cu, epoch, a.status);
                 bulk::named_sync(1, kCW * 32);
-                if (lane == 0) dev::wait_geq(uf + cu, epoch, a.status);
-                __syncwarp();
                 const int q4 = nrhs >> 2;  // 16-byte pieces per row
                 constexpr int kSteps = SW / 32;  // 32 rows x SW columns over the consumer threads
                 float4 xc[kSteps];
