@@ -458,7 +458,12 @@ int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, co
     const auto& tune = h->tuned[nrhs];
     lo.chunk = tune.valid ? tune.chunk : row_chunk();
     lo.max_nrhs = nrhs;
-    lo.rhs_split = tune.valid ? tune.rhs_split : 0;
+    // 2..8 RHS: lanes over the RHS columns (16-lane groups taking alternate
+    // nonzeros) unless tuned otherwise; measured on GB300 (FP32, lanes over
+    // the nonzeros -> over the RHS): icosphere 7, 3 / 8 RHS 0.861 -> 0.769 /
+    // 1.122 -> 0.792 ms; icosphere 6, 3 RHS 0.561 -> 0.425 ms; 64^3, 4 RHS
+    // 2.708 -> 2.594 ms; 64x64 grid, 3 RHS 0.416 -> 0.255 ms (1 RHS: equal)
+    lo.rhs_split = tune.valid ? tune.rhs_split : (nrhs >= 2 && nrhs <= 8 ? 1 : 0);
     lo.epoch = h->dev_epoch.p;
     CUDA_TRY(launch_row_sweep(lo, true, io, s));
     SnSweepArgs sn;

@@ -68,6 +68,8 @@ struct RowSweepArgs {
     int rhs_split = 0;            // 1: lanes over the RHS columns even for <= 8 RHS (autotuned)
     int batched_variant = 0;      // 1: per-system dispatch, two lane modes (<= 8 RHS, more);
                                   // 2: per-system dispatch to the mode fitted to its RHS count
+                                  // (1 RHS: lanes over the nonzeros; 2..16: 16-lane groups over
+                                  // the RHS; 17..32 / 64 / 128: 32 lanes x 1 / 2 / 4 columns)
 };
 
 enum class SweepIO {

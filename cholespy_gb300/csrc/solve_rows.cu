@@ -244,9 +244,7 @@ __global__ void __launch_bounds__(256) row_sweep_kernel(RowSweepArgs a) {
         else if (MODE == 64) row_rhs<io, LOWER, 32, 2>(d, task, s, e, epoch, a.status, lane);
         else if (MODE == 128) row_rhs<io, LOWER, 32, 4>(d, task, s, e, epoch, a.status, lane);
         else if (a.batched_variant >= 2) {  // the variant fitted to the system's RHS count
-            if (d.nrhs <= 2) row_nnz<io, LOWER, 2>(d, task, s, e, epoch, a.status, lane);
-            else if (d.nrhs <= 4) row_nnz<io, LOWER, 4>(d, task, s, e, epoch, a.status, lane);
-            else if (d.nrhs <= 8) row_nnz<io, LOWER, 8>(d, task, s, e, epoch, a.status, lane);
+            if (d.nrhs <= 1) row_nnz<io, LOWER, 1>(d, task, s, e, epoch, a.status, lane);
             else if (d.nrhs <= 16) row_rhs<io, LOWER, 16, 1>(d, task, s, e, epoch, a.status, lane);
             else if (d.nrhs <= 32) row_rhs<io, LOWER, 32, 1>(d, task, s, e, epoch, a.status, lane);
             else if (d.nrhs <= 64) row_rhs<io, LOWER, 32, 2>(d, task, s, e, epoch, a.status, lane);
