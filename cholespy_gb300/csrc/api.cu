@@ -393,16 +393,6 @@ int gbchol::row_chunk() {
 }
 
 namespace {
-
-// One full solve: leaf rows (lower) -> top units (lower) -> top units
-// (upper) -> leaf rows (upper). `in` is read through perm by the lower leaf
-// kernel; `out` is written through perm by both upper kernels.
-}  // namespace
-
-namespace {
-// Supernodal kernel of a solve: 0 the 32-column sweeps, 1 the bulk sweeps,
-// 2 the bulk sweeps on the tensor cores (tiles built for groups of <= 32
-// columns). An autotuned choice for this RHS count wins over the defaults.
 // Column slices of a bulk-sweep kind (3: two, 4: four), when nrhs splits into
 // that many slices of a multiple of 4 columns; else 1.
 int snb_kind_slices(int kind, int nrhs) {
@@ -410,6 +400,10 @@ int snb_kind_slices(int kind, int nrhs) {
     return (s > 1 && nrhs % (4 * s) == 0) ? s : 1;
 }
 
+// Supernodal kernel of a solve: 0 the 32-column sweeps, 1 the bulk sweeps,
+// 2 the bulk sweeps on the tensor cores (tiles built for groups of <= 32
+// columns), 3 / 4 the bulk sweeps with 2 / 4 column slices per unit. An
+// autotuned choice for this RHS count wins over the defaults.
 int sn_kind(const gbchol_solver* h, int nrhs, bool f32) {
     if (!f32 || !h->snb_ready || !snb_supported(nrhs)) return 0;
     const auto& t = h->tuned[nrhs];
@@ -435,7 +429,10 @@ size_t gbchol::work_bytes(const gbchol_solver* h, int nrhs, bool f32) {
 }
 
 // One full solve with the work array `work` (work_bytes: the permuted-space
-// n x nrhs array of T, then the partial-sum slots).
+// n x nrhs array of T, then the partial-sum slots): leaf rows (lower) -> top
+// units (lower) -> top units (upper) -> leaf rows (upper). `in` is read
+// through perm by the lower leaf kernel; `out` is written through perm by the
+// upper kernels (the bulk sweeps' top rows by their scatter launch).
 int gbchol::run_sweeps_with(gbchol_solver* h, bool f32, SweepIO io, int nrhs, const void* in,
                             void* out, const int* skip, void* work, cudaStream_t s) {
     const SolvePlan& P = h->plan;
