@@ -99,6 +99,18 @@ MEASURED_AUTOGRAD_BWD_TRAFFIC_F32 = {
 }
 
 
+# The reference's own GPU solve kernels (kernels/kernels.cu, built from source
+# for sm_103a) on the SAME factor, timed by `oracle/ref_gpu_bench.py --cases
+# p3d64:128:f` on GB300 (CUDA events, median): recorded, not re-run here (the
+# bench does not execute the reference's code outside its reference arm).
+# Level order computed sequentially: the reference's analysis kernel can
+# publish a stale level (flag before level, no fence), which could deadlock
+# its unbounded spin-waits. Keyed by (n, nnz(L), RHS count, precision).
+RECORDED_REFERENCE_GPU = {
+    (262144, 91560819, 128, "f32"): 69.06489562988281,
+}
+
+
 def plan_signature(info, nrhs):
     kernel = "bulk" if (12 <= nrhs <= 128 and nrhs % 4 == 0) else "sliced"
     return (int(info.n), int(info.nnz_l), int(info.top_units), int(info.top_blocks), int(nrhs), kernel)
@@ -487,6 +499,15 @@ def run_ours(args, world, rank, local):
         "gpu_launches": launches * args.steps,
         "cpu_baseline": cpu,
     }
+    ref_ms = RECORDED_REFERENCE_GPU.get((n, int(info.nnz_l), args.nrhs, "f32"))
+    if ref_ms is not None:
+        line["reference_gpu"] = {
+            "value": args.nrhs / (ref_ms / 1e3), "unit": "RHS-solves/s", "ms_per_solve": ref_ms,
+            "what": "the reference's kernels.cu FP32 solve (no refinement) on the same factor",
+            "same_factor": True, "level_order": "repaired (computed sequentially)",
+            "this_run": False, "source": "recorded by oracle/ref_gpu_bench.py --cases p3d64:128:f on GB300",
+            "ours_fp32_solve_over_reference": ref_ms / (1e3 * t_32),
+            "ours_refined_over_reference": value / (args.nrhs / (ref_ms / 1e3))}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
