@@ -16,6 +16,9 @@
 //     warps (no deadlock); the last warp out resets the ticket;
 //   * one launch can sweep many systems (a batch): each task names its
 //     system, whose arrays come from a descriptor table;
+//   * the upper leaf sweep's rows first sum the terms that were final before
+//     the launch (the top rows' x, from a second CSR) with no flag checks, so
+//     those gathers overlap the waits of the leaf chain;
 //   * flags carry an epoch kept in device memory (read at kernel start,
 //     advanced by the last warp out), so no per-solve memset of the flags
 //     and the sweeps can be captured in a CUDA graph and replayed;
