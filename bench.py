@@ -81,14 +81,16 @@ def parse_args():
 # no entry and reports null instead of a stale figure.
 MEASURED_SOLVE_TRAFFIC_F32 = {
     # 64^3 Poisson, 128 RHS, top-region width 6, bulk supernodal sweeps: 5
-    # launches (profiles/sweeps_poisson64_nrhs128_dram.md)
+    # launches (`--workload solve --k 64 --nrhs 128 --steps 2 --warmup 3`,
+    # ncu -k regex:"sweep|scatter" -s 15 -c 5)
     (262144, 91560819, 7905, 327532, 128, "bulk"): 2340551168,
 }
 
 
 # DRAM bytes (read + write) of one batched solve (its launches) and of one
 # autograd backward (solve + gradient kernel), from ncu captures of the same
-# workloads (profiles/batch256_grid2d_dram.md, profiles/autograd_icosphere7_dram.md).
+# workloads (`--workload batch|autograd --capture-only`: the launches of the
+# last solve / step).
 # Keys: (systems, total rows, total nnz(L), top-region width, row schedule)
 # and (n, nnz(L), RHS count); a changed workload or plan finds no entry.
 MEASURED_BATCH_TRAFFIC_F32 = {
