@@ -19,7 +19,7 @@ uses (cholespy_gb300/workloads.py):
 
 Tolerances, stated per test: FP64 results within 1e-12 (max-norm, relative
 to max |x|) of the oracle's FP64 sweeps; FP32 results within 1e-5 relative
-residual (spec bar for CholeskySolverF) and no less accurate than the
+residual (the parity bar for CholeskySolverF) and no less accurate than the
 oracle's own FP32 sweeps (error against the FP64 oracle at most 4x the
 oracle FP32 sweeps' error, plus 1e-6 of max |x|); refined FP32 within 1e-10
 relative residual."""
