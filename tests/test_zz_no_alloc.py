@@ -83,3 +83,41 @@ def test_solve_noalloc_leaves_free_memory_unchanged(cuda):
     free1 = torch.cuda.mem_get_info()[0]
     _ffi.check(lib.gbchol_check(s.handle))
     assert free1 == free0, (free0, free1)
+
+
+def test_solve_noalloc_replays_in_a_cuda_graph(cuda):
+    """After a first call outside capture (which looks up the static work
+    array's device address), a gbchol_solve_noalloc call can be captured in
+    a CUDA graph: each replay, with b rewritten in place in between, matches
+    gbchol_solve on the same b."""
+    from cholespy_gb300 import CholeskySolverF, _ffi
+    torch = cuda
+    s, n = _solver(torch, CholeskySolverF)
+    lib = _ffi.lib()
+    nrhs = 16
+    b = torch.randn(n, nrhs, device="cuda")
+    x = torch.zeros_like(b)
+
+    def call(out):
+        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        _ffi.check(lib.gbchol_solve_noalloc(s.handle, 0, nrhs, C.c_void_p(b.data_ptr()),
+                                            C.c_void_p(out.data_ptr()), stream))
+
+    call(x)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        call(x)
+    for seed in range(2):
+        gen = torch.Generator(device="cuda").manual_seed(seed)
+        b.copy_(torch.randn(n, nrhs, device="cuda", generator=gen))
+        x.zero_()
+        g.replay()
+        x_ref = torch.zeros_like(b)
+        _ffi.check(lib.gbchol_solve(s.handle, 0, nrhs, C.c_void_p(b.data_ptr()),
+                                    C.c_void_p(x_ref.data_ptr()),
+                                    C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        torch.cuda.synchronize()
+        _ffi.check(lib.gbchol_check(s.handle))
+        err = ((x - x_ref).abs().max() / x_ref.abs().max()).item()
+        assert err <= 1e-5, err
