@@ -39,3 +39,32 @@ def sym_matrix(n, vals, idx):
     A.sum_duplicates()
     low = sp.tril(A)
     return (low + sp.tril(low, -1).T).tocsr()
+
+
+STRUCTURES = ["forest", "star", "diagonal", "one", "dense96"]
+
+
+def structural_cases():
+    """Matrices whose elimination structure is unusual, as scipy COO (both
+    triangles): a forest of 40 disconnected grids of different sizes (many
+    elimination-tree roots), a star (one row coupled to every other), a
+    diagonal matrix (no dependencies), a 1 x 1 system, and a dense 96 x 96
+    SPD block (one supernode of three 32-column chunks). All are
+    well conditioned (condition numbers below 100)."""
+    import scipy.sparse as sp
+    blocks = []
+    for k in range(40):
+        m = 5 + (k * 7) % 23
+        vals, idx = workloads.grid2d_coo(m, 10.0, 1.0)
+        blocks.append(sp.coo_matrix((vals, idx), shape=(m * m, m * m)).tocsr())
+    forest = sp.block_diag(blocks).tocoo()
+    n = 3000
+    rows = np.r_[np.arange(n), np.arange(1, n)]
+    cols = np.r_[np.arange(n), np.zeros(n - 1, int)]
+    vals = np.r_[np.full(n, 4.0), np.full(n - 1, -1.0 / np.sqrt(n))]
+    star = sp.coo_matrix((vals, (rows, cols)), shape=(n, n))
+    star = (star + sp.tril(star, -1).T).tocoo()
+    g = np.random.default_rng(96).standard_normal((96, 96))
+    dense = sp.coo_matrix(g @ g.T / 96 + 2.0 * np.eye(96))
+    return {"forest": forest, "star": star, "diagonal": (sp.identity(500) * 3.0).tocoo(),
+            "one": sp.coo_matrix(np.array([[2.5]])), "dense96": dense}

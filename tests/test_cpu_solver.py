@@ -13,7 +13,7 @@ import pytest
 
 import oracle
 from cholespy_gb300 import _ffi, workloads
-from helpers import RHS, reference_problem, spsolve_ref
+from helpers import RHS, STRUCTURES, reference_problem, spsolve_ref, structural_cases
 
 
 def _solver_cls(variant):
@@ -241,29 +241,13 @@ def test_cpu_solver_refactorize_and_factor(gblib):
     np.testing.assert_allclose(x, spsolve_ref(n, vals2, idx, b), rtol=1e-10, atol=1e-12)
 
 
-def _structural_cases():
-    import scipy.sparse as sp
-    blocks = []
-    for k in range(40):  # a forest: 40 disconnected grids of different sizes
-        m = 5 + (k * 7) % 23
-        vals, idx = workloads.grid2d_coo(m, 10.0, 1.0)
-        blocks.append(sp.coo_matrix((vals, idx), shape=(m * m, m * m)).tocsr())
-    forest = sp.block_diag(blocks).tocoo()
-    n = 3000  # a star: one row coupled to every other
-    rows = np.r_[np.arange(n), np.arange(1, n)]
-    cols = np.r_[np.arange(n), np.zeros(n - 1, int)]
-    vals = np.r_[np.full(n, 4.0), np.full(n - 1, -1.0 / np.sqrt(n))]
-    star = sp.coo_matrix((vals, (rows, cols)), shape=(n, n))
-    star = (star + sp.tril(star, -1).T).tocoo()
-    return {"forest": forest, "star": star, "diagonal": (sp.identity(500) * 3.0).tocoo()}
-
-
-@pytest.mark.parametrize("case", ["forest", "star", "diagonal"])
+@pytest.mark.parametrize("case", list(STRUCTURES))
 def test_host_solve_structures(gblib, case):
-    """Elimination forests (several roots), a dense row and no off-diagonal
-    entries: solutions vs spsolve, bit-identical for 1 and all threads."""
+    """Elimination forests (several roots), a dense row, no off-diagonal
+    entries, a 1 x 1 system and a dense block: solutions vs spsolve,
+    bit-identical for 1 and all threads."""
     from scipy.sparse.linalg import spsolve
-    A = _structural_cases()[case]
+    A = structural_cases()[case]
     n = A.shape[0]
     f, _ = _factorize(gblib, n, A.data, (A.row, A.col))
     try:
